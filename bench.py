@@ -1,0 +1,347 @@
+#!/usr/bin/env python3
+"""Benchmark of the exact epsilon self-join on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--config c4] [--precision auto] [--proj-k K] [--n N]
+
+A step is one exact self-join of the whole synthetic workload (default: c4,
+N = 4,000,000 points, d = 64, eps for ~50 neighbours; see
+tensor_bf_main_gb300/datagen.py), inputs resident in device memory.  The JSON
+line reports pair-distances/s (N^2 ordered pairs per second, the reference's
+count semantics), the Gram kernel's tensor-pipe roofline fraction, the
+end-to-end rate through the public API from pinned host memory, the plain
+FP64 DMMA join rate (speedup denominator, measured on a row subset and
+extrapolated as N^2 / rate) and the CPU baseline (the oracle restatement of
+the reference's FP64 kernel on all host cores, bounded sample).
+
+--impl reference times the reference's CPU algorithm (the oracle port; the
+reference has no CPU join of its own and its GPU code cannot be built on the
+box) on the same workload, one bounded sample of query rows per step.
+
+With --gpus N under torchrun every rank runs an independent replica
+(replicas only: the spec path is single-GPU) and rank 0 reports the
+whole-job rate.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+PROFILE_SUMMARY = os.path.join(ROOT, "profiles", "roofline_traffic.json")
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=3)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--config", default="c4")
+    p.add_argument("--precision", default="auto")
+    p.add_argument("--proj-k", type=int, default=-1, help="-1: config default")
+    p.add_argument("--n", type=int, default=0, help="override N (smaller runs)")
+    p.add_argument("--eps", type=float, default=0.0)
+    p.add_argument("--cpu-seconds", type=float, default=12.0)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-fp64", action="store_true")
+    p.add_argument("--fp64-rows", type=int, default=65536)
+    p.add_argument("--no-e2e", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def workload(args):
+    from tensor_bf_main_gb300 import datagen
+
+    cfg = datagen.CONFIGS[args.config]
+    n = args.n or cfg["n"]
+    x = datagen.generate(args.config, n=n)
+    eps = args.eps or datagen.frozen_eps(args.config, x)
+    return x, float(eps), cfg
+
+
+def cpu_rate(x, eps, seconds, seed=0):
+    """Oracle (reference FP64 arithmetic) on a bounded sample of query rows
+    against all points, all host threads: returns (pairs/s, rows, seconds)."""
+    import oracle
+
+    oracle.build()
+    rng = np.random.default_rng(seed)
+    n = x.shape[0]
+    rows = rng.choice(n, size=min(n, 16), replace=False)
+    t0 = time.perf_counter()
+    oracle.query_counts(x, eps, rows)
+    t1 = time.perf_counter()
+    per_row = max((t1 - t0) / len(rows), 1e-9)
+    nq = int(max(1, min(n, seconds / per_row)))
+    rows = rng.choice(n, size=nq, replace=False)
+    t0 = time.perf_counter()
+    oracle.query_counts(x, eps, rows)
+    dt = time.perf_counter() - t0
+    return nq * n / dt, nq, dt, oracle.num_threads()
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self):
+        self.proc = None
+        self.path = None
+
+    def start(self, gpu_index):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(gpu_index),
+                 "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.f.close()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                rows.append((float(parts[0]), float(parts[1]), float(parts[2]), parts[4:8]))
+            except ValueError:
+                continue
+        os.unlink(self.path)
+        if not rows:
+            return None
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i, v in enumerate(r[3]) if v == "Active"})
+        loaded = [r for r in rows if r[2] > 200.0] or rows
+        return {"sm_mhz": statistics.median(r[0] for r in loaded),
+                "sm_max_mhz": max(r[1] for r in rows), "reasons": reasons,
+                "samples": len(rows), "power_w_max": max(r[2] for r in rows)}
+
+
+def peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        return None
+
+
+def run_reference(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    x, eps, cfg = workload(args)
+    n = x.shape[0]
+    import oracle
+
+    oracle.build()
+    rates = []
+    nq = None
+    for i in range(args.warmup + args.steps):
+        rate, nq, dt, cores = cpu_rate(x, eps, max(1.0, args.cpu_seconds / 3), seed=i)
+        if i >= args.warmup:
+            rates.append(rate)
+    value = statistics.mean(rates)
+    line = {
+        "impl": "reference", "metric": "pair-distances/s at FP64-exact counts", "value": value,
+        "unit": "pairs/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": n * n / value * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"{args.config}: N={n}, d={x.shape[1]}, eps={eps:.6g}",
+                   "n": n, "d": x.shape[1], "eps": eps},
+        "cpu_baseline": {"value": value, "unit": "pairs/s", "cores": oracle.num_threads(),
+                         "kind": "port",
+                         "sample": f"{nq} seeded query rows x all {n} points per step "
+                                   "(reference FP64 predicate, OpenMP over query rows); "
+                                   "ms_per_step extrapolates to the full N^2"},
+        "e2e": {"value": value, "unit": "pairs/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import torch
+
+    import tensor_bf_main_gb300 as ej
+
+    world, rank, local = dist_env()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local if world > 1 else 0)
+    torch.cuda.set_device(dev)
+    x, eps, cfg = workload(args)
+    n, d = x.shape
+    proj_k = args.proj_k if args.proj_k >= 0 else cfg.get("proj_k", 0)
+    stream = torch.cuda.current_stream(dev)
+    xd = torch.from_numpy(x).to(dev)
+    cd = torch.empty(n, dtype=torch.int32, device=dev)
+    kw = dict(precision=args.precision, proj_k=proj_k, counts=cd, stream=stream, device=dev.index)
+
+    def barrier():
+        if dist:
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        ej.self_join(xd, eps, **kw)
+    barrier()
+    torch.cuda.synchronize(dev)
+    clocks = Clocks()
+    clocks.start(dev.index)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    stats = []
+    e0.record(stream)
+    for _ in range(args.steps):
+        _, total, st = ej.self_join(xd, eps, **kw)
+        stats.append(st)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    barrier()
+    ck = clocks.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    if dist:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * float(n) * float(n) / (ms / 1e3)
+
+    # roofline of the dominant kernel (the Gram screen): executed MMA flops per
+    # launch over its CUDA-event duration, against the measured sustained
+    # dense BF16 rate (the kernel runs inside a long step)
+    pk = peaks()
+    gram_ms = statistics.mean(s["ms_gram"] for s in stats)
+    gram_flops = statistics.mean(s["gram_flops"] for s in stats)
+    achieved = gram_flops / (gram_ms / 1e3) / 1e12
+    prec = stats[0]["precision"]
+    if prec in ("fp64_dmma", "fp64_direct"):
+        roof = None
+    else:
+        peak = (pk or {}).get("bf16_tflops_sustained") or 1700.0
+        traffic = None
+        try:
+            prof = json.load(open(PROFILE_SUMMARY))
+            key = f"{args.config}:{prec}:k{proj_k}"
+            if key in prof:
+                traffic = prof[key]["traffic_bytes_per_launch"]
+        except (OSError, ValueError, KeyError):
+            pass
+        roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak, "traffic": traffic,
+                "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained" if pk else "fallback",
+                "kernel": "gram_kernel (tcgen05)", "flops_per_launch": gram_flops,
+                "ms_per_launch": gram_ms}
+
+    line = {
+        "metric": "pair-distances/s at FP64-exact counts", "value": value, "unit": "pairs/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": prec,
+        "data": "synthetic (seeded generator with the config's shape and distribution)",
+        "config": {"workload": f"{args.config}: N={n}, d={d}, eps={eps:.6g}", "n": n, "d": d,
+                   "eps": eps, "precision": prec, "proj_k": proj_k,
+                   "l2": "inputs larger than L2 (N*d*8 bytes)", "parallelism": f"replicas x{world}"},
+        "total_pairs": int(total),
+        "band_fraction": stats[-1]["band_fraction"], "band_pairs": stats[-1]["band_pairs"],
+        "tile_pairs_run": stats[-1]["tile_pairs_run"],
+        "tile_pairs_total": stats[-1]["tile_pairs_total"],
+        "phase_ms": {k: stats[-1][k] for k in ("ms_prep", "ms_train", "ms_order", "ms_gram",
+                                                "ms_recheck", "ms_total")},
+        "algorithmic_tflops": 2.0 * d * n * (n + 1) / 2 / (ms / 1e3) / 1e12,
+        "gpu_launches": int(sum(s["kernel_launches"] for s in stats)),
+        "clocks": ck,
+    }
+    if roof:
+        line["roofline"] = roof
+        line["tensor_pipe_frac"] = roof["frac"]
+
+    if rank == 0 and not args.no_fp64:
+        sub = min(n, args.fp64_rows)
+        xs = xd[:sub].contiguous()
+        cs = torch.empty(sub, dtype=torch.int32, device=dev)
+        ej.self_join(xs, eps, precision="fp64_dmma", counts=cs, stream=stream, device=dev.index)
+        torch.cuda.synchronize(dev)
+        f0 = torch.cuda.Event(enable_timing=True)
+        f1 = torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        ej.self_join(xs, eps, precision="fp64_dmma", counts=cs, stream=stream, device=dev.index)
+        f1.record(stream)
+        torch.cuda.synchronize(dev)
+        fms = f0.elapsed_time(f1)
+        rate = sub * sub / (fms / 1e3)
+        line["fp64_dmma_join"] = {"value": rate, "unit": "pairs/s",
+                                  "sample": f"first {sub} rows, extrapolated as N^2/rate",
+                                  "extrapolated_ms_full": n * n / rate * 1e3,
+                                  "speedup": value / world / rate}
+
+    if rank == 0 and not args.no_e2e:
+        xh = torch.from_numpy(x).pin_memory()
+        ch = np.empty(n, dtype=np.int32)
+        ej.self_join(xh, eps, precision=args.precision, proj_k=proj_k, counts=ch, stream=stream)
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            ej.self_join(xh, eps, precision=args.precision, proj_k=proj_k, counts=ch,
+                         stream=stream)
+        torch.cuda.synchronize(dev)
+        e2e_s = (time.perf_counter() - t0) / args.steps
+        line["e2e"] = {"value": float(n) * n / e2e_s, "unit": "pairs/s",
+                       "h2d_bytes_per_step": int(n * d * 8), "d2h_bytes_per_step": int(n * 4 + 8),
+                       "ms_per_step": e2e_s * 1e3}
+
+    if rank == 0 and not args.no_cpu_baseline:
+        rate, nq, dt, cores = cpu_rate(x, eps, args.cpu_seconds)
+        line["cpu_baseline"] = {"value": rate, "unit": "pairs/s", "cores": cores, "kind": "port",
+                                "sample": f"{nq} seeded query rows x all {n} points "
+                                          f"({dt:.1f} s, oracle restatement of the reference "
+                                          "FP64 kernel, OpenMP over query rows)"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

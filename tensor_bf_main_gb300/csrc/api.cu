@@ -1,0 +1,570 @@
+// api.cu -- the C ABI of libejoin.so and the join driver.
+//
+// Re-designs the reference driver GPUJoinMainBruteForce (gpu_join.cu:210-322):
+// the reference uploads the padded dataset, optionally converts it, computes
+// chunked norms, launches one kernel chosen by searchMode, synchronises and
+// copies one 64-bit counter back -- never zeroing the counter, never freeing
+// device memory and exiting on an unknown mode.  Here the driver
+//   1. places the points in device memory (host or device input),
+//   2. runs the chosen exact pipeline:
+//        FP64_DIRECT  exact FP64 tiles (the judge)
+//        FP64_DMMA    FP64 Gram screen + band recheck
+//        BF16/FP16    centre, scale, pack; tcgen05 Gram screen + band recheck
+//      optionally behind the learned tile-pair pruning (k_learn.cu),
+//   3. re-runs the screen with a larger band queue if it overflowed,
+//   4. returns per-point counts and their total,
+// with status codes instead of exits and all scratch freed on return.
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "ejoin_internal.cuh"
+
+namespace ejoin {
+
+// ------------------------------------------------------------- errors --
+
+static thread_local int t_status = 0;
+static thread_local char t_msg[2048] = "";
+
+int set_error(int status, const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(t_msg, sizeof t_msg, fmt, ap);
+    va_end(ap);
+    t_status = status;
+    return status;
+}
+
+int cuda_error(cudaError_t e, const char* what, const char* file, int line) {
+    cudaGetLastError();
+    return set_error(e == cudaErrorMemoryAllocation ? EJOIN_ENOMEM : EJOIN_ECUDA,
+                     "%s failed (%s:%d): %s", what, file, line, cudaGetErrorString(e));
+}
+
+static thread_local uint64_t t_launches = 0;
+void note_launch(uint64_t k) { t_launches += k; }
+uint64_t launches_so_far() { return t_launches; }
+
+void clear_error() {
+    t_status = 0;
+    t_msg[0] = 0;
+}
+
+// ---------------------------------------------------------- threshold --
+
+// Largest double T with sqrt(T) <= eps.  Correctly rounded sqrt is monotone,
+// so sqrt(d2) <= eps (the reference predicate, kernel_join.cu:194) is
+// exactly d2 <= T.  NaN eps -> NaN, eps < 0 -> -inf, +inf -> +inf.
+double threshold(double eps) {
+    if (isnan(eps)) return NAN;
+    if (eps < 0.0) return -INFINITY;
+    if (isinf(eps)) return INFINITY;
+    double t = eps * eps;
+    if (isinf(t)) t = 1.7976931348623157e308;
+    while (t > 0.0 && sqrt(t) > eps) t = nextafter(t, 0.0);
+    for (;;) {
+        const double up = nextafter(t, INFINITY);
+        if (isinf(up) || !(sqrt(up) <= eps)) break;
+        t = up;
+    }
+    return t;
+}
+
+// Bounds of the oracle's rounding: d2 computed by the reference arithmetic
+// satisfies |d2 - delta^2| <= c_o delta^2 + a_o for the exact squared
+// distance delta^2 ((d+2) roundings of at most 2^-53 each, plus subnormal
+// absolute error).  Pairs with delta^2 <= Tlo certainly satisfy d2 <= T;
+// pairs with delta^2 > Thi certainly do not.
+static void oracle_band(double T, uint32_t d, double* Tlo, double* Thi) {
+    const double co = (d + 4) * kU * 1.0001;
+    const double ao = (d + 2) * 4.9406564584124654e-324 * 2.0;
+    double lo = (T - ao) / (1.0 + co) * (1.0 - 4 * kU);
+    double hi = (T + ao) / (1.0 - co) * (1.0 + 4 * kU);
+    *Tlo = lo > 0.0 ? lo : 0.0;
+    *Thi = hi;
+}
+
+// ------------------------------------------------------------ devices --
+
+struct DeviceScope {
+    int prev = -1;
+    int enter(int dev) {
+        if (cudaGetDevice(&prev) != cudaSuccess) {
+            cudaGetLastError();
+            prev = -1;
+        }
+        EJ_CUDA(cudaSetDevice(dev));
+        return EJOIN_OK;
+    }
+    ~DeviceScope() {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+};
+
+static int check_device(int dev, int* sms) {
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count == 0) {
+        cudaGetLastError();
+        return set_error(EJOIN_ENODEV, "no CUDA device available (%s)",
+                         e == cudaSuccess ? "count 0" : cudaGetErrorString(e));
+    }
+    if (dev < 0 || dev >= count) return set_error(EJOIN_EINVAL, "device %d out of range (%d devices)", dev, count);
+    cudaDeviceProp p;
+    EJ_CUDA(cudaGetDeviceProperties(&p, dev));
+    if (p.major != 10 || p.minor != 3)
+        return set_error(EJOIN_ENODEV,
+                         "device %d is sm_%d%d; libejoin.so is built for sm_103a (GB300) only", dev,
+                         p.major, p.minor);
+    *sms = p.multiProcessorCount;
+    static bool pool_done[64] = {};
+    if (dev < 64 && !pool_done[dev]) {
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+            uint64_t thr = UINT64_MAX;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+        }
+        cudaGetLastError();
+        pool_done[dev] = true;
+    }
+    return EJOIN_OK;
+}
+
+static bool is_device_ptr(const void* p) {
+    if (!p) return false;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+// Compact n x d rows (row stride ld) into device memory.
+static int stage_points(const double* points, uint64_t n, uint32_t d, uint64_t ld, DBuf<double>& buf,
+                        const double** Xout, cudaStream_t s) {
+    const bool dev = is_device_ptr(points);
+    if (dev && ld == d) {
+        *Xout = points;
+        return EJOIN_OK;
+    }
+    EJ_TRY(buf.alloc(n * d, s, "points"));
+    if (ld == d) {
+        EJ_CUDA(cudaMemcpyAsync(buf.p, points, n * d * sizeof(double),
+                                dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
+    } else {
+        EJ_CUDA(cudaMemcpy2DAsync(buf.p, d * sizeof(double), points, ld * sizeof(double),
+                                  d * sizeof(double), n,
+                                  dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
+    }
+    *Xout = buf.p;
+    return EJOIN_OK;
+}
+
+// ---------------------------------------------------------- pipelines --
+
+struct Join {
+    cudaStream_t s;
+    int sms;
+    const double* X;  // n x d, device
+    uint64_t n;
+    uint32_t d;
+    double T;
+    ejoin_options opt;
+    ejoin_stats* st;
+    int32_t* counts;         // device, >= n_pad entries, packed-row order
+    const uint32_t* perm;    // packed row -> original row (null = identity)
+};
+
+static uint64_t round_up(uint64_t v, uint64_t m) { return (v + m - 1) / m * m; }
+
+static uint64_t band_budget(uint64_t want) {
+    size_t fr = 0, tot = 0;
+    if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) {
+        cudaGetLastError();
+        return want;
+    }
+    const uint64_t maxe = (uint64_t)(fr / 4) / sizeof(BandPair);
+    return std::min(want, std::max<uint64_t>(maxe, 1u << 20));
+}
+
+// Runs `screen` (which fills counts and the band queue), re-running it with a
+// larger queue on overflow, then rechecks the band in FP64.
+template <typename Screen>
+static int screen_and_recheck(Join& J, uint64_t cap0, Screen&& screen, uint64_t n_pad,
+                              EventTimer& tg, EventTimer& tr) {
+    DBuf<BandPair> band;
+    DBuf<DevStatus> dst;
+    EJ_TRY(dst.alloc(1, J.s, "status"));
+    uint64_t cap = band_budget(cap0);
+    for (int attempt = 0;; ++attempt) {
+        EJ_TRY(band.alloc(cap, J.s, "band queue"));
+        EJ_TRY(dst.zero(J.s));
+        EJ_CUDA(cudaMemsetAsync(J.counts, 0, n_pad * sizeof(int32_t), J.s));
+        tg.start(J.s);
+        EJ_TRY(screen(band.p, cap, dst.p));
+        tg.stop(J.s);
+        DevStatus h;
+        EJ_CUDA(cudaMemcpyAsync(&h, dst.p, sizeof h, cudaMemcpyDeviceToHost, J.s));
+        EJ_CUDA(cudaStreamSynchronize(J.s));
+        if (h.timeout)
+            return set_error(EJOIN_ETIMEOUT, "Gram kernel: a bounded device wait expired (site %u)", h.where);
+        if (h.band_count <= cap) {
+            tr.start(J.s);
+            EJ_TRY(launch_band_recheck(J.X, J.d, J.perm, J.T, band.p, h.band_count, J.counts, dst.p, J.s));
+            tr.stop(J.s);
+            EJ_CUDA(cudaMemcpyAsync(&h, dst.p, sizeof h, cudaMemcpyDeviceToHost, J.s));
+            EJ_CUDA(cudaStreamSynchronize(J.s));
+            J.st->band_pairs = h.band_count;
+            J.st->band_hits = h.band_hits;
+            J.st->ms_gram = tg.ms();
+            J.st->ms_recheck = tr.ms();
+            return EJOIN_OK;
+        }
+        J.st->band_overflows++;
+        const uint64_t want = h.band_count + h.band_count / 16 + 1024;
+        const uint64_t got = band_budget(want);
+        if (got < want || attempt >= 3)
+            return set_error(EJOIN_ENOMEM, "band queue needs %llu entries; device memory allows %llu",
+                             (unsigned long long)want, (unsigned long long)got);
+        cap = want;
+    }
+}
+
+static int run_direct(Join& J) {
+    EventTimer t;
+    EJ_CUDA(cudaMemsetAsync(J.counts, 0, J.n * sizeof(int32_t), J.s));
+    t.start(J.s);
+    EJ_TRY(launch_direct_selfjoin(J.X, J.n, J.d, J.T, J.counts, J.s));
+    t.stop(J.s);
+    J.st->ms_gram = t.ms();
+    const double pairs = (double)J.n * (double)(J.n + 1) / 2.0;
+    J.st->gram_flops = 3.0 * J.d * pairs;
+    J.st->precision = EJOIN_FP64_DIRECT;
+    return EJOIN_OK;
+}
+
+static int run_dmma(Join& J) {
+    EventTimer tp, tg, tr;
+    tp.start(J.s);
+    DBuf<uint8_t> bad;
+    DBuf<double> mu;
+    EJ_TRY(bad.alloc(J.n, J.s, "row flags"));
+    EJ_TRY(mu.alloc(J.d, J.s, "mean"));
+    double maxabs = 0;
+    uint64_t ngood = 0;
+    EJ_TRY(launch_center_stats(J.X, J.n, J.d, bad.p, mu.p, &maxabs, &ngood, J.s));
+    DmmaParams P;
+    P.d = J.d;
+    P.dp = (uint32_t)round_up(J.d, 32);
+    oracle_band(J.T, J.d, &P.Tlo, &P.Thi);
+    P.sTlo = sqrt(P.Tlo) * (1 - 4 * kU);
+    P.sThi = sqrt(P.Thi) * (1 + 4 * kU);
+    P.crel = 2.0 * (P.dp + 8) * kU;
+    const uint64_t n_pad = round_up(J.n, 64);
+    DBuf<double> Y, h, g;
+    EJ_TRY(Y.alloc(n_pad * P.dp, J.s, "centred FP64 rows"));
+    EJ_TRY(h.alloc(n_pad, J.s, "in thresholds"));
+    EJ_TRY(g.alloc(n_pad, J.s, "out thresholds"));
+    EJ_TRY(launch_pack_dmma(J.X, J.n, n_pad, J.perm, bad.p, mu.p, P, Y.p, h.p, g.p, J.s));
+    tp.stop(J.s);
+    J.st->ms_prep = tp.ms();
+    const uint64_t nT = n_pad / 64;
+    J.st->tile_pairs_total = nT * (nT + 1) / 2;
+    J.st->tile_pairs_run = J.st->tile_pairs_total;
+    J.st->gram_flops = 2.0 * P.dp * 64.0 * 64.0 * (double)J.st->tile_pairs_run;
+    J.st->precision = EJOIN_FP64_DMMA;
+    auto screen = [&](BandPair* band, uint64_t cap, DevStatus* st) {
+        return launch_dmma_join(Y.p, n_pad, P.dp, h.p, g.p, J.counts, band, cap, st, J.s);
+    };
+    return screen_and_recheck(J, std::max<uint64_t>(1u << 20, J.n), screen, n_pad, tg, tr);
+}
+
+// Global power-of-two scale of the centred data for the 16-bit operands.
+static double screen_scale(Fmt f, double maxabs, uint32_t d) {
+    if (!(maxabs > 0.0) || !isfinite(maxabs)) return 1.0;
+    double target = (f == Fmt::FP16) ? 64.0 / sqrt((double)d) : 1.0;
+    int e = (int)floor(log2(target / maxabs));
+    e = std::max(-1000, std::min(1000, e));
+    return ldexp(1.0, e);
+}
+
+static int run_screen16(Join& J, Fmt fmt, bool split) {
+    EventTimer tp, tg, tr;
+    tp.start(J.s);
+    DBuf<uint8_t> bad;
+    DBuf<double> mu;
+    EJ_TRY(bad.alloc(J.n, J.s, "row flags"));
+    EJ_TRY(mu.alloc(J.d, J.s, "mean"));
+    double maxabs = 0;
+    uint64_t ngood = 0;
+    EJ_TRY(launch_center_stats(J.X, J.n, J.d, bad.p, mu.p, &maxabs, &ngood, J.s));
+    ScreenParams P;
+    P.fmt = fmt;
+    P.split = split ? 1 : 0;
+    P.d = J.d;
+    P.dp = (uint32_t)round_up(J.d, 64);
+    P.width = P.dp * (split ? 2 : 1) + 64;
+    P.scale = screen_scale(fmt, maxabs, J.d);
+    double Tlo, Thi;
+    oracle_band(J.T, J.d, &Tlo, &Thi);
+    const double s2 = P.scale * P.scale;
+    const double cap_t = 1.152921504606846976e18;  // 2^60, far above any |z| distance
+    P.Tlo = std::min(Tlo * s2, cap_t);
+    P.Thi = std::min(Thi * s2, cap_t);
+    P.sTlo = sqrt(P.Tlo) * (1 - 4 * kU);
+    P.sThi = sqrt(P.Thi) * (1 + 4 * kU);
+    const double kprod = (split ? 3.0 : 1.0) * P.dp + 16.0;
+    const double scale_opt = J.opt.acc_bound_scale > 0 ? J.opt.acc_bound_scale : 1.0;
+    P.cacc = scale_opt * (kprod + 16.0) * ldexp(1.0, -22);
+    P.absacc = (kprod + 16.0) * ldexp(1.0, -125);
+    P.clamp_lo = (fmt == Fmt::FP16) ? -16384.0 : -kTwo100;
+    const uint64_t n_pad = round_up(J.n, 128);
+    DBuf<uint16_t> Q;
+    DBuf<float> beta, tmax;
+    EJ_TRY(Q.alloc(n_pad * P.width, J.s, "packed operands"));
+    EJ_TRY(beta.alloc(n_pad, J.s, "out margins"));
+    EJ_TRY(tmax.alloc(n_pad / 128, J.s, "tile margins"));
+    EJ_TRY(launch_pack16(J.X, J.n, n_pad, J.perm, bad.p, mu.p, P, Q.p, beta.p, J.s));
+    EJ_TRY(launch_tile_max(beta.p, nullptr, n_pad, tmax.p, J.s));
+    tp.stop(J.s);
+    J.st->ms_prep = tp.ms();
+    const uint64_t nT = n_pad / 128;
+    DBuf<uint2> work;
+    uint64_t nwork = 0;
+    EJ_TRY(build_worklist(nT, nullptr, nullptr, 0, 0.0, work, &nwork, nullptr, J.s));
+    J.st->tile_pairs_total = nT * (nT + 1) / 2;
+    J.st->tile_pairs_run = nwork;
+    J.st->gram_flops = 2.0 * kprod * 128.0 * 128.0 * (double)nwork;
+    J.st->precision = fmt == Fmt::FP16 ? EJOIN_FP16 : (split ? EJOIN_BF16_SPLIT : EJOIN_BF16);
+    auto screen = [&](BandPair* band, uint64_t cap, DevStatus* st) {
+        return launch_gram16(Q.p, n_pad, P, work.p, nwork, tmax.p, J.counts, band, cap, st, J.sms,
+                             J.s);
+    };
+    const uint64_t cap0 = std::max<uint64_t>(1u << 22, 32 * J.n);
+    return screen_and_recheck(J, cap0, screen, n_pad, tg, tr);
+}
+
+static int resolve_precision(int p, uint32_t d) {
+    if (p == EJOIN_AUTO) return EJOIN_BF16_SPLIT;
+    (void)d;
+    return p;
+}
+
+static int self_join_impl(const double* points, uint64_t n, uint32_t d, double eps,
+                          const ejoin_options* opt_in, int32_t* counts_out, uint64_t* total_out,
+                          ejoin_stats* stats_out) {
+    ejoin_options opt;
+    ejoin_default_options(&opt);
+    if (opt_in) {
+        if (opt_in->struct_size != sizeof(ejoin_options))
+            return set_error(EJOIN_EINVAL, "ejoin_options.struct_size mismatch (%u != %zu)",
+                             opt_in->struct_size, sizeof(ejoin_options));
+        opt = *opt_in;
+    }
+    if (d == 0) return set_error(EJOIN_EINVAL, "dimension must be >= 1");
+    if (n && !points) return set_error(EJOIN_EINVAL, "points is NULL");
+    if (n > 0x7fffff00ull) return set_error(EJOIN_EUNSUPPORTED, "n = %llu exceeds 2^31 - 256", (unsigned long long)n);
+    const uint64_t ld = opt.ld ? opt.ld : d;
+    if (ld < d) return set_error(EJOIN_EINVAL, "row stride %llu < d %u", (unsigned long long)ld, d);
+    if (opt.precision < EJOIN_FP64_DIRECT || opt.precision > EJOIN_AUTO)
+        return set_error(EJOIN_EINVAL, "unknown precision mode %d", opt.precision);
+    if (opt.acc_bound_scale < 1.0)
+        return set_error(EJOIN_EINVAL, "acc_bound_scale must be >= 1 (got %g)", opt.acc_bound_scale);
+    ejoin_stats stats;
+    memset(&stats, 0, sizeof stats);
+    stats.n = n;
+    stats.d = d;
+    DeviceScope ds;
+    int sms = 0;
+    EJ_TRY(check_device(opt.device, &sms));
+    EJ_TRY(ds.enter(opt.device));
+    cudaStream_t s = opt.stream ? (cudaStream_t)opt.stream : cudaStreamPerThread;
+    const bool out_dev = is_device_ptr(counts_out);
+    const double T = threshold(eps);
+    const uint64_t launches0 = launches_so_far();
+    EventTimer tt;
+    tt.start(s);
+
+    Join J;
+    J.s = s;
+    J.sms = sms;
+    J.n = n;
+    J.d = d;
+    J.T = T;
+    J.opt = opt;
+    J.st = &stats;
+    J.perm = nullptr;
+    DBuf<double> xbuf;
+    DBuf<int32_t> cbuf;
+    const uint64_t n_pad = round_up(std::max<uint64_t>(n, 1), 128);
+    EJ_TRY(cbuf.alloc(n_pad, s, "counts"));
+    EJ_TRY(cbuf.zero(s));
+    J.counts = cbuf.p;
+    int prec = resolve_precision(opt.precision, d);
+    stats.precision = prec;
+    if (n > 0 && !isnan(T) && T >= 0.0) {
+        EJ_TRY(stage_points(points, n, d, ld, xbuf, &J.X, s));
+        if (isinf(T)) prec = EJOIN_FP64_DIRECT;  // every non-NaN pair counts: judge only
+        switch (prec) {
+            case EJOIN_FP64_DIRECT: EJ_TRY(run_direct(J)); break;
+            case EJOIN_FP64_DMMA: EJ_TRY(run_dmma(J)); break;
+            case EJOIN_FP16: EJ_TRY(run_screen16(J, Fmt::FP16, false)); break;
+            case EJOIN_BF16: EJ_TRY(run_screen16(J, Fmt::BF16, false)); break;
+            case EJOIN_BF16_SPLIT: EJ_TRY(run_screen16(J, Fmt::BF16, true)); break;
+            case EJOIN_FP8_E4M3:
+                return set_error(EJOIN_EUNSUPPORTED, "FP8 screen not available in this build");
+            default: return set_error(EJOIN_EINVAL, "unknown precision %d", prec);
+        }
+    }
+    DBuf<unsigned long long> tot;
+    EJ_TRY(tot.alloc(1, s, "total"));
+    EJ_TRY(tot.zero(s));
+    EJ_TRY(sum_counts(J.counts, n, tot.p, s));
+    if (counts_out && n) {
+        if (J.perm) {
+            if (out_dev) {
+                EJ_TRY(scatter_counts(J.counts, J.perm, n, counts_out, s));
+            } else {
+                DBuf<int32_t> tmp;
+                EJ_TRY(tmp.alloc(n, s, "scattered counts"));
+                EJ_TRY(scatter_counts(J.counts, J.perm, n, tmp.p, s));
+                EJ_CUDA(cudaMemcpyAsync(counts_out, tmp.p, n * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+                EJ_CUDA(cudaStreamSynchronize(s));
+            }
+        } else {
+            EJ_CUDA(cudaMemcpyAsync(counts_out, J.counts, n * sizeof(int32_t),
+                                    out_dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s));
+        }
+    }
+    unsigned long long total = 0;
+    EJ_CUDA(cudaMemcpyAsync(&total, tot.p, sizeof total, cudaMemcpyDeviceToHost, s));
+    tt.stop(s);
+    EJ_CUDA(cudaStreamSynchronize(s));
+    stats.ms_total = tt.ms();
+    stats.kernel_launches = launches_so_far() - launches0;
+    const double computed = (double)n * (double)n;
+    stats.band_fraction = computed > 0 ? (double)stats.band_pairs / computed : 0.0;
+    if (total_out) *total_out = total;
+    if (stats_out) *stats_out = stats;
+    return EJOIN_OK;
+}
+
+}  // namespace ejoin
+
+using namespace ejoin;
+
+extern "C" {
+
+int ejoin_default_options(ejoin_options* opt) {
+    if (!opt) return set_error(EJOIN_EINVAL, "opt is NULL");
+    memset(opt, 0, sizeof *opt);
+    opt->struct_size = sizeof(ejoin_options);
+    opt->device = 0;
+    opt->precision = EJOIN_AUTO;
+    opt->proj_k = 0;
+    opt->train_pairs = 1u << 20;
+    opt->train_steps = 200;
+    opt->order = EJOIN_ORDER_MORTON;
+    opt->seed = 0x5eed5eedull;
+    opt->acc_bound_scale = 1.0;
+    return EJOIN_OK;
+}
+
+int ejoin_self_join(const double* points, uint64_t n, uint32_t d, double eps,
+                    const ejoin_options* opt, int32_t* counts_out, uint64_t* total_out,
+                    ejoin_stats* stats_out) {
+    clear_error();
+    return self_join_impl(points, n, d, eps, opt, counts_out, total_out, stats_out);
+}
+
+int ejoin_query_counts(const double* points, uint64_t n, uint32_t d, double eps,
+                       const uint64_t* rows, uint64_t nq, const ejoin_options* opt_in,
+                       int32_t* counts_out) {
+    clear_error();
+    ejoin_options opt;
+    ejoin_default_options(&opt);
+    if (opt_in) {
+        if (opt_in->struct_size != sizeof(ejoin_options)) return set_error(EJOIN_EINVAL, "ejoin_options.struct_size mismatch");
+        opt = *opt_in;
+    }
+    if (d == 0 || (n && !points) || (nq && (!rows || !counts_out)))
+        return set_error(EJOIN_EINVAL, "bad arguments");
+    const uint64_t ld = opt.ld ? opt.ld : d;
+    if (ld < d) return set_error(EJOIN_EINVAL, "row stride < d");
+    DeviceScope ds;
+    int sms = 0;
+    EJ_TRY(check_device(opt.device, &sms));
+    EJ_TRY(ds.enter(opt.device));
+    cudaStream_t s = opt.stream ? (cudaStream_t)opt.stream : cudaStreamPerThread;
+    const double T = threshold(eps);
+    const bool out_dev = is_device_ptr(counts_out);
+    DBuf<double> xbuf;
+    const double* X = nullptr;
+    DBuf<uint64_t> rbuf;
+    DBuf<int32_t> cbuf;
+    EJ_TRY(cbuf.alloc(nq ? nq : 1, s, "query counts"));
+    EJ_TRY(cbuf.zero(s));
+    if (n && nq && !isnan(T) && T >= 0.0) {
+        EJ_TRY(stage_points(points, n, d, ld, xbuf, &X, s));
+        for (uint64_t i = 0; i < nq; ++i) {
+            if (!is_device_ptr(rows) && rows[i] >= n)
+                return set_error(EJOIN_EINVAL, "query row %llu >= n", (unsigned long long)rows[i]);
+        }
+        EJ_TRY(rbuf.alloc(nq, s, "query rows"));
+        EJ_CUDA(cudaMemcpyAsync(rbuf.p, rows, nq * sizeof(uint64_t), cudaMemcpyDefault, s));
+        EJ_TRY(launch_direct_query(X, n, d, T, rbuf.p, nq, cbuf.p, s));
+    }
+    if (nq)
+        EJ_CUDA(cudaMemcpyAsync(counts_out, cbuf.p, nq * sizeof(int32_t),
+                                out_dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s));
+    EJ_CUDA(cudaStreamSynchronize(s));
+    return EJOIN_OK;
+}
+
+double ejoin_threshold(double eps) { return threshold(eps); }
+
+int ejoin_last_error(char* buf, size_t len) {
+    if (buf && len) {
+        strncpy(buf, t_msg, len - 1);
+        buf[len - 1] = 0;
+    }
+    return t_status;
+}
+
+int ejoin_version(void) { return EJOIN_VERSION_MAJOR * 100 + EJOIN_VERSION_MINOR; }
+
+void ejoin_free(void* p) { free(p); }
+
+int ejoin_gpu_join_main_brute_force(unsigned int searchMode, unsigned int device, double* dataset,
+                                    unsigned int* nbQueryPoints, double* epsilon,
+                                    uint64_t* totalNeighbors, unsigned int input_dim,
+                                    unsigned int compute_dim) {
+    clear_error();
+    if (!nbQueryPoints || !epsilon || !totalNeighbors)
+        return set_error(EJOIN_EINVAL, "NULL argument");
+    if (input_dim == 0 || compute_dim < input_dim)
+        return set_error(EJOIN_EINVAL, "bad dimensions (input %u, compute %u)", input_dim, compute_dim);
+    ejoin_options opt;
+    ejoin_default_options(&opt);
+    opt.device = (int32_t)device;
+    opt.ld = compute_dim;
+    switch (searchMode) {
+        case 1: case 2: opt.precision = EJOIN_FP64_DIRECT; break;  // SM_GPU, SM_CUDA_ALT
+        case 3: case 4: opt.precision = EJOIN_AUTO; break;         // SM_TENSOR, SM_TENSOR_MQ
+        case 5: opt.precision = EJOIN_AUTO; opt.proj_k = 8; break; // learned pruning
+        default: return set_error(EJOIN_EINVAL, "Unknown search mode %u", searchMode);
+    }
+    uint64_t total = 0;
+    int rc = self_join_impl(dataset, *nbQueryPoints, input_dim, *epsilon, &opt, nullptr, &total, nullptr);
+    if (rc == EJOIN_OK) *totalNeighbors = total;
+    return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,246 @@
+// ejoin_internal.cuh -- definitions shared by the translation units of
+// libejoin.so.  Host: status/error plumbing, stream-ordered device buffers,
+// event timers.  Device: the exact FP64 pair arithmetic of the reference
+// (kernel_join.cu:184-199) and the band-queue record.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+
+#include <string>
+
+#include "ejoin.h"
+
+namespace ejoin {
+
+// ---------------------------------------------------------------- errors --
+
+int set_error(int status, const char* fmt, ...);
+// Kernel launches issued by the calling thread (reported in ejoin_stats).
+void note_launch(uint64_t k = 1);
+uint64_t launches_so_far();
+int cuda_error(cudaError_t e, const char* what, const char* file, int line);
+void clear_error();
+
+#define EJ_CUDA(expr)                                                        \
+    do {                                                                     \
+        cudaError_t _e = (expr);                                             \
+        if (_e != cudaSuccess) return ::ejoin::cuda_error(_e, #expr, __FILE__, __LINE__); \
+    } while (0)
+
+#define EJ_TRY(expr)                  \
+    do {                              \
+        int _rc = (expr);             \
+        if (_rc != EJOIN_OK) return _rc; \
+    } while (0)
+
+// ------------------------------------------------------- device buffers --
+
+// Stream-ordered device allocation from the device's default memory pool
+// (the pool keeps freed blocks cached, so repeated joins do not pay for
+// cudaMalloc).  Freed on the same stream when the buffer goes out of scope.
+template <typename T>
+struct DBuf {
+    T* p = nullptr;
+    size_t count = 0;
+    cudaStream_t s = nullptr;
+    DBuf() = default;
+    DBuf(const DBuf&) = delete;
+    DBuf& operator=(const DBuf&) = delete;
+    ~DBuf() { release(); }
+    void release() {
+        if (p) cudaFreeAsync(p, s);
+        p = nullptr;
+        count = 0;
+    }
+    int alloc(size_t n, cudaStream_t stream, const char* what) {
+        release();
+        s = stream;
+        count = n;
+        if (n == 0) return EJOIN_OK;
+        cudaError_t e = cudaMallocAsync((void**)&p, n * sizeof(T), stream);
+        if (e != cudaSuccess) {
+            p = nullptr;
+            cudaGetLastError();
+            return set_error(EJOIN_ENOMEM, "device allocation of %zu bytes for %s failed: %s",
+                             n * sizeof(T), what, cudaGetErrorString(e));
+        }
+        return EJOIN_OK;
+    }
+    int zero(cudaStream_t stream) {
+        if (!p) return EJOIN_OK;
+        EJ_CUDA(cudaMemsetAsync(p, 0, count * sizeof(T), stream));
+        return EJOIN_OK;
+    }
+};
+
+struct EventTimer {
+    cudaEvent_t a = nullptr, b = nullptr;
+    EventTimer() {
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+    }
+    ~EventTimer() {
+        if (a) cudaEventDestroy(a);
+        if (b) cudaEventDestroy(b);
+    }
+    void start(cudaStream_t s) { cudaEventRecord(a, s); }
+    void stop(cudaStream_t s) { cudaEventRecord(b, s); }
+    double ms() {
+        float v = 0.f;
+        cudaEventSynchronize(b);
+        cudaEventElapsedTime(&v, a, b);
+        return v;
+    }
+};
+
+// ------------------------------------------------------------ constants --
+
+constexpr double kU = 1.1102230246251565e-16;  // 2^-53, FP64 unit roundoff
+constexpr double kTwo100 = 1.2676506002282294e30;  // 2^100
+
+// Band-queue record: directed pair (i, j) in packed-row index space.  Bit 31
+// of j is set when the pair also credits j (an off-diagonal tile pair: the
+// tile kernels visit only I <= J, so (j, i) is never visited on its own).
+struct BandPair {
+    uint32_t i;
+    uint32_t j;
+};
+constexpr uint32_t kBandBoth = 0x80000000u;
+
+// Status word written by kernels whose waits are bounded.
+struct DevStatus {
+    unsigned int timeout;    // a bounded wait expired (where: code below)
+    unsigned int where;
+    unsigned long long band_count;  // band pairs produced (may exceed capacity)
+    unsigned long long band_hits;
+};
+
+// --------------------------------------------------------- device math --
+
+// Squared distance exactly as the reference's FP64 kernel forms it
+// (kernel_join.cu:185-189 compiled with nvcc's default contraction): per
+// coordinate t = a - b rounded once, acc = fma(t, t, acc), index order.
+__device__ __forceinline__ double exact_d2(const double* __restrict__ a,
+                                           const double* __restrict__ b, uint32_t d) {
+    double acc = 0.0;
+    for (uint32_t k = 0; k < d; ++k) {
+        double t = __dsub_rn(a[k], b[k]);
+        acc = __fma_rn(t, t, acc);
+    }
+    return acc;
+}
+
+// Decode linear index t of the row-major upper triangle of an nT x nT grid
+// into (I, J), I <= J.
+__device__ __forceinline__ void tri_decode(uint64_t t, uint64_t nT, uint64_t& I, uint64_t& J) {
+    // row r holds nT - r entries and starts at r*nT - r*(r-1)/2
+    double b = 2.0 * (double)nT + 1.0;
+    double disc = b * b - 8.0 * (double)t;
+    uint64_t i = (uint64_t)((b - sqrt(disc > 0 ? disc : 0.0)) * 0.5);
+    if (i > nT - 1) i = nT - 1;
+    auto first = [nT](uint64_t r) { return r * nT - r * (r - 1) / 2; };
+    while (i > 0 && first(i) > t) --i;
+    while (i + 1 < nT && first(i + 1) <= t) ++i;
+    I = i;
+    J = i + (t - first(i));
+}
+
+// Warp-aggregated append of `cnt` band pairs held by this lane; returns this
+// lane's first slot (slots >= cap are dropped by the caller; the count still
+// grows so the host can size a re-run).
+__device__ __forceinline__ unsigned long long band_reserve(DevStatus* st, unsigned cnt) {
+    const unsigned lane = threadIdx.x & 31;
+    unsigned incl = cnt;
+    for (int o = 1; o < 32; o <<= 1) {
+        unsigned v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= (unsigned)o) incl += v;
+    }
+    unsigned total = __shfl_sync(0xffffffffu, incl, 31);
+    unsigned long long base = 0;
+    if (lane == 31 && total) base = atomicAdd(&st->band_count, (unsigned long long)total);
+    base = __shfl_sync(0xffffffffu, base, 31);
+    return base + (incl - cnt);
+}
+
+// ------------------------------------------------- screen parameters --
+
+// Operand formats of the tensor-core screen.
+enum class Fmt : int { BF16 = 0, FP16 = 1, E4M3 = 2 };
+
+// Per-join constants of the screen's error bound (all in the scaled, centred
+// coordinate space z = s * fl(x - mu) unless stated).
+struct ScreenParams {
+    double scale;      // s, a power of two
+    double Tlo, Thi;   // s^2 * T_lo, s^2 * T_hi (oracle rounding folded in)
+    double sTlo, sThi; // sqrt(Tlo) rounded down, sqrt(Thi) rounded up
+    double cacc;       // relative bound of the tensor-core accumulation error
+    double absacc;     // absolute bound (FP32 underflow) of the same
+    double clamp_lo;   // smallest alpha the operand format can carry
+    uint32_t d, dp;    // coordinates, padded coordinates (per slab multiple)
+    uint32_t width;    // packed row width in elements
+    int split;         // 1 = hi + lo products
+    Fmt fmt;
+};
+
+// Per-join constants of the FP64 DMMA screen (unscaled centred space y).
+struct DmmaParams {
+    double Tlo, Thi, sTlo, sThi;
+    double crel;       // relative bound (Gram + norms + epilogue rounding)
+    uint32_t d, dp;
+};
+
+// --------------------------------------------------- host entry points --
+// (implemented in the kernel translation units)
+
+struct JoinCtx;  // api.cu
+
+// k_direct.cu
+int launch_direct_selfjoin(const double* X, uint64_t n, uint32_t d, double T, int32_t* counts,
+                           cudaStream_t s);
+int launch_direct_query(const double* X, uint64_t n, uint32_t d, double T, const uint64_t* rows,
+                        uint64_t nq, int32_t* counts, cudaStream_t s);
+int launch_band_recheck(const double* X, uint32_t d, const uint32_t* perm, double T,
+                        const BandPair* band, uint64_t nband, int32_t* counts, DevStatus* st,
+                        cudaStream_t s);
+
+// k_dmma.cu: FP64 DMMA Gram screen over upper-triangle 64x64 tile pairs.
+int launch_dmma_join(const double* Y, uint64_t n_pad, uint32_t dp, const double* h,
+                     const double* g, int32_t* counts, BandPair* band, uint64_t band_cap,
+                     DevStatus* st, cudaStream_t s);
+
+// k_umma.cu: tcgen05 Gram screen over a tile-pair work list (16-bit operands).
+int launch_gram16(const void* Q, uint64_t n_pad, const ScreenParams& P, const uint2* work,
+                  uint64_t nwork, const float* tmax, int32_t* counts, BandPair* band,
+                  uint64_t band_cap, DevStatus* st, int num_sms, cudaStream_t s);
+
+// k_misc.cu
+int build_worklist(uint64_t nT, const double* lo, const double* hi, uint32_t k, double thr,
+                   DBuf<uint2>& work, uint64_t* nwork_out, uint64_t* ncand_out, cudaStream_t s);
+int sum_counts(const int32_t* counts, uint64_t n, unsigned long long* dev_total, cudaStream_t s);
+int scatter_counts(const int32_t* src, const uint32_t* perm, uint64_t n, int32_t* dst,
+                   cudaStream_t s);
+
+// k_prep.cu
+// bad[i] = 1 for rows with a non-finite coordinate; mean over the good rows
+// (deterministic two-pass sums); max |fl(x - mu)| over good rows.
+int launch_center_stats(const double* X, uint64_t n, uint32_t d, uint8_t* bad, double* mu,
+                        double* maxabs, uint64_t* ngood, cudaStream_t s);
+// FP64 centred copy Y[n_pad][dp] and per-row thresholds h, g for the DMMA screen.
+int launch_pack_dmma(const double* X, uint64_t n, uint64_t n_pad, const uint32_t* perm,
+                     const uint8_t* bad, const double* mu, const DmmaParams& P, double* Y,
+                     double* h, double* g, cudaStream_t s);
+// 16-bit operand rows [hi | lo | aug] and per-row out-margins beta.
+int launch_pack16(const double* X, uint64_t n, uint64_t n_pad, const uint32_t* perm,
+                  const uint8_t* bad, const double* mu, const ScreenParams& P, void* Q,
+                  float* beta, cudaStream_t s);
+// FP8 operand rows and per-row (sigma, alpha, beta, 0).
+int launch_pack8(const double* X, uint64_t n, uint64_t n_pad, const uint32_t* perm,
+                 const uint8_t* bad, const double* mu, const ScreenParams& P, uint8_t* Q,
+                 float4* meta, cudaStream_t s);
+// per 128-row tile: max of beta (16-bit) or of meta.z (FP8), as float
+int launch_tile_max(const float* beta, const float4* meta, uint64_t n_pad, float* tmax,
+                    cudaStream_t s);
+
+}  // namespace ejoin

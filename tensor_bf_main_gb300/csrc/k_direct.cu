@@ -1,0 +1,217 @@
+// k_direct.cu -- FP64 CUDA-core kernels with the reference's exact arithmetic.
+//
+//  * direct_selfjoin_kernel: the exact judge (EJOIN_FP64_DIRECT, reference
+//    searchMode 1, kernel_join.cu:168-200).  The reference runs one thread
+//    per query over all N candidates and bumps one global 64-bit counter per
+//    hit; here a CTA takes one 64x64 tile pair of the upper triangle (I <= J),
+//    stages both row blocks in shared memory k-chunk by k-chunk, every thread
+//    keeps a 4x4 block of independent FP64 chains, and the hits become
+//    per-point counts (row counts for I, column counts for J when I < J).
+//    d2(a, b) and d2(b, a) are bitwise equal ((a-b)^2 == (b-a)^2), so the
+//    upper triangle is exact.
+//  * direct_query_kernel: the same tile over (query rows) x (all points).
+//  * band_recheck_kernel: one thread per band pair, the same chain.
+//
+// Zero padding of the k loop is exact: fma(0, 0, acc) == acc for acc >= +0.
+#include "ejoin_internal.cuh"
+
+namespace ejoin {
+namespace {
+
+constexpr int TB = 64;        // tile edge (points)
+constexpr int KC = 32;        // k-chunk staged per step
+constexpr int PADK = TB + 1;  // smem row pitch (doubles) of the k-major stage
+
+// Stage rows [r0, r0+64) x coords [k0, k0+KC) of X (row stride ld) into
+// S[k][r] (k-major).  rows >= n and coords >= d are zero.
+__device__ __forceinline__ void stage_tile(double (*S)[PADK], const double* __restrict__ X,
+                                           uint64_t n, uint32_t d, uint64_t r0, uint32_t k0,
+                                           const uint64_t* __restrict__ rowmap, uint64_t nmap) {
+    for (int e = threadIdx.x; e < TB * KC; e += blockDim.x) {
+        int r = e / KC, k = e % KC;
+        uint64_t row = r0 + r;
+        uint32_t kk = k0 + k;
+        double v = 0.0;
+        if (rowmap) {
+            if (row < nmap && kk < d) v = X[rowmap[row] * (uint64_t)d + kk];
+        } else if (row < n && kk < d) {
+            v = X[row * (uint64_t)d + kk];
+        }
+        S[k][r] = v;
+    }
+}
+
+// One 64x64 tile of exact squared distances.  Thread (ty, tx) owns rows
+// ty + 16*rr and columns tx + 16*cc.
+__device__ __forceinline__ void tile_chains(double acc[4][4], double (*SA)[PADK],
+                                            double (*SB)[PADK], int ty, int tx) {
+#pragma unroll 4
+    for (int k = 0; k < KC; ++k) {
+        double a[4], b[4];
+#pragma unroll
+        for (int rr = 0; rr < 4; ++rr) a[rr] = SA[k][ty + 16 * rr];
+#pragma unroll
+        for (int cc = 0; cc < 4; ++cc) b[cc] = SB[k][tx + 16 * cc];
+#pragma unroll
+        for (int rr = 0; rr < 4; ++rr)
+#pragma unroll
+            for (int cc = 0; cc < 4; ++cc) {
+                double t = __dsub_rn(a[rr], b[cc]);
+                acc[rr][cc] = __fma_rn(t, t, acc[rr][cc]);
+            }
+    }
+}
+
+__global__ void __launch_bounds__(256) direct_selfjoin_kernel(const double* __restrict__ X,
+                                                              uint64_t n, uint32_t d, double T,
+                                                              uint64_t nT, uint64_t tiles,
+                                                              int32_t* counts) {
+    __shared__ double SA[KC][PADK];
+    __shared__ double SB[KC][PADK];
+    __shared__ int rowc[TB], colc[TB];
+    const uint64_t t = blockIdx.x + (uint64_t)blockIdx.y * gridDim.x;
+    if (t >= tiles) return;
+    uint64_t I, J;
+    tri_decode(t, nT, I, J);
+    const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+    if (threadIdx.x < TB) {
+        rowc[threadIdx.x] = 0;
+        colc[threadIdx.x] = 0;
+    }
+    double acc[4][4];
+#pragma unroll
+    for (int rr = 0; rr < 4; ++rr)
+#pragma unroll
+        for (int cc = 0; cc < 4; ++cc) acc[rr][cc] = 0.0;
+    for (uint32_t k0 = 0; k0 < d; k0 += KC) {
+        __syncthreads();
+        stage_tile(SA, X, n, d, I * TB, k0, nullptr, 0);
+        stage_tile(SB, X, n, d, J * TB, k0, nullptr, 0);
+        __syncthreads();
+        tile_chains(acc, SA, SB, ty, tx);
+    }
+    const bool diag = (I == J);
+#pragma unroll
+    for (int rr = 0; rr < 4; ++rr) {
+        uint64_t i = I * TB + ty + 16 * rr;
+#pragma unroll
+        for (int cc = 0; cc < 4; ++cc) {
+            uint64_t j = J * TB + tx + 16 * cc;
+            if (i < n && j < n && acc[rr][cc] <= T) {
+                atomicAdd(&rowc[ty + 16 * rr], 1);
+                if (!diag) atomicAdd(&colc[tx + 16 * cc], 1);
+            }
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < TB) {
+        uint64_t i = I * TB + threadIdx.x, j = J * TB + threadIdx.x;
+        if (rowc[threadIdx.x] && i < n) atomicAdd(&counts[i], rowc[threadIdx.x]);
+        if (colc[threadIdx.x] && j < n) atomicAdd(&counts[j], colc[threadIdx.x]);
+    }
+}
+
+__global__ void __launch_bounds__(256) direct_query_kernel(const double* __restrict__ X, uint64_t n,
+                                                           uint32_t d, double T,
+                                                           const uint64_t* __restrict__ rows,
+                                                           uint64_t nq, int32_t* counts) {
+    __shared__ double SA[KC][PADK];
+    __shared__ double SB[KC][PADK];
+    __shared__ int rowc[TB];
+    const uint64_t Q = blockIdx.y, J = blockIdx.x;
+    const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+    if (threadIdx.x < TB) rowc[threadIdx.x] = 0;
+    double acc[4][4];
+#pragma unroll
+    for (int rr = 0; rr < 4; ++rr)
+#pragma unroll
+        for (int cc = 0; cc < 4; ++cc) acc[rr][cc] = 0.0;
+    for (uint32_t k0 = 0; k0 < d; k0 += KC) {
+        __syncthreads();
+        stage_tile(SA, X, n, d, Q * TB, k0, rows, nq);
+        stage_tile(SB, X, n, d, J * TB, k0, nullptr, 0);
+        __syncthreads();
+        tile_chains(acc, SA, SB, ty, tx);
+    }
+#pragma unroll
+    for (int rr = 0; rr < 4; ++rr) {
+        uint64_t q = Q * TB + ty + 16 * rr;
+#pragma unroll
+        for (int cc = 0; cc < 4; ++cc) {
+            uint64_t j = J * TB + tx + 16 * cc;
+            if (q < nq && j < n && acc[rr][cc] <= T) atomicAdd(&rowc[ty + 16 * rr], 1);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < TB) {
+        uint64_t q = Q * TB + threadIdx.x;
+        if (rowc[threadIdx.x] && q < nq) atomicAdd(&counts[q], rowc[threadIdx.x]);
+    }
+}
+
+__global__ void __launch_bounds__(256) band_recheck_kernel(const double* __restrict__ X, uint32_t d,
+                                                           const uint32_t* __restrict__ perm,
+                                                           double T,
+                                                           const BandPair* __restrict__ band,
+                                                           uint64_t nband, int32_t* counts,
+                                                           DevStatus* st) {
+    uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    unsigned hit = 0;
+    if (e < nband) {
+        BandPair bp = band[e];
+        uint32_t i = bp.i, j = bp.j & ~kBandBoth;
+        uint64_t oi = perm ? perm[i] : i, oj = perm ? perm[j] : j;
+        double d2 = exact_d2(X + oi * (uint64_t)d, X + oj * (uint64_t)d, d);
+        if (d2 <= T) {
+            hit = 1;
+            atomicAdd(&counts[i], 1);
+            if (bp.j & kBandBoth) atomicAdd(&counts[j], 1);
+        }
+    }
+    unsigned c = __reduce_add_sync(0xffffffffu, hit);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(&st->band_hits, (unsigned long long)c);
+}
+
+}  // namespace
+
+int launch_direct_selfjoin(const double* X, uint64_t n, uint32_t d, double T, int32_t* counts,
+                           cudaStream_t s) {
+    if (n == 0) return EJOIN_OK;
+    uint64_t nT = (n + TB - 1) / TB;
+    uint64_t tiles = nT * (nT + 1) / 2;
+    uint64_t gx = tiles < 1048576ull ? tiles : 1048576ull;
+    uint64_t gy = (tiles + gx - 1) / gx;
+    if (gy > 65535)
+        return set_error(EJOIN_EUNSUPPORTED, "direct join: %llu tile pairs exceed the grid",
+                         (unsigned long long)tiles);
+    direct_selfjoin_kernel<<<dim3((unsigned)gx, (unsigned)gy), 256, 0, s>>>(X, n, d, T, nT, tiles,
+                                                                            counts);
+    EJ_CUDA(cudaGetLastError());
+    note_launch();
+    return EJOIN_OK;
+}
+
+int launch_direct_query(const double* X, uint64_t n, uint32_t d, double T, const uint64_t* rows,
+                        uint64_t nq, int32_t* counts, cudaStream_t s) {
+    if (n == 0 || nq == 0) return EJOIN_OK;
+    uint64_t gx = (n + TB - 1) / TB, gy = (nq + TB - 1) / TB;
+    if (gx > 0x7fffffffull || gy > 65535) return set_error(EJOIN_EUNSUPPORTED, "query grid too large");
+    direct_query_kernel<<<dim3((unsigned)gx, (unsigned)gy), 256, 0, s>>>(X, n, d, T, rows, nq, counts);
+    EJ_CUDA(cudaGetLastError());
+    note_launch();
+    return EJOIN_OK;
+}
+
+int launch_band_recheck(const double* X, uint32_t d, const uint32_t* perm, double T,
+                        const BandPair* band, uint64_t nband, int32_t* counts, DevStatus* st,
+                        cudaStream_t s) {
+    if (nband == 0) return EJOIN_OK;
+    uint64_t blocks = (nband + 255) / 256;
+    if (blocks > 0x7fffffffull) return set_error(EJOIN_EUNSUPPORTED, "band too large");
+    band_recheck_kernel<<<(unsigned)blocks, 256, 0, s>>>(X, d, perm, T, band, nband, counts, st);
+    EJ_CUDA(cudaGetLastError());
+    note_launch();
+    return EJOIN_OK;
+}
+
+}  // namespace ejoin

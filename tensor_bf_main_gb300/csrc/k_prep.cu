@@ -1,0 +1,342 @@
+// k_prep.cu -- centring, norms and operand packing for the Gram screens.
+//
+// Re-designs the reference's convertDataset (kernel_join.cu:44-54, a plain
+// FP64 -> FP16 cast) and preComputedSquaredCoordinates (kernel_join.cu:57-88,
+// partial squared norms per 16-wide chunk).  Here one pass per row:
+//   y = fl(x - mu)       FP64 centring (mu = mean of the finite rows)
+//   z = s * y            exact power-of-two scale
+//   q = hi (+ lo)        operands in BF16/FP16 (hi + lo split) or FP8
+// and, in FP64, the per-row quantities of the rigorous error bound: the
+// norm of q, the quantisation residual ||z - q|| (exact per coordinate), the
+// centring error, and from them the in-threshold alpha (carried by the GEMM
+// itself in three extra K columns, see k_umma.cu) and the out-margin beta.
+//
+// Every stored operand is zero or a normal number of its format: values below
+// the smallest normal are flushed here, so the tensor cores never see a
+// subnormal input and the residual accounts for the flush exactly.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cuda_fp8.h>
+#include <string.h>
+
+#include "ejoin_internal.cuh"
+
+namespace ejoin {
+namespace {
+
+constexpr int ROWS_PER_BLOCK_MEAN = 1024;
+
+__global__ void rowcheck_kernel(const double* __restrict__ X, uint64_t n, uint32_t d,
+                                uint8_t* bad, unsigned long long* ngood) {
+    const uint64_t row = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / 32;
+    const int lane = threadIdx.x & 31;
+    bool ok = true;
+    if (row < n) {
+        for (uint32_t k = lane; k < d; k += 32) ok &= isfinite(X[row * d + k]) != 0;
+    }
+    ok = __all_sync(0xffffffffu, ok);
+    if (row < n && lane == 0) {
+        bad[row] = ok ? 0 : 1;
+        if (ok) atomicAdd(ngood, 1ull);
+    }
+}
+
+// partial[b][k] = sum over good rows of block b (fixed order: deterministic)
+__global__ void colsum_partial_kernel(const double* __restrict__ X, uint64_t n, uint32_t d,
+                                      const uint8_t* __restrict__ bad, double* partial) {
+    const uint64_t r0 = blockIdx.x * (uint64_t)ROWS_PER_BLOCK_MEAN;
+    const uint64_t r1 = min(n, r0 + ROWS_PER_BLOCK_MEAN);
+    for (uint32_t k = threadIdx.x; k < d; k += blockDim.x) {
+        double s = 0.0;
+        for (uint64_t r = r0; r < r1; ++r)
+            if (!bad[r]) s += X[r * d + k];
+        partial[blockIdx.x * (uint64_t)d + k] = s;
+    }
+}
+
+__global__ void colsum_final_kernel(const double* __restrict__ partial, uint32_t nb, uint32_t d,
+                                    const unsigned long long* ngood, double* mu) {
+    uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= d) return;
+    double s = 0.0;
+    for (uint32_t b = 0; b < nb; ++b) s += partial[(uint64_t)b * d + k];
+    unsigned long long g = *ngood;
+    mu[k] = g ? s / (double)g : 0.0;
+}
+
+__global__ void maxabs_kernel(const double* __restrict__ X, uint64_t n, uint32_t d,
+                              const uint8_t* __restrict__ bad, const double* __restrict__ mu,
+                              unsigned long long* maxbits) {
+    const uint64_t row = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / 32;
+    const int lane = threadIdx.x & 31;
+    double m = 0.0;
+    if (row < n && !bad[row]) {
+        for (uint32_t k = lane; k < d; k += 32) m = fmax(m, fabs(__dsub_rn(X[row * d + k], mu[k])));
+    }
+    for (int o = 16; o; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (lane == 0 && m > 0.0) atomicMax(maxbits, (unsigned long long)__double_as_longlong(m));
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// ------------------------------------------------------ format rounding --
+
+struct FmtInfo {
+    int fbits;          // fraction bits
+    double min_normal;  // smallest positive normal
+};
+__device__ __forceinline__ FmtInfo fmt_info(Fmt f) {
+    if (f == Fmt::BF16) return {7, 1.1754943508222875e-38};  // 2^-126
+    if (f == Fmt::FP16) return {10, 6.103515625e-05};        // 2^-14
+    return {3, 0.015625};                                     // E4M3: 2^-6
+}
+
+// Round v to `fbits` fraction bits (ties to even) and flush results below the
+// format's smallest normal to zero.  v is a normal double (or zero).
+__device__ __forceinline__ double round_fmt(double v, FmtInfo fi) {
+    if (fabs(v) < fi.min_normal) return 0.0;
+    unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    const int sh = 52 - fi.fbits;
+    unsigned long long lsb = (b >> sh) & 1ull;
+    b += ((1ull << (sh - 1)) - 1ull) + lsb;
+    b &= ~((1ull << sh) - 1ull);
+    double r = __longlong_as_double((long long)b);
+    return fabs(r) < fi.min_normal ? 0.0 : r;
+}
+
+// Smallest representable value of the format >= v (normal or zero).
+__device__ __forceinline__ double round_fmt_up(double v, FmtInfo fi) {
+    double r = round_fmt(v, fi);
+    if (r >= v) return r;
+    if (r == 0.0) return v > 0.0 ? fi.min_normal : 0.0;  // v in (-min_normal, 0): 0 >= v
+    int e;
+    frexp(fabs(r), &e);  // |r| in [2^(e-1), 2^e)
+    double ulp = ldexp(1.0, e - 1 - fi.fbits);
+    double up = r + ulp;  // exact; crossing towards zero stays representable
+    return fabs(up) < fi.min_normal ? 0.0 : up;
+}
+
+__device__ __forceinline__ uint16_t to_bits16(double r, Fmt f) {
+    float x = (float)r;  // exact: r already has <= 11 significant bits
+    if (f == Fmt::BF16) return (uint16_t)(__float_as_uint(x) >> 16);
+    return __half_as_ushort(__float2half_rn(x));
+}
+
+__device__ __forceinline__ uint8_t to_bits8(double r) {
+    return (uint8_t)__nv_cvt_float_to_fp8((float)r, __NV_SATFINITE, __NV_E4M3);
+}
+
+// ------------------------------------------------------------ DMMA pack --
+
+__global__ void pack_dmma_kernel(const double* __restrict__ X, uint64_t n, uint64_t n_pad,
+                                 const uint32_t* __restrict__ perm, const uint8_t* __restrict__ bad,
+                                 const double* __restrict__ mu, DmmaParams P, double* Y, double* h,
+                                 double* g) {
+    const uint64_t p = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / 32;
+    const int lane = threadIdx.x & 31;
+    if (p >= n_pad) return;
+    const uint64_t src = p < n ? (perm ? perm[p] : p) : 0;
+    const bool good = p < n && !bad[src];
+    double nrm = 0.0;
+    for (uint32_t k = lane; k < P.dp; k += 32) {
+        double y = 0.0;
+        if (good && k < P.d) y = __dsub_rn(X[src * P.d + k], mu[k]);
+        Y[p * P.dp + k] = y;
+        nrm = __fma_rn(y, y, nrm);
+    }
+    nrm = warp_sum(nrm);
+    if (lane) return;
+    if (!good) {
+        h[p] = INFINITY;
+        g[p] = INFINITY;
+        return;
+    }
+    const double gs = (P.d + 4) * kU;
+    const double nup = nrm * (1 + gs), ndn = nrm * (1 - gs);
+    const double rho = 1.0001 * kU * sqrt(nup) * (1 + 8 * kU);
+    // in:  G >= h_i + h_j   (h rounded up, incl. epilogue subtraction rounding)
+    double hv = 0.5 * (nup * (1 + P.crel) + 2.0 * P.sTlo * rho - 0.5 * P.Tlo);
+    hv += 8 * kU * (nup + fabs(hv) + P.Tlo + P.sTlo * rho);
+    // out: G <  g_i + g_j   (g rounded down)
+    double gv = 0.5 * (ndn - P.crel * nup - 0.5 * P.Thi - 2.0 * P.sThi * rho - 2.0 * rho * rho);
+    gv -= 8 * kU * (nup + fabs(gv) + P.Thi + P.sThi * rho);
+    h[p] = hv;
+    g[p] = gv;
+}
+
+// --------------------------------------------------- 16-bit screen pack --
+
+template <Fmt F>
+__global__ void pack16_kernel(const double* __restrict__ X, uint64_t n, uint64_t n_pad,
+                              const uint32_t* __restrict__ perm, const uint8_t* __restrict__ bad,
+                              const double* __restrict__ mu, ScreenParams P, uint16_t* Q,
+                              float* beta) {
+    const uint64_t p = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / 32;
+    const int lane = threadIdx.x & 31;
+    if (p >= n_pad) return;
+    const FmtInfo fi = fmt_info(F);
+    const uint64_t src = p < n ? (perm ? perm[p] : p) : 0;
+    const bool good = p < n && !bad[src];
+    uint16_t* row = Q + p * (uint64_t)P.width;
+    double z2 = 0, e2 = 0, nq = 0, a2 = 0, l2 = 0;
+    for (uint32_t k = lane; k < P.dp; k += 32) {
+        double hi = 0.0, lo = 0.0;
+        if (good && k < P.d) {
+            double z = __dsub_rn(X[src * P.d + k], mu[k]) * P.scale;  // exact scaling
+            hi = round_fmt(z, fi);
+            double r = __dsub_rn(z, hi);  // exact
+            double e = r;
+            if (P.split) {
+                lo = round_fmt(r, fi);
+                e = __dsub_rn(r, lo);  // exact
+            }
+            double q = __dadd_rn(hi, lo);  // exact (<= 2 * fbits + 2 significant bits)
+            double aq = fabs(hi) + fabs(lo);
+            z2 = __fma_rn(z, z, z2);
+            e2 = __fma_rn(e, e, e2);
+            nq = __fma_rn(q, q, nq);
+            a2 = __fma_rn(aq, aq, a2);
+            l2 = __fma_rn(lo, lo, l2);
+        }
+        row[k] = to_bits16(hi, F);
+        if (P.split) row[P.dp + k] = to_bits16(lo, F);
+    }
+    z2 = warp_sum(z2);
+    e2 = warp_sum(e2);
+    nq = warp_sum(nq);
+    a2 = warp_sum(a2);
+    l2 = warp_sum(l2);
+
+    double ah[3] = {0, 0, 0};
+    double b = 0.0;
+    if (good) {
+        const double gs = (P.d + 4) * kU;
+        const double nup = nq * (1 + gs), ndn = nq * (1 - gs);
+        const double a2u = a2 * (1 + gs), lu = l2 * (1 + gs);
+        const double rho = (sqrt(e2 * (1 + gs)) + 1.0001 * kU * sqrt(z2 * (1 + gs))) * (1 + 8 * kU);
+        double R = nup + P.cacc * a2u + lu + P.absacc - 0.5 * P.Tlo + 2.0 * P.sTlo * rho;
+        R += 8 * kU * (nup + P.cacc * a2u + lu + P.absacc + 0.5 * P.Tlo + 2.0 * P.sTlo * rho);
+        double at = R >= 0 ? R / (2.0 * (1.0 - P.cacc)) : R / (2.0 * (1.0 + P.cacc));
+        at += fabs(at) * 4 * kU;
+        at = fmax(at, P.clamp_lo);
+        ah[0] = round_fmt(at, fi);
+        double r1 = __dsub_rn(at, ah[0]);
+        ah[1] = round_fmt(r1, fi);
+        double r2 = __dsub_rn(r1, ah[1]);
+        ah[2] = round_fmt_up(r2, fi);
+        const double alpha = ah[0] + ah[1] + ah[2];  // >= at (ah[2] >= r2)
+        b = 0.5 * P.Thi + 2.0 * P.sThi * rho + 2.0 * rho * rho - ndn + 2.0 * alpha +
+            P.cacc * (a2u + 2.0 * fabs(alpha)) + lu + P.absacc;
+        b += 8 * kU * (0.5 * P.Thi + 2.0 * P.sThi * rho + 2.0 * rho * rho + ndn + 2.0 * fabs(alpha) +
+                       P.cacc * (a2u + 2.0 * fabs(alpha)) + lu + P.absacc);
+        b *= 0.5;
+    } else {
+        // never in, never band: C = q_i.q_j - alpha_i - alpha_j << -W
+        ah[0] = (F == Fmt::FP16) ? 32768.0 : kTwo100;
+    }
+    // aug slab: A side [a0 a1 a2 -1 -1 -1 0 ..] (16), B side [-1 -1 -1 a0 a1 a2 0 ..] (16), 0 x 32
+    uint16_t* aug = row + (P.split ? 2 * P.dp : P.dp);
+    double v0 = 0.0, v1 = 0.0;
+    if (lane < 3) v0 = ah[lane];
+    else if (lane < 6) v0 = -1.0;
+    else if (lane >= 16 && lane < 19) v0 = -1.0;
+    else if (lane >= 19 && lane < 22) v0 = ah[lane - 19];
+    aug[lane] = to_bits16(v0, F);
+    aug[lane + 32] = to_bits16(v1, F);
+    if (lane == 0) beta[p] = good ? __double2float_ru(b) : 0.0f;
+}
+
+__global__ void tile_max_kernel(const float* __restrict__ beta, const float4* __restrict__ meta,
+                                uint64_t ntiles, float* tmax) {
+    const uint64_t t = blockIdx.x;
+    if (t >= ntiles) return;
+    float m = 0.0f;  // pad / bad rows carry 0
+    for (int r = threadIdx.x; r < 128; r += blockDim.x) {
+        float v = beta ? beta[t * 128 + r] : meta[t * 128 + r].z;
+        m = fmaxf(m, v);
+    }
+    for (int o = 16; o; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    __shared__ float sm[4];
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x / 32] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float r = sm[0];
+        for (int w = 1; w < (int)(blockDim.x / 32); ++w) r = fmaxf(r, sm[w]);
+        tmax[t] = r;
+    }
+}
+
+}  // namespace
+
+int launch_center_stats(const double* X, uint64_t n, uint32_t d, uint8_t* bad, double* mu,
+                        double* maxabs, uint64_t* ngood_host, cudaStream_t s) {
+    DBuf<unsigned long long> cnt;
+    EJ_TRY(cnt.alloc(2, s, "center stats"));
+    EJ_TRY(cnt.zero(s));
+    const uint64_t warps_blocks = (n * 32 + 255) / 256;
+    rowcheck_kernel<<<(unsigned)warps_blocks, 256, 0, s>>>(X, n, d, bad, cnt.p);
+    EJ_CUDA(cudaGetLastError());
+    note_launch();
+    const uint32_t nb = (uint32_t)((n + ROWS_PER_BLOCK_MEAN - 1) / ROWS_PER_BLOCK_MEAN);
+    DBuf<double> part;
+    EJ_TRY(part.alloc((size_t)nb * d, s, "column partial sums"));
+    colsum_partial_kernel<<<nb, 128, 0, s>>>(X, n, d, bad, part.p);
+    EJ_CUDA(cudaGetLastError());
+    note_launch();
+    colsum_final_kernel<<<(d + 127) / 128, 128, 0, s>>>(part.p, nb, d, cnt.p, mu);
+    EJ_CUDA(cudaGetLastError());
+    note_launch();
+    maxabs_kernel<<<(unsigned)warps_blocks, 256, 0, s>>>(X, n, d, bad, mu, cnt.p + 1);
+    EJ_CUDA(cudaGetLastError());
+    note_launch();
+    unsigned long long h[2];
+    EJ_CUDA(cudaMemcpyAsync(h, cnt.p, sizeof h, cudaMemcpyDeviceToHost, s));
+    EJ_CUDA(cudaStreamSynchronize(s));
+    *ngood_host = h[0];
+    double m;
+    memcpy(&m, &h[1], sizeof m);
+    *maxabs = m;
+    return EJOIN_OK;
+}
+
+int launch_pack_dmma(const double* X, uint64_t n, uint64_t n_pad, const uint32_t* perm,
+                     const uint8_t* bad, const double* mu, const DmmaParams& P, double* Y,
+                     double* h, double* g, cudaStream_t s) {
+    const uint64_t blocks = (n_pad * 32 + 255) / 256;
+    pack_dmma_kernel<<<(unsigned)blocks, 256, 0, s>>>(X, n, n_pad, perm, bad, mu, P, Y, h, g);
+    EJ_CUDA(cudaGetLastError());
+    note_launch();
+    return EJOIN_OK;
+}
+
+int launch_pack16(const double* X, uint64_t n, uint64_t n_pad, const uint32_t* perm,
+                  const uint8_t* bad, const double* mu, const ScreenParams& P, void* Q,
+                  float* beta, cudaStream_t s) {
+    const uint64_t blocks = (n_pad * 32 + 255) / 256;
+    if (P.fmt == Fmt::BF16)
+        pack16_kernel<Fmt::BF16><<<(unsigned)blocks, 256, 0, s>>>(X, n, n_pad, perm, bad, mu, P,
+                                                                  (uint16_t*)Q, beta);
+    else if (P.fmt == Fmt::FP16)
+        pack16_kernel<Fmt::FP16><<<(unsigned)blocks, 256, 0, s>>>(X, n, n_pad, perm, bad, mu, P,
+                                                                  (uint16_t*)Q, beta);
+    else
+        return set_error(EJOIN_EINTERNAL, "pack16: bad format");
+    EJ_CUDA(cudaGetLastError());
+    note_launch();
+    return EJOIN_OK;
+}
+
+int launch_tile_max(const float* beta, const float4* meta, uint64_t n_pad, float* tmax,
+                    cudaStream_t s) {
+    const uint64_t nt = n_pad / 128;
+    if (nt == 0) return EJOIN_OK;
+    tile_max_kernel<<<(unsigned)nt, 128, 0, s>>>(beta, meta, nt, tmax);
+    EJ_CUDA(cudaGetLastError());
+    note_launch();
+    return EJOIN_OK;
+}
+
+}  // namespace ejoin

@@ -1,0 +1,345 @@
+// k_umma.cu -- the tcgen05 Gram screen (EJOIN_BF16 / BF16_SPLIT / FP16).
+//
+// Re-designs the reference's main tensor path,
+// distanceCalculationBruteForceTensorHalf (kernel_join.cu:328-524): there a
+// warp computes -2*Q*C^T + |c|^2 for 16 queries x 16 candidates per wmma
+// m16n16k16, round-trips every k-chunk through shared memory, re-adds the
+// query norms in scalar code and bumps one global counter per hit with
+// sqrt(|d2|) <= eps.  Here:
+//
+//  * A persistent CTA per SM walks a list of 128x128 tile pairs (I <= J, the
+//    upper triangle only).  Warp 0 streams K-slabs of both row blocks into a
+//    6-stage shared-memory ring with TMA (128-byte swizzle).  One thread of
+//    warp 1 issues tcgen05.mma (M=128, N=128, K=16 per instruction) into one
+//    of two FP32 accumulators in tensor memory, so the next tile's MMAs run
+//    while 8 epilogue warps read the previous one.
+//  * Operand rows are [hi | lo | aug] (k_prep.cu).  With the hi+lo split the
+//    MMAs form hi*hi + hi*lo + lo*hi.  The aug slab adds -alpha_i - alpha_j,
+//    so the accumulator holds C_ij = q_i.q_j - alpha_i - alpha_j and the
+//    rigorous screen is a sign test:
+//        C >= 0          pair certainly within eps        (counted)
+//        C < -W_IJ       pair certainly outside eps
+//        otherwise       band: queued for the FP64 recheck
+//    W_IJ = max beta over tile I + max beta over tile J.
+//  * The epilogue packs sign bits with one funnel shift per element, counts
+//    rows with popc, transposes the 32x32 bit block across the warp to count
+//    columns (off-diagonal tiles credit both points), and flushes per-point
+//    counts once per tile.  No distance ever reaches global memory.
+//
+// Every wait is bounded (umma_ptx.cuh); on expiry all roles stop, in-flight
+// copies and MMAs are drained (bounded) and tensor memory is freed.
+#include "tmap.cuh"
+#include "umma_ptx.cuh"
+
+namespace ejoin {
+namespace {
+
+constexpr int NST = 6;                      // smem ring stages
+constexpr int SLAB_BYTES = 128 * 128;       // 128 rows x 128 bytes
+constexpr int STAGE_BYTES = 2 * SLAB_BYTES; // A slab + B slab
+constexpr int NUM_EPI_WARPS = 8;
+constexpr int NTHREADS = (2 + NUM_EPI_WARPS) * 32;
+constexpr uint32_t TMEM_COLS = 256;         // two 128x128 FP32 accumulators
+constexpr uint32_t FULL = 0xffffffffu;
+
+struct GramArgs {
+    const uint2* work;
+    uint64_t nwork;
+    const float* tmax;
+    int32_t* counts;
+    BandPair* band;
+    uint64_t band_cap;
+    DevStatus* st;
+    uint32_t nhi;    // 64-element data slabs per part
+    uint32_t split;  // hi + lo
+    uint32_t fmt;    // 0 = FP16, 1 = BF16 (instruction-descriptor operand format)
+};
+
+struct Ctl {
+    uint64_t full[NST], empty[NST];
+    uint64_t tfull[2], tempty[2];
+    uint64_t ebar[2];
+    uint64_t fin;
+    uint32_t tmem_base;
+    int rowacc[2][128];
+    int colacc[2][128];
+};
+
+constexpr size_t SMEM_BYTES = 1024 + (size_t)NST * STAGE_BYTES + sizeof(Ctl);
+
+// 32x32 bit-matrix transpose across the warp: lane r holds row r (bit c =
+// column c); afterwards lane c holds column c (bit r = row r).
+__device__ __forceinline__ uint32_t transpose32(uint32_t x, uint32_t lane) {
+    const uint32_t masks[5] = {0x0000FFFFu, 0x00FF00FFu, 0x0F0F0F0Fu, 0x33333333u, 0x55555555u};
+    uint32_t j = 16;
+#pragma unroll
+    for (int l = 0; l < 5; ++l, j >>= 1) {
+        const uint32_t m = masks[l];
+        const uint32_t y = __shfl_xor_sync(FULL, x, j);
+        x = (lane & j) ? (((y >> j) & m) | (x & ~m)) : ((x & m) | ((y & m) << j));
+    }
+    return x;
+}
+
+__device__ __forceinline__ uint32_t slab_x(uint32_t step, uint32_t nhi, uint32_t split) {
+    const uint32_t dp = 64 * nhi;
+    if (split) {
+        if (step < 2 * nhi) return (step & 1) ? dp + 64 * (step >> 1) : 64 * (step >> 1);
+        return 2 * dp;
+    }
+    return step < nhi ? 64 * step : dp;
+}
+
+__global__ void __launch_bounds__(NTHREADS, 1)
+    gram_kernel(const __grid_constant__ CUtensorMap tq, const GramArgs a) {
+    extern __shared__ uint8_t smraw[];
+    uint8_t* stages = (uint8_t*)(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
+    Ctl& S = *reinterpret_cast<Ctl*>(stages + (size_t)NST * STAGE_BYTES);
+    const uint32_t warp = threadIdx.x / 32, lane = threadIdx.x & 31;
+
+    if (warp == 1) {
+        ptx::tmem_alloc(&S.tmem_base, TMEM_COLS);
+        ptx::tmem_relinquish();
+    }
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < NST; ++s) {
+            ptx::mbar_init(&S.full[s], 1);
+            ptx::mbar_init(&S.empty[s], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            ptx::mbar_init(&S.tfull[b], 1);
+            ptx::mbar_init(&S.tempty[b], NUM_EPI_WARPS);
+            ptx::mbar_init(&S.ebar[b], NUM_EPI_WARPS);
+        }
+        ptx::mbar_init(&S.fin, 1);
+        ptx::fence_barrier_init();
+        ptx::tma_prefetch_desc(&tq);
+    }
+    for (int i = threadIdx.x; i < 512; i += NTHREADS) (&S.rowacc[0][0])[i] = 0;
+    ptx::tc_fence_before();
+    __syncthreads();
+    ptx::tc_fence_after();
+    const uint32_t tmem = S.tmem_base;
+    const uint32_t nsteps = a.nhi * (a.split ? 2u : 1u) + 1u;
+
+    if (warp == 0) {
+        // ------------------------------------------------ TMA producer
+        if (lane == 0) {
+            uint32_t st = 0, ph = 0;
+            uint32_t issued_ph[NST];
+            uint32_t issued = 0;
+            bool ok = true;
+            for (uint64_t u = blockIdx.x; u < a.nwork && ok; u += gridDim.x) {
+                const uint2 w = a.work[u];
+                for (uint32_t step = 0; step < nsteps; ++step) {
+                    if (!ptx::mbar_wait(&S.empty[st], ph ^ 1u, a.st, 10)) {
+                        ok = false;
+                        break;
+                    }
+                    uint8_t* sa = stages + (size_t)st * STAGE_BYTES;
+                    const int32_t x = (int32_t)slab_x(step, a.nhi, a.split);
+                    ptx::mbar_arrive_expect_tx(&S.full[st], STAGE_BYTES);
+                    ptx::tma_load_2d(sa, &tq, x, (int32_t)(w.x * 128u), &S.full[st]);
+                    ptx::tma_load_2d(sa + SLAB_BYTES, &tq, x, (int32_t)(w.y * 128u), &S.full[st]);
+                    issued_ph[st] = ph;
+                    ++issued;
+                    if (++st == NST) {
+                        st = 0;
+                        ph ^= 1u;
+                    }
+                }
+            }
+            // drain: every issued copy has landed before the CTA can exit
+            const uint32_t last = issued < NST ? issued : NST;
+            for (uint32_t k = 0; k < last; ++k) {
+                const uint32_t s = (st + NST - 1 - k) % NST;
+                ptx::mbar_wait(&S.full[s], issued_ph[s], a.st, 11);
+            }
+        }
+    } else if (warp == 1) {
+        // ------------------------------------------------ MMA issuer
+        if (lane == 0) {
+            const uint32_t idesc = ptx::idesc_f32acc(a.fmt, a.fmt, 128, 128);
+            uint32_t st = 0, ph = 0, it = 0;
+            bool ok = true;
+            auto take = [&](uint32_t& s_out) -> bool {
+                if (!ptx::mbar_wait(&S.full[st], ph, a.st, 20)) return false;
+                s_out = st;
+                if (++st == NST) {
+                    st = 0;
+                    ph ^= 1u;
+                }
+                return true;
+            };
+            for (uint64_t u = blockIdx.x; u < a.nwork && ok; u += gridDim.x, ++it) {
+                const uint32_t b = it & 1u, use = it >> 1;
+                if (!ptx::mbar_wait(&S.tempty[b], (use & 1u) ^ 1u, a.st, 21)) break;
+                ptx::tc_fence_after();
+                const uint32_t d_tmem = tmem + b * 128u;
+                uint32_t acc = 0;
+                for (uint32_t c = 0; c < a.nhi && ok; ++c) {
+                    uint32_t s_hi, s_lo = 0;
+                    if (!take(s_hi)) { ok = false; break; }
+                    if (a.split && !take(s_lo)) { ok = false; break; }
+                    ptx::tc_fence_after();
+                    const uint64_t ah = ptx::sdesc_sw128(ptx::smem_u32(stages + (size_t)s_hi * STAGE_BYTES));
+                    const uint64_t bh = ptx::sdesc_sw128(ptx::smem_u32(stages + (size_t)s_hi * STAGE_BYTES + SLAB_BYTES));
+                    if (a.split) {
+                        const uint64_t al = ptx::sdesc_sw128(ptx::smem_u32(stages + (size_t)s_lo * STAGE_BYTES));
+                        const uint64_t bl = ptx::sdesc_sw128(ptx::smem_u32(stages + (size_t)s_lo * STAGE_BYTES + SLAB_BYTES));
+#pragma unroll
+                        for (uint32_t kk = 0; kk < 4; ++kk) {
+                            ptx::mma_f16(d_tmem, ah + 2 * kk, bh + 2 * kk, idesc, acc);
+                            acc = 1;
+                            ptx::mma_f16(d_tmem, ah + 2 * kk, bl + 2 * kk, idesc, 1);
+                            ptx::mma_f16(d_tmem, al + 2 * kk, bh + 2 * kk, idesc, 1);
+                        }
+                        ptx::mma_commit(&S.empty[s_hi]);
+                        ptx::mma_commit(&S.empty[s_lo]);
+                    } else {
+#pragma unroll
+                        for (uint32_t kk = 0; kk < 4; ++kk) {
+                            ptx::mma_f16(d_tmem, ah + 2 * kk, bh + 2 * kk, idesc, acc);
+                            acc = 1;
+                        }
+                        ptx::mma_commit(&S.empty[s_hi]);
+                    }
+                }
+                if (!ok) break;
+                uint32_t s_aug;
+                if (!take(s_aug)) break;
+                ptx::tc_fence_after();
+                {
+                    // A side: aug elements 0..15, B side: aug elements 16..31 (+32 bytes)
+                    const uint64_t aa = ptx::sdesc_sw128(ptx::smem_u32(stages + (size_t)s_aug * STAGE_BYTES));
+                    const uint64_t ba = ptx::sdesc_sw128(ptx::smem_u32(stages + (size_t)s_aug * STAGE_BYTES + SLAB_BYTES)) + 2;
+                    ptx::mma_f16(d_tmem, aa, ba, idesc, acc);
+                }
+                ptx::mma_commit(&S.empty[s_aug]);
+                ptx::mma_commit(&S.tfull[b]);
+            }
+            // drain: all MMAs complete before tensor memory is freed
+            ptx::mma_commit(&S.fin);
+            ptx::mbar_wait(&S.fin, 0, a.st, 22);
+        }
+    } else {
+        // ------------------------------------------------ epilogue warps
+        const uint32_t ew = warp - 2;          // 0..7
+        const uint32_t q = warp & 3u;          // tensor-memory lane quarter
+        const uint32_t hf = ew >> 2;           // column half
+        const uint32_t et = ew * 32 + lane;    // 0..255
+        uint32_t it = 0;
+        for (uint64_t u = blockIdx.x; u < a.nwork; u += gridDim.x, ++it) {
+            const uint32_t b = it & 1u, use = it >> 1;
+            const uint2 w = a.work[u];
+            const bool diag = (w.x == w.y);
+            const float s = a.tmax[w.x] + a.tmax[w.y];
+            const float W = fmaf(fabsf(s), 9.5367431640625e-07f, s);  // s + |s| 2^-20 >= beta_i + beta_j
+            if (!ptx::mbar_wait(&S.tfull[b], use & 1u, a.st, 30)) break;
+            ptx::tc_fence_after();
+            uint32_t v[2][32];
+            const uint32_t taddr = tmem + ((q * 32u) << 16) + b * 128u + hf * 64u;
+            ptx::tmem_ld_32x32b_x32(taddr, v[0]);
+            ptx::tmem_ld_32x32b_x32(taddr + 32u, v[1]);
+            ptx::tmem_ld_wait();
+            ptx::tc_fence_before();
+            __syncwarp();
+            if (lane == 0) ptx::mbar_arrive(&S.tempty[b]);
+
+            int* racc = S.rowacc[b];
+            int* cacc = S.colacc[b];
+            const uint32_t row = w.x * 128u + q * 32u + lane;
+            int rowcnt = 0;
+#pragma unroll
+            for (int ch = 0; ch < 2; ++ch) {
+                uint32_t neg = 0, negw = 0;
+#pragma unroll
+                for (int c = 31; c >= 0; --c) {
+                    const uint32_t x = v[ch][c];
+                    neg = __funnelshift_l(x, neg, 1);
+                    const uint32_t y = __float_as_uint(__uint_as_float(x) + W);
+                    negw = __funnelshift_l(y, negw, 1);
+                }
+                const uint32_t inm = ~neg;
+                rowcnt += __popc(inm);
+                const uint32_t bandm = neg & ~negw;
+                const uint32_t col0 = w.y * 128u + hf * 64u + ch * 32u;
+                if (__any_sync(FULL, bandm != 0)) {
+                    unsigned long long slot = band_reserve(a.st, __popc(bandm));
+                    uint32_t m = bandm;
+                    while (m) {
+                        const uint32_t c = __ffs(m) - 1;
+                        m &= m - 1;
+                        if (slot < a.band_cap) {
+                            BandPair bp;
+                            bp.i = row;
+                            bp.j = (col0 + c) | (diag ? 0u : kBandBoth);
+                            a.band[slot] = bp;
+                        }
+                        ++slot;
+                    }
+                }
+                if (!diag) {
+                    const uint32_t colbits = transpose32(inm, lane);
+                    const int cc = __popc(colbits);
+                    if (cc) atomicAdd(&cacc[hf * 64u + ch * 32u + lane], cc);
+                }
+            }
+            if (rowcnt) atomicAdd(&racc[q * 32u + lane], rowcnt);
+            __syncwarp();
+            if (lane == 0) ptx::mbar_arrive(&S.ebar[b]);
+            if (!ptx::mbar_wait(&S.ebar[b], use & 1u, a.st, 31)) break;
+            if (et < 128) {
+                const int r = racc[et];
+                if (r) atomicAdd(&a.counts[w.x * 128u + et], r);
+                racc[et] = 0;
+            } else {
+                const int c = cacc[et - 128];
+                if (c) atomicAdd(&a.counts[w.y * 128u + et - 128], c);
+                cacc[et - 128] = 0;
+            }
+        }
+    }
+
+    ptx::tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        ptx::tc_fence_after();
+        ptx::tmem_dealloc(tmem, TMEM_COLS);
+    }
+}
+
+}  // namespace
+
+int launch_gram16(const void* Q, uint64_t n_pad, const ScreenParams& P, const uint2* work,
+                  uint64_t nwork, const float* tmax, int32_t* counts, BandPair* band,
+                  uint64_t band_cap, DevStatus* st, int num_sms, cudaStream_t s) {
+    if (nwork == 0) return EJOIN_OK;
+    if (n_pad % 128 || P.dp % 64) return set_error(EJOIN_EINTERNAL, "gram16: bad padding");
+    if (n_pad > 0x7fffff80ull) return set_error(EJOIN_EUNSUPPORTED, "gram16: too many rows");
+    CUtensorMap map;
+    EJ_TRY(make_tmap_2d(&map, Q,
+                        P.fmt == Fmt::BF16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16
+                                           : CU_TENSOR_MAP_DATA_TYPE_FLOAT16,
+                        2, P.width, n_pad, 64, 128));
+    GramArgs a;
+    a.work = work;
+    a.nwork = nwork;
+    a.tmax = tmax;
+    a.counts = counts;
+    a.band = band;
+    a.band_cap = band_cap;
+    a.st = st;
+    a.nhi = P.dp / 64;
+    a.split = P.split ? 1u : 0u;
+    a.fmt = P.fmt == Fmt::BF16 ? 1u : 0u;
+    EJ_CUDA(cudaFuncSetAttribute(gram_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)SMEM_BYTES));
+    const uint64_t grid = nwork < (uint64_t)num_sms ? nwork : (uint64_t)num_sms;
+    gram_kernel<<<(unsigned)grid, NTHREADS, SMEM_BYTES, s>>>(map, a);
+    EJ_CUDA(cudaGetLastError());
+    note_launch();
+    return EJOIN_OK;
+}
+
+}  // namespace ejoin

@@ -1,0 +1,192 @@
+"""Seeded synthetic workloads with the shapes of the join's benchmark configs.
+
+The reference measured on files (SUSY, MSD, expo, uniform) that are not
+available; these generators stand in for them with the shapes, sizes and
+value distributions of the five benchmark configurations:
+
+  c1  N=10,000     d=128   i.i.d. uniform [0,1)                       mean ~32 nbrs
+  c2  N=1,000,000  d=128   64 isotropic Gaussians, centres U[0,1)^d,
+                           sigma 0.05                                  mean ~64
+  c3  N=2,000,000  d=256   N(0, diag(i^-1.5)) under a seeded Haar
+                           rotation, +10 per coordinate                means 16/128/1024
+  c4  N=4,000,000  d=64    256 clusters on an 8-dim latent (centres
+                           U[0,1)^8, sigma 0.02) embedded by a seeded
+                           orthonormal 64x8 map, + N(0, 0.01^2) noise  mean ~50
+  c5  N=1,000,000  d=1024  1000 Gaussians projected to the unit
+                           sphere; eps^2 = 2 - 2*0.8 (cosine 0.8)      mean ~20
+
+Generation is chunked with fixed per-chunk child seeds (numpy PCG64), so the
+output does not depend on the number of threads.  ``EPS`` holds the radii
+frozen by ``calibrate`` (pooled k-smallest distances of seeded query rows
+against all points); ``C5_SIGMA`` is the cluster spread calibrated for c5.
+"""
+from __future__ import annotations
+
+import os
+from concurrent.futures import ThreadPoolExecutor
+
+import numpy as np
+
+CHUNK = 1 << 16
+
+CONFIGS = {
+    "c1": dict(n=10_000, d=128, kind="uniform", target=32),
+    "c2": dict(n=1_000_000, d=128, kind="gmm", k=64, sigma=0.05, target=64),
+    "c3": dict(n=2_000_000, d=256, kind="powerlaw", target=(16, 128, 1024)),
+    "c4": dict(n=4_000_000, d=64, kind="latent", k=256, latent=8, sigma=0.02, noise=0.01,
+               target=50),
+    "c5": dict(n=1_000_000, d=1024, kind="sphere", k=1000, target=20),
+}
+
+# Frozen radii (see calibrate()); c3 holds one radius per target mean.
+EPS = {
+    "c1": 3.9568644945066116,
+    "c2": 0.6694213287635902,
+    "c3": None,
+    "c4": 0.09982793683043545,
+    "c5": float(np.sqrt(0.4)),
+}
+C5_SIGMA = None
+
+SEED = 20251203
+
+
+def _threads() -> int:
+    return max(1, min(16, os.cpu_count() or 1))
+
+
+def _chunked(n: int, d: int, seed: int, fill):
+    """out[n, d] filled chunk by chunk by fill(rng, lo, hi, out_view)."""
+    out = np.empty((n, d), dtype=np.float64)
+    starts = list(range(0, n, CHUNK))
+    seeds = np.random.SeedSequence(seed).spawn(len(starts))
+
+    def work(t):
+        lo = starts[t]
+        hi = min(n, lo + CHUNK)
+        fill(np.random.Generator(np.random.PCG64(seeds[t])), lo, hi, out[lo:hi])
+
+    with ThreadPoolExecutor(_threads()) as ex:
+        list(ex.map(work, range(len(starts))))
+    return out
+
+
+def generate(name: str, n: int | None = None, seed: int = SEED, sigma: float | None = None):
+    """Points (n, d) float64 of config `name` (n defaults to the config's N)."""
+    cfg = CONFIGS[name]
+    n = cfg["n"] if n is None else int(n)
+    d = cfg["d"]
+    rng = np.random.Generator(np.random.PCG64(seed))
+    kind = cfg["kind"]
+    if kind == "uniform":
+        return _chunked(n, d, seed + 1, lambda r, lo, hi, o: o.__setitem__(slice(None), r.random((hi - lo, d))))
+    if kind == "gmm":
+        centres = rng.random((cfg["k"], d))
+        s = cfg["sigma"]
+
+        def fill(r, lo, hi, o):
+            lab = r.integers(0, cfg["k"], hi - lo)
+            o[:] = centres[lab] + s * r.standard_normal((hi - lo, d))
+        return _chunked(n, d, seed + 2, fill)
+    if kind == "powerlaw":
+        lam = np.arange(1, d + 1, dtype=np.float64) ** -1.5
+        q, rr = np.linalg.qr(rng.standard_normal((d, d)))
+        R = q * np.sign(np.diag(rr))  # Haar-distributed rotation
+        M = (R * np.sqrt(lam)[None, :]).T  # x = R diag(sqrt(lam)) g  ->  g @ M
+
+        def fill(r, lo, hi, o):
+            o[:] = r.standard_normal((hi - lo, d)) @ M + 10.0
+        return _chunked(n, d, seed + 3, fill)
+    if kind == "latent":
+        centres = rng.random((cfg["k"], cfg["latent"]))
+        E, _ = np.linalg.qr(rng.standard_normal((d, cfg["latent"])))  # 64 x 8 orthonormal
+        s, noise = cfg["sigma"], cfg["noise"]
+
+        def fill(r, lo, hi, o):
+            lab = r.integers(0, cfg["k"], hi - lo)
+            z = centres[lab] + s * r.standard_normal((hi - lo, cfg["latent"]))
+            o[:] = z @ E.T + noise * r.standard_normal((hi - lo, d))
+        return _chunked(n, d, seed + 4, fill)
+    if kind == "sphere":
+        centres = rng.standard_normal((cfg["k"], d))
+        centres /= np.linalg.norm(centres, axis=1, keepdims=True)
+        s = C5_SIGMA if sigma is None else sigma
+        if s is None:
+            raise RuntimeError("c5 spread not calibrated")
+
+        def fill(r, lo, hi, o):
+            lab = r.integers(0, cfg["k"], hi - lo)
+            v = centres[lab] + s * r.standard_normal((hi - lo, d))
+            o[:] = v / np.linalg.norm(v, axis=1, keepdims=True)
+        return _chunked(n, d, seed + 5, fill)
+    raise ValueError(kind)
+
+
+def _smallest_dists(x, rows, kkeep):
+    """For each query row, its kkeep smallest distances to all points (approx.,
+    Gram form in float64: calibration only)."""
+    q = x[rows]
+    qn = (q * q).sum(1)
+    best = np.full((len(rows), kkeep), np.inf)
+    step = 1 << 16
+    for lo in range(0, x.shape[0], step):
+        c = x[lo:lo + step]
+        d2 = qn[:, None] + (c * c).sum(1)[None, :] - 2.0 * (q @ c.T)
+        np.maximum(d2, 0, out=d2)
+        both = np.concatenate([best, d2], axis=1)
+        best = np.partition(both, kkeep - 1, axis=1)[:, :kkeep]
+    return np.sqrt(np.sort(best, axis=1))
+
+
+def calibrate_eps(x, target: float, nq: int = 256, seed: int = SEED) -> float:
+    """eps with mean neighbour count ~= target (self included) on nq seeded rows."""
+    rng = np.random.Generator(np.random.PCG64(seed + 99))
+    rows = rng.choice(x.shape[0], size=min(nq, x.shape[0]), replace=False)
+    kkeep = int(min(x.shape[0], max(8, 4 * target)))
+    while True:
+        dist = _smallest_dists(x, rows, kkeep)
+        pooled = np.sort(dist.ravel())
+        want = int(round(target * len(rows)))
+        eps = float(pooled[min(want, pooled.size) - 1])
+        # every query's kept list must reach beyond eps, else counts are clipped
+        if np.all(dist[:, -1] > eps) or kkeep == x.shape[0]:
+            return eps
+        kkeep = min(x.shape[0], kkeep * 4)
+
+
+def frozen_eps(name: str, x) -> float:
+    """The frozen radius of config `name` for the full-size workload; for a
+    reduced N the radius is recalibrated on the given points."""
+    cfg = CONFIGS[name]
+    e = EPS.get(name)
+    t = cfg["target"]
+    if isinstance(e, list):
+        e = e[0]
+    if e is not None and x.shape[0] == cfg["n"]:
+        return float(e)
+    if name == "c5":
+        return float(np.sqrt(0.4))
+    return calibrate_eps(x, t[0] if isinstance(t, tuple) else t)
+
+
+def mean_count(x, eps: float, nq: int = 256, seed: int = SEED) -> float:
+    rng = np.random.Generator(np.random.PCG64(seed + 98))
+    rows = rng.choice(x.shape[0], size=min(nq, x.shape[0]), replace=False)
+    dist = _smallest_dists(x, rows, min(x.shape[0], 4096))
+    return float((dist <= eps).sum(1).mean())
+
+
+if __name__ == "__main__":
+    import json
+    import sys
+
+    out = {}
+    for name in sys.argv[1:] or ["c1", "c2", "c3", "c4"]:
+        x = generate(name)
+        t = CONFIGS[name]["target"]
+        if isinstance(t, tuple):
+            out[name] = [calibrate_eps(x, tt) for tt in t]
+        else:
+            out[name] = calibrate_eps(x, t)
+        print(name, out[name], flush=True)
+    print(json.dumps(out))

@@ -1,0 +1,72 @@
+"""CPU: the oracle against the golden vectors and an independent restatement."""
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+
+def load_f64(name, d):
+    return np.fromfile(os.path.join(GOLDEN, name), dtype="<f8").reshape(-1, d)
+
+
+@pytest.mark.parametrize("name", ["test100", "test128"])
+def test_oracle_known_answers(oracle_mod, name):
+    g = json.load(open(os.path.join(GOLDEN, "join_golden.json")))["files"][name]
+    x = load_f64(name + ".f64", g["d"])
+    assert x.shape == (g["n"], g["d"])
+    for case in g["cases"]:
+        counts, total = oracle_mod.self_join(x, case["eps"])
+        assert total == case["total"], case["eps"]
+        assert counts.tolist() == case["counts"]
+
+
+def test_oracle_ties_against_rational_restatement(oracle_mod):
+    g = json.load(open(os.path.join(GOLDEN, "ties.json")))
+    x = load_f64("ties.f64", g["d"])
+    for case in g["cases"]:
+        counts, total = oracle_mod.self_join(x, case["eps"])
+        assert total == case["total"], case["eps"]
+        assert counts.tolist() == case["counts"]
+
+
+def test_oracle_matches_python_loops_random(oracle_mod):
+    rng = np.random.default_rng(3)
+    x = rng.random((40, 5))
+    for eps in (0.2, 0.5, 0.8):
+        c1, t1 = oracle_mod.self_join(x, eps)
+        c2, t2 = oracle_mod.py_self_join(x, eps)
+        assert t1 == t2 and c1.tolist() == c2.tolist()
+
+
+def test_threshold_properties(oracle_mod):
+    rng = np.random.default_rng(5)
+    for eps in list(rng.random(200) * 10) + [1e-300, 1e-160, 1e150, 1.0, 0.1]:
+        T = oracle_mod.threshold(eps)
+        assert math.sqrt(T) <= eps
+        assert not (math.sqrt(math.nextafter(T, math.inf)) <= eps)
+        assert T == oracle_mod.py_threshold(eps)
+    assert oracle_mod.threshold(0.0) == 0.0
+    assert oracle_mod.threshold(-1.0) == -math.inf
+    assert math.isnan(oracle_mod.threshold(float("nan")))
+    assert oracle_mod.threshold(float("inf")) == math.inf
+
+
+def test_oracle_nonfinite_rows(oracle_mod):
+    x = np.array([[0.0, 0.0], [np.nan, 0.0], [np.inf, 1.0], [0.0, 0.1]])
+    c, t = oracle_mod.self_join(x, 0.5)
+    assert c.tolist() == [2, 0, 0, 2]
+    c, t = oracle_mod.self_join(x, float("inf"))
+    # inf row: d2 = inf with finite rows (counted at eps = inf), NaN with itself (inf - inf)
+    assert c.tolist() == [3, 0, 2, 3]
+
+
+def test_oracle_query_counts(oracle_mod):
+    rng = np.random.default_rng(9)
+    x = rng.random((300, 7))
+    full, _ = oracle_mod.self_join(x, 0.6)
+    rows = np.array([0, 5, 299, 17])
+    assert oracle_mod.query_counts(x, 0.6, rows).tolist() == full[rows].tolist()
