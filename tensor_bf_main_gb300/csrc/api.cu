@@ -217,7 +217,7 @@ static int screen_and_recheck(Join& J, uint64_t cap0, Screen&& screen, uint64_t 
             return set_error(EJOIN_ETIMEOUT, "Gram kernel: a bounded device wait expired (site %u)", h.where);
         if (h.band_count <= cap) {
             tr.start(J.s);
-            EJ_TRY(launch_band_recheck(J.X, J.d, J.perm, J.T, band.p, h.band_count, J.counts, dst.p, J.s));
+            EJ_TRY(launch_band_recheck(J.X, J.n, J.d, J.perm, J.T, band.p, h.band_count, J.counts, dst.p, J.s));
             tr.stop(J.s);
             EJ_CUDA(cudaMemcpyAsync(&h, dst.p, sizeof h, cudaMemcpyDeviceToHost, J.s));
             EJ_CUDA(cudaStreamSynchronize(J.s));
@@ -315,7 +315,10 @@ static int run_screen16(Join& J, Fmt fmt, bool split) {
     double Tlo, Thi;
     oracle_band(J.T, J.d, &Tlo, &Thi);
     const double s2 = P.scale * P.scale;
-    const double cap_t = 1.152921504606846976e18;  // 2^60, far above any |z| distance
+    // Every finite pair has s_q = |q_i - q_j|^2 <= 4 max|q|^2 (<= 2^14 for FP16
+    // by the choice of scale, <= 4d for BF16): capping T far above that keeps
+    // both tests exact while bounding the margins in the operand range.
+    const double cap_t = (fmt == Fmt::FP16) ? 32768.0 : 1.152921504606846976e18;
     P.Tlo = std::min(Tlo * s2, cap_t);
     P.Thi = std::min(Thi * s2, cap_t);
     P.sTlo = sqrt(P.Tlo) * (1 - 4 * kU);

@@ -201,7 +201,7 @@ int launch_direct_selfjoin(const double* X, uint64_t n, uint32_t d, double T, in
                            cudaStream_t s);
 int launch_direct_query(const double* X, uint64_t n, uint32_t d, double T, const uint64_t* rows,
                         uint64_t nq, int32_t* counts, cudaStream_t s);
-int launch_band_recheck(const double* X, uint32_t d, const uint32_t* perm, double T,
+int launch_band_recheck(const double* X, uint64_t n, uint32_t d, const uint32_t* perm, double T,
                         const BandPair* band, uint64_t nband, int32_t* counts, DevStatus* st,
                         cudaStream_t s);
 

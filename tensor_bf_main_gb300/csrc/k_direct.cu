@@ -153,13 +153,15 @@ __global__ void __launch_bounds__(256) band_recheck_kernel(const double* __restr
                                                            const uint32_t* __restrict__ perm,
                                                            double T,
                                                            const BandPair* __restrict__ band,
-                                                           uint64_t nband, int32_t* counts,
-                                                           DevStatus* st) {
+                                                           uint64_t nband, uint64_t n,
+                                                           int32_t* counts, DevStatus* st) {
     uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
     unsigned hit = 0;
-    if (e < nband) {
-        BandPair bp = band[e];
-        uint32_t i = bp.i, j = bp.j & ~kBandBoth;
+    BandPair bp = {0u, 0u};
+    if (e < nband) bp = band[e];
+    const uint32_t i = bp.i, j = bp.j & ~kBandBoth;
+    // padding rows (index >= n) hold no point: such pairs are never neighbours
+    if (e < nband && i < n && j < n) {
         uint64_t oi = perm ? perm[i] : i, oj = perm ? perm[j] : j;
         double d2 = exact_d2(X + oi * (uint64_t)d, X + oj * (uint64_t)d, d);
         if (d2 <= T) {
@@ -202,13 +204,14 @@ int launch_direct_query(const double* X, uint64_t n, uint32_t d, double T, const
     return EJOIN_OK;
 }
 
-int launch_band_recheck(const double* X, uint32_t d, const uint32_t* perm, double T,
+int launch_band_recheck(const double* X, uint64_t n, uint32_t d, const uint32_t* perm, double T,
                         const BandPair* band, uint64_t nband, int32_t* counts, DevStatus* st,
                         cudaStream_t s) {
     if (nband == 0) return EJOIN_OK;
     uint64_t blocks = (nband + 255) / 256;
     if (blocks > 0x7fffffffull) return set_error(EJOIN_EUNSUPPORTED, "band too large");
-    band_recheck_kernel<<<(unsigned)blocks, 256, 0, s>>>(X, d, perm, T, band, nband, counts, st);
+    band_recheck_kernel<<<(unsigned)blocks, 256, 0, s>>>(X, d, perm, T, band, nband, n, counts,
+                                                         st);
     EJ_CUDA(cudaGetLastError());
     note_launch();
     return EJOIN_OK;
