@@ -182,6 +182,23 @@ int ejoin_gpu_join_main_brute_force(unsigned int searchMode, unsigned int device
                                     double* epsilon, uint64_t* totalNeighbors,
                                     unsigned int input_dim, unsigned int compute_dim);
 
+/* Exact self-join that allocates no device memory, for callers that cannot
+ * call cudaMalloc while they run the join (an engine that owns all device
+ * memory through its own pool, a serving path that forbids allocation and
+ * its implicit synchronisation, a process under a hard memory cap).  No
+ * counterpart in the reference.  It runs the FP64 DMMA screen and the FP64
+ * band recheck (counts identical to ejoin_self_join) with all scratch in one
+ * static 32 MiB device array that every GPU loading the library holds until
+ * exit.  Limits: n <= 16384, d <= 128 (else EJOIN_EINVAL); a boundary band
+ * larger than the array's queue returns EJOIN_ENOMEM.  `points` (n x d,
+ * contiguous) and `counts` (n int32) must be device memory; *total_out is
+ * host memory (may be NULL); `stream` may be NULL.  The first call on a
+ * device resolves the array's address and should come before any stream
+ * capture on that device.  All calls share the array: calls that overlap on
+ * the GPU race. */
+int ejoin_self_join_noalloc(const double* points, uint64_t n, uint32_t d, double eps,
+                            int device, void* stream, int32_t* counts, uint64_t* total_out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -102,7 +102,7 @@ EXPORTED = [
     "ejoin_default_options", "ejoin_self_join", "ejoin_query_counts", "ejoin_train_projection",
     "ejoin_certify_spectral_norm", "ejoin_threshold", "ejoin_import_dataset",
     "ejoin_import_binary", "ejoin_free", "ejoin_last_error", "ejoin_version",
-    "ejoin_gpu_join_main_brute_force",
+    "ejoin_gpu_join_main_brute_force", "ejoin_self_join_noalloc",
 ]
 
 _lib = None
@@ -133,6 +133,7 @@ def load_library(path: str = LIB_PATH):
     L.ejoin_last_error.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
     L.ejoin_gpu_join_main_brute_force.argtypes = [u32, u32, vp, ctypes.POINTER(u32),
                                                   ctypes.POINTER(dbl), ctypes.POINTER(u64), u32, u32]
+    L.ejoin_self_join_noalloc.argtypes = [vp, u64, u32, dbl, ctypes.c_int, vp, vp, ctypes.POINTER(u64)]
     for name in EXPORTED:
         if name not in ("ejoin_threshold", "ejoin_free"):
             getattr(L, name).restype = ctypes.c_int

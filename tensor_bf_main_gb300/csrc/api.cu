@@ -81,7 +81,7 @@ double threshold(double eps) {
 // distance delta^2 ((d+2) roundings of at most 2^-53 each, plus subnormal
 // absolute error).  Pairs with delta^2 <= Tlo certainly satisfy d2 <= T;
 // pairs with delta^2 > Thi certainly do not.
-static void oracle_band(double T, uint32_t d, double* Tlo, double* Thi) {
+void oracle_band(double T, uint32_t d, double* Tlo, double* Thi) {
     const double co = (d + 4) * kU * 1.0001;
     const double ao = (d + 2) * 4.9406564584124654e-324 * 2.0;
     double lo = (T - ao) / (1.0 + co) * (1.0 - 4 * kU);
