@@ -105,6 +105,9 @@ EXPORTED = [
     "ejoin_gpu_join_main_brute_force", "ejoin_self_join_noalloc",
 ]
 
+# Test hooks declared in include/ejoin_testing.h.
+TESTING = ["ejoin_testing_projection_grad", "ejoin_testing_renormalise"]
+
 _lib = None
 
 
@@ -133,6 +136,10 @@ def load_library(path: str = LIB_PATH):
     L.ejoin_last_error.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
     L.ejoin_gpu_join_main_brute_force.argtypes = [u32, u32, vp, ctypes.POINTER(u32),
                                                   ctypes.POINTER(dbl), ctypes.POINTER(u64), u32, u32]
+    L.ejoin_testing_projection_grad.argtypes = [vp, vp, u64, vp, u32, u32, vp, vp]
+    L.ejoin_testing_projection_grad.restype = ctypes.c_int
+    L.ejoin_testing_renormalise.argtypes = [vp, u32, u32, vp]
+    L.ejoin_testing_renormalise.restype = ctypes.c_int
     L.ejoin_self_join_noalloc.argtypes = [vp, u64, u32, dbl, ctypes.c_int, vp, vp, ctypes.POINTER(u64)]
     for name in EXPORTED:
         if name not in ("ejoin_threshold", "ejoin_free"):

@@ -175,6 +175,7 @@ struct Join {
     const double* X;  // n x d, device
     uint64_t n;
     uint32_t d;
+    double eps;
     double T;
     ejoin_options opt;
     ejoin_stats* st;
@@ -286,6 +287,54 @@ static int run_dmma(Join& J) {
     return screen_and_recheck(J, std::max<uint64_t>(1u << 20, J.n), screen, n_pad, tg, tr);
 }
 
+// Learned ordering: projection P (given or trained on the GPU), its certified
+// spectral-norm bound sigma, the permutation into projected order and the
+// boxes of the 128-row tiles.  A tile pair is skipped when the squared gap of
+// its boxes exceeds sigma^2 * T_hi: then every pair in it has
+// delta^2 >= gap^2 / sigma^2 > T_hi, i.e. d2 > T.
+struct Learned {
+    DBuf<uint32_t> perm;
+    DBuf<double> lo, hi;
+    double thr = 0.0;
+    uint32_t k = 0;
+};
+
+static int prepare_learned(Join& J, uint64_t n_pad, Learned& L) {
+    const uint32_t k = J.opt.proj_k;
+    if (k == 0 || k > 16) return set_error(EJOIN_EINVAL, "proj_k must be in 0..16 (got %u)", k);
+    EventTimer tt, to;
+    std::vector<float> P;
+    double sigma = 0.0;
+    tt.start(J.s);
+    if (J.opt.projection) {
+        P.assign(J.opt.projection, J.opt.projection + (size_t)k * J.d);
+        EJ_TRY(cert_spectral_norm(P.data(), k, J.d, &sigma));
+    } else {
+        TrainResult tr;
+        EJ_TRY(train_projection_dev(J.X, J.n, J.d, J.eps, k, J.opt.train_pairs, J.opt.train_steps,
+                                    J.opt.seed, J.opt.order == EJOIN_ORDER_LEAD, J.s, tr));
+        P.swap(tr.P);
+        sigma = tr.sigma_cert;
+    }
+    tt.stop(J.s);
+    to.start(J.s);
+    DBuf<float> Pd;
+    EJ_TRY(Pd.alloc(P.size(), J.s, "projection"));
+    EJ_CUDA(cudaMemcpyAsync(Pd.p, P.data(), P.size() * sizeof(float), cudaMemcpyHostToDevice, J.s));
+    EJ_TRY(learned_order(J.X, J.n, n_pad, J.d, Pd.p, k, J.opt.order == EJOIN_ORDER_LEAD, L.perm,
+                         &L.lo, &L.hi, J.s));
+    to.stop(J.s);
+    double Tlo, Thi;
+    oracle_band(J.T, J.d, &Tlo, &Thi);
+    L.thr = Thi * sigma * sigma * (1.0 + 32 * kU);
+    L.k = k;
+    J.perm = L.perm.p;
+    J.st->sigma_cert = sigma;
+    J.st->ms_train = tt.ms();
+    J.st->ms_order = to.ms();
+    return EJOIN_OK;
+}
+
 // Global power-of-two scale of the centred data for the 16-bit operands.
 static double screen_scale(Fmt f, double maxabs, uint32_t d) {
     if (!(maxabs > 0.0) || !isfinite(maxabs)) return 1.0;
@@ -305,6 +354,12 @@ static int run_screen16(Join& J, Fmt fmt, bool split) {
     double maxabs = 0;
     uint64_t ngood = 0;
     EJ_TRY(launch_center_stats(J.X, J.n, J.d, bad.p, mu.p, &maxabs, &ngood, J.s));
+    tp.stop(J.s);
+    const double ms_center = tp.ms();
+    const uint64_t n_pad = round_up(J.n, 128);
+    Learned L;
+    if (J.opt.proj_k) EJ_TRY(prepare_learned(J, n_pad, L));
+    tp.start(J.s);
     ScreenParams P;
     P.fmt = fmt;
     P.split = split ? 1 : 0;
@@ -328,7 +383,6 @@ static int run_screen16(Join& J, Fmt fmt, bool split) {
     P.cacc = scale_opt * (kprod + 16.0) * ldexp(1.0, -22);
     P.absacc = (kprod + 16.0) * ldexp(1.0, -125);
     P.clamp_lo = (fmt == Fmt::FP16) ? -16384.0 : -kTwo100;
-    const uint64_t n_pad = round_up(J.n, 128);
     DBuf<uint16_t> Q;
     DBuf<float> beta, tmax;
     EJ_TRY(Q.alloc(n_pad * P.width, J.s, "packed operands"));
@@ -337,11 +391,16 @@ static int run_screen16(Join& J, Fmt fmt, bool split) {
     EJ_TRY(launch_pack16(J.X, J.n, n_pad, J.perm, bad.p, mu.p, P, Q.p, beta.p, J.s));
     EJ_TRY(launch_tile_max(beta.p, nullptr, n_pad, tmax.p, J.s));
     tp.stop(J.s);
-    J.st->ms_prep = tp.ms();
+    J.st->ms_prep = ms_center + tp.ms();
     const uint64_t nT = n_pad / 128;
     DBuf<uint2> work;
     uint64_t nwork = 0;
-    EJ_TRY(build_worklist(nT, nullptr, nullptr, 0, 0.0, work, &nwork, nullptr, J.s));
+    EventTimer tw;
+    tw.start(J.s);
+    EJ_TRY(build_worklist(nT, L.k ? L.lo.p : nullptr, L.k ? L.hi.p : nullptr, L.k, L.thr, work,
+                          &nwork, nullptr, J.s));
+    tw.stop(J.s);
+    J.st->ms_order += tw.ms();
     J.st->tile_pairs_total = nT * (nT + 1) / 2;
     J.st->tile_pairs_run = nwork;
     J.st->gram_flops = 2.0 * kprod * 128.0 * 128.0 * (double)nwork;
@@ -400,6 +459,7 @@ static int self_join_impl(const double* points, uint64_t n, uint32_t d, double e
     J.sms = sms;
     J.n = n;
     J.d = d;
+    J.eps = eps;
     J.T = T;
     J.opt = opt;
     J.st = &stats;
@@ -528,6 +588,49 @@ int ejoin_query_counts(const double* points, uint64_t n, uint32_t d, double eps,
         EJ_CUDA(cudaMemcpyAsync(counts_out, cbuf.p, nq * sizeof(int32_t),
                                 out_dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s));
     EJ_CUDA(cudaStreamSynchronize(s));
+    return EJOIN_OK;
+}
+
+int ejoin_train_projection(const double* points, uint64_t n, uint32_t d, double eps,
+                           const ejoin_options* opt_in, float* P_out, double* sigma_cert_out,
+                           ejoin_stats* stats_out) {
+    clear_error();
+    ejoin_options opt;
+    ejoin_default_options(&opt);
+    if (opt_in) {
+        if (opt_in->struct_size != sizeof(ejoin_options)) return set_error(EJOIN_EINVAL, "ejoin_options.struct_size mismatch");
+        opt = *opt_in;
+    }
+    if (d == 0 || n < 2 || !points || !P_out) return set_error(EJOIN_EINVAL, "bad arguments");
+    if (opt.proj_k == 0 || opt.proj_k > 16) return set_error(EJOIN_EINVAL, "proj_k must be in 1..16");
+    if (!(eps > 0.0) || isinf(eps)) return set_error(EJOIN_EINVAL, "eps must be positive and finite");
+    const uint64_t ld = opt.ld ? opt.ld : d;
+    if (ld < d) return set_error(EJOIN_EINVAL, "row stride < d");
+    DeviceScope ds;
+    int sms = 0;
+    EJ_TRY(check_device(opt.device, &sms));
+    EJ_TRY(ds.enter(opt.device));
+    cudaStream_t s = opt.stream ? (cudaStream_t)opt.stream : cudaStreamPerThread;
+    DBuf<double> xbuf;
+    const double* X = nullptr;
+    EJ_TRY(stage_points(points, n, d, ld, xbuf, &X, s));
+    EventTimer t;
+    t.start(s);
+    TrainResult tr;
+    EJ_TRY(train_projection_dev(X, n, d, eps, opt.proj_k, opt.train_pairs, opt.train_steps, opt.seed,
+                                opt.order == EJOIN_ORDER_LEAD, s, tr));
+    t.stop(s);
+    memcpy(P_out, tr.P.data(), tr.P.size() * sizeof(float));
+    if (sigma_cert_out) *sigma_cert_out = tr.sigma_cert;
+    if (stats_out) {
+        memset(stats_out, 0, sizeof *stats_out);
+        stats_out->n = n;
+        stats_out->d = d;
+        stats_out->sigma_cert = tr.sigma_cert;
+        stats_out->ms_train = t.ms();
+        stats_out->reserved[0] = tr.loss_first;
+        stats_out->reserved[1] = tr.loss_last;
+    }
     return EJOIN_OK;
 }
 

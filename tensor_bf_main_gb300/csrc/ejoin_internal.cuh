@@ -9,6 +9,7 @@
 #include <stdio.h>
 
 #include <string>
+#include <vector>
 
 #include "ejoin.h"
 
@@ -221,6 +222,21 @@ int build_worklist(uint64_t nT, const double* lo, const double* hi, uint32_t k, 
 int sum_counts(const int32_t* counts, uint64_t n, unsigned long long* dev_total, cudaStream_t s);
 int scatter_counts(const int32_t* src, const uint32_t* perm, uint64_t n, int32_t* dst,
                    cudaStream_t s);
+
+// k_learn.cu: learned projection, ordering, tile boxes
+struct TrainResult {
+    std::vector<float> P;
+    double loss_first = 0, loss_last = 0;
+    double sigma_cert = 0;
+};
+int train_projection_dev(const double* X, uint64_t n, uint32_t d, double eps, uint32_t k,
+                         uint64_t pairs, uint32_t steps, uint64_t seed, int lead_only,
+                         cudaStream_t s, TrainResult& out);
+int learned_order(const double* X, uint64_t n, uint64_t n_pad, uint32_t d, const float* P_dev,
+                  uint32_t k, int lead_only, DBuf<uint32_t>& perm, DBuf<double>* lo,
+                  DBuf<double>* hi, cudaStream_t s);
+// host.cpp: certified upper bound of ||P||_2
+int cert_spectral_norm(const float* P, uint32_t k, uint32_t d, double* out);
 
 // k_prep.cu
 // bad[i] = 1 for rows with a non-finite coordinate; mean over the good rows

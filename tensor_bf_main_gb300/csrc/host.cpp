@@ -14,6 +14,7 @@
 namespace ejoin {
 int set_error(int status, const char* fmt, ...);
 void clear_error();
+int cert_spectral_norm(const float* P, uint32_t k, uint32_t d, double* bound_out);
 }  // namespace ejoin
 
 using ejoin::set_error;
@@ -135,6 +136,14 @@ int ejoin_import_binary(const char* filename, uint32_t dim, double** points_out,
 // radius computations carry an extra relative margin for their own rounding.
 int ejoin_certify_spectral_norm(const float* P, uint32_t k, uint32_t d, double* bound_out) {
     ejoin::clear_error();
+    return ejoin::cert_spectral_norm(P, k, d, bound_out);
+}
+
+}  // extern "C"
+
+namespace ejoin {
+
+int cert_spectral_norm(const float* P, uint32_t k, uint32_t d, double* bound_out) {
     if (!P || !bound_out || k == 0 || d == 0 || k > 256)
         return set_error(EJOIN_EINVAL, "bad arguments");
     const double u = 1.1102230246251565e-16;
@@ -197,4 +206,4 @@ int ejoin_certify_spectral_norm(const float* P, uint32_t k, uint32_t d, double* 
     return EJOIN_OK;
 }
 
-}  // extern "C"
+}  // namespace ejoin

@@ -1,12 +1,510 @@
 // k_learn.cu -- learned contractive projection and tile-pair pruning.
+//
+// New relative to the reference (which has no pruning): a k x d FP32
+// projection P with ||P||_2 <= sigma (certified) gives the guaranteed lower
+// bound  |x_i - x_j| >= |P x_i - P x_j| / sigma.  Points are ordered along the
+// projected coordinates (Morton key over the leading coordinates, or the
+// leading coordinate alone), the 128-row tiles of that order get bounding
+// boxes in projected space (widened by the FP64 rounding bound of each
+// projection), and a tile pair whose boxes are farther apart than
+// sigma * sqrt(T_hi) cannot hold a neighbour pair: the work-list builder
+// (k_misc.cu) drops it before any GEMM.  Skipped tiles contribute 0, which is
+// exact because the bound is rigorous.
+//
+// Training (on the GPU, by this file's kernels):
+//   pairs   sampled by the join: half uniform random pairs, half pairs that
+//           are close in the current projected order (the pairs that decide
+//           whether neighbouring tiles can be skipped); exact FP64 distances
+//   forward y = P v (v = x_i - x_j), r = |y|
+//   loss    hinge on pairs farther than eps: mean max(0, 1 - r / t),
+//           t = min(delta, 2 eps)
+//   backward dL/dP = - sum_active (1 / (M t r)) y v^T
+//   step    Adam, then power-iteration renormalisation P <- P / max(1, s),
+//           s an (inflated) power-iteration estimate of ||P||_2
+// The final certificate is ejoin_certify_spectral_norm (host.cpp).
+#include <cub/cub.cuh>
+
+#include <math.h>
+#include <string.h>
+
+#include <vector>
+
 #include "ejoin_internal.cuh"
 
-using namespace ejoin;
+namespace ejoin {
 
-extern "C" int ejoin_train_projection(const double* points, uint64_t n, uint32_t d, double eps,
-                                      const ejoin_options* opt, float* P_out,
-                                      double* sigma_cert_out, ejoin_stats* stats_out) {
-    (void)points; (void)n; (void)d; (void)eps; (void)opt; (void)P_out; (void)sigma_cert_out;
-    (void)stats_out;
-    return set_error(EJOIN_EUNSUPPORTED, "projection training not available in this build");
+int cert_spectral_norm(const float* P, uint32_t k, uint32_t d, double* out);
+
+namespace {
+
+__host__ __device__ __forceinline__ uint64_t splitmix64(uint64_t x) {
+    x += 0x9E3779B97F4A7C15ull;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    return x ^ (x >> 31);
+}
+
+// ------------------------------------------------------------ projection --
+
+// proj[i][a] = sum_c P[a][c] x[i][c] in FP64 (FP32 P values are exact in
+// FP64), and err[i] >= max_a |computed - exact| = gamma_{d+2} sum_c |P x|.
+// Non-finite rows get NaN (they are never neighbours of anything).
+__global__ void project_kernel(const double* __restrict__ X, uint64_t n, uint32_t d,
+                               const float* __restrict__ P, uint32_t k, double* proj, double* err) {
+    const uint64_t i = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / 32;
+    const int lane = threadIdx.x & 31;
+    if (i >= n) return;
+    const double* x = X + i * d;
+    const double g = (d + 8) * kU * 1.01;
+    double emax = 0.0;
+    bool finite = true;
+    for (uint32_t a = 0; a < k; ++a) {
+        double s = 0.0, sa = 0.0;
+        for (uint32_t c = lane; c < d; c += 32) {
+            const double pc = (double)P[(uint64_t)a * d + c];
+            const double xc = x[c];
+            s = __fma_rn(pc, xc, s);
+            sa += fabs(pc * xc);
+        }
+        for (int o = 16; o; o >>= 1) {
+            s += __shfl_xor_sync(0xffffffffu, s, o);
+            sa += __shfl_xor_sync(0xffffffffu, sa, o);
+        }
+        finite &= isfinite(s) && isfinite(sa);
+        emax = fmax(emax, g * sa);
+        if (lane == 0) proj[i * k + a] = s;
+    }
+    if (lane == 0) {
+        err[i] = finite ? emax * (1 + 8 * kU) : NAN;
+        if (!finite)
+            for (uint32_t a = 0; a < k; ++a) proj[i * k + a] = NAN;
+    }
+}
+
+__device__ __forceinline__ unsigned long long ordered_bits(double v) {
+    unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    return (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double from_ordered_bits(unsigned long long b) {
+    b = (b & 0x8000000000000000ull) ? (b & 0x7fffffffffffffffull) : ~b;
+    return __longlong_as_double((long long)b);
+}
+
+__global__ void range_kernel(const double* __restrict__ proj, uint64_t n, uint32_t k,
+                             unsigned long long* mn, unsigned long long* mx) {
+    const uint32_t a = blockIdx.y;
+    unsigned long long lo = ~0ull, hi = 0ull;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const double v = proj[i * k + a];
+        if (!isnan(v)) {
+            const unsigned long long b = ordered_bits(v);
+            lo = min(lo, b);
+            hi = max(hi, b);
+        }
+    }
+    for (int o = 16; o; o >>= 1) {
+        lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMin(&mn[a], lo);
+        atomicMax(&mx[a], hi);
+    }
+}
+
+// Sort keys: Morton interleave of the leading min(k, 8) coordinates quantised
+// to 64 / m bits each, or the order-preserving bits of coordinate 0.  NaN
+// rows sort last.
+__global__ void key_kernel(const double* __restrict__ proj, uint64_t n, uint32_t k, int lead_only,
+                           const unsigned long long* mn, const unsigned long long* mx,
+                           unsigned long long* keys, uint32_t* idx) {
+    const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    idx[i] = (uint32_t)i;
+    const double p0 = proj[i * k];
+    if (isnan(p0)) {
+        keys[i] = ~0ull;
+        return;
+    }
+    if (lead_only) {
+        keys[i] = ordered_bits(p0);
+        return;
+    }
+    const uint32_t m = k < 8 ? k : 8;
+    const uint32_t bits = 64 / m;
+    unsigned long long key = 0;
+    uint32_t q[8];
+    for (uint32_t a = 0; a < m; ++a) {
+        const double lo = from_ordered_bits(mn[a]), hi = from_ordered_bits(mx[a]);
+        const double span = hi - lo;
+        double t = span > 0 ? (proj[i * k + a] - lo) / span : 0.0;
+        t = fmin(fmax(t, 0.0), 1.0);
+        const double levels = ldexp(1.0, (int)bits) - 1.0;
+        q[a] = (uint32_t)(t * levels);
+    }
+    for (int b = (int)bits - 1; b >= 0; --b)
+        for (uint32_t a = 0; a < m; ++a) key = (key << 1) | ((q[a] >> b) & 1u);
+    keys[i] = key;
+}
+
+// Per 128-row tile of the sorted order: [lo, hi] of every projected
+// coordinate, widened by each row's rounding bound; non-finite and padding
+// rows are left out (they are never neighbours).
+__global__ void boxes_kernel(const double* __restrict__ proj, const double* __restrict__ err,
+                             const uint32_t* __restrict__ perm, uint64_t n, uint32_t k,
+                             double* lo, double* hi) {
+    const uint64_t t = blockIdx.x;
+    for (uint32_t a = threadIdx.y; a < k; a += blockDim.y) {
+        double l = INFINITY, h = -INFINITY;
+        for (uint32_t r = threadIdx.x; r < 128; r += blockDim.x) {
+            const uint64_t p = t * 128 + r;
+            if (p >= n) continue;
+            const uint64_t i = perm[p];
+            const double v = proj[i * k + a], e = err[i];
+            if (isnan(v) || isnan(e)) continue;
+            l = fmin(l, __dsub_rd(v, e));
+            h = fmax(h, __dadd_ru(v, e));
+        }
+        for (int o = 16; o; o >>= 1) {
+            l = fmin(l, __shfl_xor_sync(0xffffffffu, l, o));
+            h = fmax(h, __shfl_xor_sync(0xffffffffu, h, o));
+        }
+        if (threadIdx.x == 0) {
+            lo[t * k + a] = l;
+            hi[t * k + a] = h;
+        }
+    }
+}
+
+// --------------------------------------------------------------- training --
+
+struct PairBatch {
+    float* V;        // [M][d] differences (FP32; training does not need exactness)
+    float* tgt;      // [M] hinge target t (0 = pair not far: inactive)
+};
+
+// Half uniform random pairs, half pairs close in the current order (perm).
+__global__ void sample_pairs_kernel(const double* __restrict__ X, uint64_t n, uint32_t d,
+                                    const uint32_t* __restrict__ perm, uint64_t M, uint64_t seed,
+                                    double eps, uint32_t window, PairBatch pb) {
+    const uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (e >= M) return;
+    const uint64_t h1 = splitmix64(seed ^ (e * 0x9E3779B97F4A7C15ull));
+    const uint64_t h2 = splitmix64(h1);
+    uint64_t i, j;
+    if (e & 1) {
+        i = h1 % n;
+        j = h2 % n;
+    } else {
+        const uint64_t t = h1 % n;
+        uint64_t u = t + 1 + (h2 % window);
+        if (u >= n) u = t >= 1 + (h2 % window) ? t - 1 - (h2 % window) : 0;
+        i = perm ? perm[t] : t;
+        j = perm ? perm[u] : u;
+    }
+    const double* a = X + i * d;
+    const double* b = X + j * d;
+    double s = 0.0;
+    bool fin = true;
+    for (uint32_t c = 0; c < d; ++c) {
+        const double v = a[c] - b[c];
+        fin &= isfinite(v) != 0;
+        s = __fma_rn(v, v, s);
+        pb.V[e * d + c] = (float)v;
+    }
+    const double delta = sqrt(s);
+    float t = 0.0f;
+    if (fin && delta > eps * 1.02) t = (float)fmin(delta, 2.0 * eps);
+    pb.tgt[e] = t;
+}
+
+constexpr int TRAIN_THREADS = 256;
+
+// Forward + hinge loss + backward for a block of pairs; G += dL/dP (atomics),
+// loss += sum of hinge terms.  P in shared memory; k <= K (rows >= k are zero).
+template <int K>
+__global__ void __launch_bounds__(TRAIN_THREADS) train_step_kernel(const float* __restrict__ P,
+                                                                   uint32_t k, uint32_t d,
+                                                                   PairBatch pb, uint64_t M,
+                                                                   float* G, float* loss) {
+    extern __shared__ float sm[];
+    float* sP = sm;                        // k * d
+    float* sC = sm + k * d;                // TRAIN_THREADS * k coefficients
+    for (uint32_t e = threadIdx.x; e < k * d; e += blockDim.x) sP[e] = P[e];
+    __syncthreads();
+    const float invM = 1.0f / (float)M;
+    float lsum = 0.0f;
+    for (uint64_t base = blockIdx.x * (uint64_t)TRAIN_THREADS; base < M;
+         base += (uint64_t)gridDim.x * TRAIN_THREADS) {
+        const uint64_t e = base + threadIdx.x;
+        float y[K];
+        float coef = 0.0f;
+#pragma unroll
+        for (int a = 0; a < K; ++a) y[a] = 0.0f;
+        if (e < M && pb.tgt[e] > 0.0f) {
+            const float* v = pb.V + e * d;
+            for (uint32_t c = 0; c < d; ++c) {
+                const float vc = v[c];
+#pragma unroll
+                for (int a = 0; a < K; ++a)
+                    if (a < (int)k) y[a] = fmaf(sP[a * d + c], vc, y[a]);
+            }
+            float r2 = 0.0f;
+#pragma unroll
+            for (int a = 0; a < K; ++a) r2 = fmaf(y[a], y[a], r2);
+            const float r = sqrtf(r2), t = pb.tgt[e];
+            if (r < t) {
+                lsum += 1.0f - r / t;
+                coef = r > 0.0f ? -invM / (t * r) : 0.0f;
+            }
+        }
+#pragma unroll
+        for (int a = 0; a < K; ++a)
+            if (a < (int)k) sC[threadIdx.x * k + a] = coef != 0.0f ? coef * y[a] : 0.0f;
+        __syncthreads();
+        // G[a][c] += sum_p sC[p][a] * V[p][c]
+        const uint64_t np = (M - base) < TRAIN_THREADS ? (M - base) : TRAIN_THREADS;
+        for (uint32_t el = threadIdx.x; el < k * d; el += blockDim.x) {
+            const uint32_t a = el / d, c = el % d;
+            float acc = 0.0f;
+            for (uint64_t p = 0; p < np; ++p) {
+                const float cf = sC[p * k + a];
+                if (cf != 0.0f) acc = fmaf(cf, pb.V[(base + p) * d + c], acc);
+            }
+            if (acc != 0.0f) atomicAdd(&G[el], acc);
+        }
+        __syncthreads();
+    }
+    for (int o = 16; o; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
+    if ((threadIdx.x & 31) == 0 && lsum != 0.0f) atomicAdd(loss, lsum * invM);
+}
+
+__global__ void adam_kernel(float* P, const float* G, float* m1, float* m2, uint32_t nel, float lr,
+                            float b1, float b2, float c1, float c2) {
+    const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nel) return;
+    const float g = G[e];
+    const float a = b1 * m1[e] + (1.0f - b1) * g;
+    const float b = b2 * m2[e] + (1.0f - b2) * g * g;
+    m1[e] = a;
+    m2[e] = b;
+    P[e] -= lr * (a / c1) / (sqrtf(b / c2) + 1e-8f);
+}
+
+// Power iteration on P P^T (k x k), then P /= max(1, 1.02 * sigma_est).
+// One block; k <= 16.
+__global__ void renorm_kernel(float* P, uint32_t k, uint32_t d, float* sigma_out) {
+    __shared__ double M[16 * 16];
+    __shared__ double v[16], w[16];
+    __shared__ double lam;
+    for (uint32_t e = threadIdx.x; e < k * k; e += blockDim.x) {
+        const uint32_t a = e / k, b = e % k;
+        double s = 0.0;
+        for (uint32_t c = 0; c < d; ++c) s += (double)P[a * d + c] * (double)P[b * d + c];
+        M[e] = s;
+    }
+    if (threadIdx.x < k) v[threadIdx.x] = 1.0 + 0.01 * threadIdx.x;
+    __syncthreads();
+    for (int it = 0; it < 40; ++it) {
+        if (threadIdx.x < k) {
+            double s = 0.0;
+            for (uint32_t b = 0; b < k; ++b) s += M[threadIdx.x * k + b] * v[b];
+            w[threadIdx.x] = s;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double nn = 0.0;
+            for (uint32_t b = 0; b < k; ++b) nn += w[b] * w[b];
+            lam = sqrt(nn);
+            const double inv = lam > 0 ? 1.0 / lam : 0.0;
+            for (uint32_t b = 0; b < k; ++b) v[b] = w[b] * inv;
+        }
+        __syncthreads();
+    }
+    const float sig = (float)(sqrt(lam) * 1.02);
+    const float scale = sig > 1.0f ? 1.0f / sig : 1.0f;
+    for (uint32_t e = threadIdx.x; e < k * d; e += blockDim.x) P[e] *= scale;
+    if (threadIdx.x == 0 && sigma_out) *sigma_out = sig;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------ host side --
+
+// Projects all points with P (host k x d), orders them and computes the tile
+// boxes.  perm (n entries, sorted position -> original row), lo/hi
+// ([n_pad/128][k]) are allocated here.
+int learned_order(const double* X, uint64_t n, uint64_t n_pad, uint32_t d, const float* P_dev,
+                  uint32_t k, int lead_only, DBuf<uint32_t>& perm, DBuf<double>* lo,
+                  DBuf<double>* hi, cudaStream_t s) {
+    DBuf<double> proj, err;
+    EJ_TRY(proj.alloc(n * k, s, "projections"));
+    EJ_TRY(err.alloc(n, s, "projection error bounds"));
+    project_kernel<<<(unsigned)((n * 32 + 255) / 256), 256, 0, s>>>(X, n, d, P_dev, k, proj.p, err.p);
+    EJ_CUDA(cudaGetLastError());
+    note_launch();
+    DBuf<unsigned long long> rng;
+    EJ_TRY(rng.alloc(2 * k, s, "projection ranges"));
+    EJ_CUDA(cudaMemsetAsync(rng.p, 0xff, k * sizeof(unsigned long long), s));
+    EJ_CUDA(cudaMemsetAsync(rng.p + k, 0, k * sizeof(unsigned long long), s));
+    range_kernel<<<dim3(256, k), 256, 0, s>>>(proj.p, n, k, rng.p, rng.p + k);
+    EJ_CUDA(cudaGetLastError());
+    note_launch();
+    DBuf<unsigned long long> keys, keys2;
+    DBuf<uint32_t> idx;
+    EJ_TRY(keys.alloc(n, s, "sort keys"));
+    EJ_TRY(keys2.alloc(n, s, "sorted keys"));
+    EJ_TRY(idx.alloc(n, s, "sort values"));
+    EJ_TRY(perm.alloc(n, s, "permutation"));
+    key_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(proj.p, n, k, lead_only, rng.p,
+                                                           rng.p + k, keys.p, idx.p);
+    EJ_CUDA(cudaGetLastError());
+    note_launch();
+    size_t tmp_bytes = 0;
+    EJ_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, keys.p, keys2.p, idx.p, perm.p,
+                                            (int)n, 0, 64, s));
+    DBuf<uint8_t> tmp;
+    EJ_TRY(tmp.alloc(tmp_bytes, s, "sort scratch"));
+    EJ_CUDA(cub::DeviceRadixSort::SortPairs(tmp.p, tmp_bytes, keys.p, keys2.p, idx.p, perm.p,
+                                            (int)n, 0, 64, s));
+    note_launch(8);  // onesweep passes (library kernels, counted approximately)
+    if (lo && hi) {
+        const uint64_t nt = n_pad / 128;
+        EJ_TRY(lo->alloc(nt * k, s, "tile boxes"));
+        EJ_TRY(hi->alloc(nt * k, s, "tile boxes"));
+        boxes_kernel<<<(unsigned)nt, dim3(32, 8), 0, s>>>(proj.p, err.p, perm.p, n, k, lo->p, hi->p);
+        EJ_CUDA(cudaGetLastError());
+        note_launch();
+    }
+    return EJOIN_OK;
+}
+
+int train_projection_dev(const double* X, uint64_t n, uint32_t d, double eps, uint32_t k,
+                         uint64_t pairs, uint32_t steps, uint64_t seed, int lead_only,
+                         cudaStream_t s, TrainResult& out) {
+    if (k == 0 || k > 16) return set_error(EJOIN_EINVAL, "proj_k must be in 1..16");
+    if (n < 2) return set_error(EJOIN_EINVAL, "training needs at least 2 points");
+    const uint32_t nel = k * d;
+    // seeded Gaussian initialisation (Box-Muller on splitmix64), then certified scaling
+    std::vector<float> P0(nel);
+    for (uint32_t e = 0; e < nel; ++e) {
+        const uint64_t a = splitmix64(seed * 0x2545F4914F6CDD1Dull + 2 * e);
+        const uint64_t b = splitmix64(seed * 0x2545F4914F6CDD1Dull + 2 * e + 1);
+        const double u1 = ((a >> 11) + 1.0) * (1.0 / 9007199254740993.0);
+        const double u2 = (b >> 11) * (1.0 / 9007199254740992.0);
+        P0[e] = (float)(sqrt(-2.0 * log(u1)) * cos(6.283185307179586 * u2));
+    }
+    double s0 = 0;
+    EJ_TRY(cert_spectral_norm(P0.data(), k, d, &s0));
+    for (auto& v : P0) v = (float)(v / (s0 * 1.0001));
+    DBuf<float> P, G, m1, m2, loss, sig;
+    EJ_TRY(P.alloc(nel, s, "projection"));
+    EJ_TRY(G.alloc(nel, s, "gradient"));
+    EJ_TRY(m1.alloc(nel, s, "adam m"));
+    EJ_TRY(m2.alloc(nel, s, "adam v"));
+    EJ_TRY(loss.alloc(steps + 1, s, "loss"));
+    EJ_TRY(sig.alloc(1, s, "sigma"));
+    EJ_CUDA(cudaMemcpyAsync(P.p, P0.data(), nel * sizeof(float), cudaMemcpyHostToDevice, s));
+    EJ_TRY(m1.zero(s));
+    EJ_TRY(m2.zero(s));
+    EJ_TRY(loss.zero(s));
+    const uint64_t M = pairs ? pairs : (1u << 20);
+    DBuf<float> V, tgt;
+    EJ_TRY(V.alloc(M * d, s, "training pair differences"));
+    EJ_TRY(tgt.alloc(M, s, "training pair targets"));
+    PairBatch pb{V.p, tgt.p};
+    const uint32_t rounds = steps >= 4 ? 4 : (steps ? steps : 1);
+    const uint64_t n_pad = (n + 127) / 128 * 128;
+    const float b1 = 0.9f, b2 = 0.999f;
+    const float lr = 0.02f;
+    const size_t shm = (size_t)(k * d + TRAIN_THREADS * k) * sizeof(float);
+    if (shm > 200 * 1024) return set_error(EJOIN_EUNSUPPORTED, "projection too large for training");
+    auto step_fn = k <= 8 ? train_step_kernel<8> : train_step_kernel<16>;
+    EJ_CUDA(cudaFuncSetAttribute(step_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
+    uint32_t t_step = 0;
+    for (uint32_t r = 0; r < rounds; ++r) {
+        DBuf<uint32_t> perm;
+        EJ_TRY(learned_order(X, n, n_pad, d, P.p, k, lead_only, perm, nullptr, nullptr, s));
+        sample_pairs_kernel<<<(unsigned)((M + 255) / 256), 256, 0, s>>>(
+            X, n, d, perm.p, M, seed + 7919ull * (r + 1), eps, 256, pb);
+        EJ_CUDA(cudaGetLastError());
+        note_launch();
+        const uint32_t nsteps = steps / rounds + (r < steps % rounds ? 1 : 0);
+        for (uint32_t it = 0; it < nsteps; ++it, ++t_step) {
+            EJ_TRY(G.zero(s));
+            step_fn<<<304, TRAIN_THREADS, shm, s>>>(P.p, k, d, pb, M, G.p, loss.p + t_step);
+            EJ_CUDA(cudaGetLastError());
+            const float c1 = 1.0f - powf(b1, (float)(t_step + 1));
+            const float c2 = 1.0f - powf(b2, (float)(t_step + 1));
+            adam_kernel<<<(nel + 255) / 256, 256, 0, s>>>(P.p, G.p, m1.p, m2.p, nel, lr, b1, b2,
+                                                          c1, c2);
+            EJ_CUDA(cudaGetLastError());
+            renorm_kernel<<<1, 256, 0, s>>>(P.p, k, d, sig.p);
+            EJ_CUDA(cudaGetLastError());
+            note_launch(3);
+        }
+    }
+    out.P.resize(nel);
+    std::vector<float> L(steps ? steps : 1);
+    EJ_CUDA(cudaMemcpyAsync(out.P.data(), P.p, nel * sizeof(float), cudaMemcpyDeviceToHost, s));
+    EJ_CUDA(cudaMemcpyAsync(L.data(), loss.p, L.size() * sizeof(float), cudaMemcpyDeviceToHost, s));
+    EJ_CUDA(cudaStreamSynchronize(s));
+    out.loss_first = L.front();
+    out.loss_last = L.back();
+    EJ_TRY(cert_spectral_norm(out.P.data(), k, d, &out.sigma_cert));
+    return EJOIN_OK;
+}
+
+}  // namespace ejoin
+
+// ------------------------------------------------------------ test hooks --
+
+extern "C" int ejoin_testing_projection_grad(const float* V, const float* tgt, uint64_t M,
+                                             const float* P, uint32_t k, uint32_t d, float* G_out,
+                                             float* loss_out) {
+    using namespace ejoin;
+    clear_error();
+    if (!V || !tgt || !P || !G_out || !loss_out || k == 0 || k > 16 || d == 0 || M == 0)
+        return set_error(EJOIN_EINVAL, "bad arguments");
+    cudaStream_t s = cudaStreamPerThread;
+    DBuf<float> dV, dT, dP, dG, dL;
+    EJ_TRY(dV.alloc(M * d, s, "V"));
+    EJ_TRY(dT.alloc(M, s, "targets"));
+    EJ_TRY(dP.alloc((size_t)k * d, s, "P"));
+    EJ_TRY(dG.alloc((size_t)k * d, s, "G"));
+    EJ_TRY(dL.alloc(1, s, "loss"));
+    EJ_CUDA(cudaMemcpyAsync(dV.p, V, M * d * sizeof(float), cudaMemcpyHostToDevice, s));
+    EJ_CUDA(cudaMemcpyAsync(dT.p, tgt, M * sizeof(float), cudaMemcpyHostToDevice, s));
+    EJ_CUDA(cudaMemcpyAsync(dP.p, P, (size_t)k * d * sizeof(float), cudaMemcpyHostToDevice, s));
+    EJ_TRY(dG.zero(s));
+    EJ_TRY(dL.zero(s));
+    const size_t shm = (size_t)(k * d + TRAIN_THREADS * k) * sizeof(float);
+    auto fn = k <= 8 ? train_step_kernel<8> : train_step_kernel<16>;
+    EJ_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
+    PairBatch pb{dV.p, dT.p};
+    fn<<<64, TRAIN_THREADS, shm, s>>>(dP.p, k, d, pb, M, dG.p, dL.p);
+    EJ_CUDA(cudaGetLastError());
+    EJ_CUDA(cudaMemcpyAsync(G_out, dG.p, (size_t)k * d * sizeof(float), cudaMemcpyDeviceToHost, s));
+    EJ_CUDA(cudaMemcpyAsync(loss_out, dL.p, sizeof(float), cudaMemcpyDeviceToHost, s));
+    EJ_CUDA(cudaStreamSynchronize(s));
+    return EJOIN_OK;
+}
+
+extern "C" int ejoin_testing_renormalise(float* P, uint32_t k, uint32_t d, float* sigma_est_out) {
+    using namespace ejoin;
+    clear_error();
+    if (!P || k == 0 || k > 16 || d == 0) return set_error(EJOIN_EINVAL, "bad arguments");
+    cudaStream_t s = cudaStreamPerThread;
+    DBuf<float> dP, dS;
+    EJ_TRY(dP.alloc((size_t)k * d, s, "P"));
+    EJ_TRY(dS.alloc(1, s, "sigma"));
+    EJ_CUDA(cudaMemcpyAsync(dP.p, P, (size_t)k * d * sizeof(float), cudaMemcpyHostToDevice, s));
+    renorm_kernel<<<1, 256, 0, s>>>(dP.p, k, d, dS.p);
+    EJ_CUDA(cudaGetLastError());
+    EJ_CUDA(cudaMemcpyAsync(P, dP.p, (size_t)k * d * sizeof(float), cudaMemcpyDeviceToHost, s));
+    if (sigma_est_out)
+        EJ_CUDA(cudaMemcpyAsync(sigma_est_out, dS.p, sizeof(float), cudaMemcpyDeviceToHost, s));
+    EJ_CUDA(cudaStreamSynchronize(s));
+    return EJOIN_OK;
 }
