@@ -244,7 +244,9 @@ def train_projection(points, eps: float, k: int = 8, device: int = 0, **kw):
     _check(L.ejoin_train_projection(ptr, n, d, float(eps), ctypes.byref(o), P.ctypes.data,
                                     ctypes.byref(sig), ctypes.byref(st)))
     del keep
-    return P, sig.value, st.as_dict()
+    info = st.as_dict()
+    info["loss_first"], info["loss_last"] = st.reserved[0], st.reserved[1]
+    return P, sig.value, info
 
 
 def certify_spectral_norm(P) -> float:

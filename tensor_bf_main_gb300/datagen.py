@@ -34,8 +34,8 @@ CONFIGS = {
     "c2": dict(n=1_000_000, d=128, kind="gmm", k=64, sigma=0.05, target=64),
     "c3": dict(n=2_000_000, d=256, kind="powerlaw", target=(16, 128, 1024)),
     "c4": dict(n=4_000_000, d=64, kind="latent", k=256, latent=8, sigma=0.02, noise=0.01,
-               target=50),
-    "c5": dict(n=1_000_000, d=1024, kind="sphere", k=1000, target=20),
+               target=50, proj_k=8),
+    "c5": dict(n=1_000_000, d=1024, kind="sphere", k=1000, target=20, proj_k=16),
 }
 
 # Frozen radii (see calibrate()); c3 holds one radius per target mean.
