@@ -293,9 +293,11 @@ __global__ void adam_kernel(float* P, const float* G, float* m1, float* m2, uint
 }
 
 // Power iteration on P P^T (k x k), then P /= max(1, 1.02 * sigma_est).
-// One block; k <= 16.
+// The iteration runs on (P P^T)^32, formed by five normalised squarings, so it
+// converges even when the leading eigenvalues are close; the estimate is the
+// Rayleigh quotient of the original P P^T.  One block; k <= 16.
 __global__ void renorm_kernel(float* P, uint32_t k, uint32_t d, float* sigma_out) {
-    __shared__ double M[16 * 16];
+    __shared__ double M[16 * 16], A[16 * 16], B[16 * 16];
     __shared__ double v[16], w[16];
     __shared__ double lam;
     for (uint32_t e = threadIdx.x; e < k * k; e += blockDim.x) {
@@ -303,26 +305,52 @@ __global__ void renorm_kernel(float* P, uint32_t k, uint32_t d, float* sigma_out
         double s = 0.0;
         for (uint32_t c = 0; c < d; ++c) s += (double)P[a * d + c] * (double)P[b * d + c];
         M[e] = s;
+        A[e] = s;
+    }
+    __syncthreads();
+    for (int sq = 0; sq < 5; ++sq) {
+        double mx = 0.0;
+        for (uint32_t e = 0; e < k * k; ++e) mx = fmax(mx, fabs(A[e]));
+        const double inv = mx > 0 ? 1.0 / mx : 0.0;
+        for (uint32_t e = threadIdx.x; e < k * k; e += blockDim.x) {
+            const uint32_t a = e / k, b = e % k;
+            double s = 0.0;
+            for (uint32_t c = 0; c < k; ++c) s += (A[a * k + c] * inv) * (A[c * k + b] * inv);
+            B[e] = s;
+        }
+        __syncthreads();
+        for (uint32_t e = threadIdx.x; e < k * k; e += blockDim.x) A[e] = B[e];
+        __syncthreads();
     }
     if (threadIdx.x < k) v[threadIdx.x] = 1.0 + 0.01 * threadIdx.x;
     __syncthreads();
-    for (int it = 0; it < 40; ++it) {
+    for (int it = 0; it < 8; ++it) {
         if (threadIdx.x < k) {
             double s = 0.0;
-            for (uint32_t b = 0; b < k; ++b) s += M[threadIdx.x * k + b] * v[b];
+            for (uint32_t b = 0; b < k; ++b) s += A[threadIdx.x * k + b] * v[b];
             w[threadIdx.x] = s;
         }
         __syncthreads();
         if (threadIdx.x == 0) {
             double nn = 0.0;
             for (uint32_t b = 0; b < k; ++b) nn += w[b] * w[b];
-            lam = sqrt(nn);
-            const double inv = lam > 0 ? 1.0 / lam : 0.0;
+            const double inv = nn > 0 ? 1.0 / sqrt(nn) : 0.0;
             for (uint32_t b = 0; b < k; ++b) v[b] = w[b] * inv;
         }
         __syncthreads();
     }
-    const float sig = (float)(sqrt(lam) * 1.02);
+    if (threadIdx.x == 0) {
+        double num = 0.0, den = 0.0;
+        for (uint32_t a = 0; a < k; ++a) {
+            double s = 0.0;
+            for (uint32_t b = 0; b < k; ++b) s += M[a * k + b] * v[b];
+            num += v[a] * s;
+            den += v[a] * v[a];
+        }
+        lam = den > 0 ? num / den : 0.0;
+    }
+    __syncthreads();
+    const float sig = (float)(sqrt(fmax(lam, 0.0)) * 1.02);
     const float scale = sig > 1.0f ? 1.0f / sig : 1.0f;
     for (uint32_t e = threadIdx.x; e < k * d; e += blockDim.x) P[e] *= scale;
     if (threadIdx.x == 0 && sigma_out) *sigma_out = sig;
