@@ -344,7 +344,9 @@ static double screen_scale(Fmt f, double maxabs, uint32_t d) {
     return ldexp(1.0, e);
 }
 
-static int run_screen16(Join& J, Fmt fmt, bool split) {
+// L owns the permutation that J.perm points to; it must outlive the final
+// scatter of the counts, so the caller keeps it.
+static int run_screen16(Join& J, Fmt fmt, bool split, Learned& L) {
     EventTimer tp, tg, tr;
     tp.start(J.s);
     DBuf<uint8_t> bad;
@@ -357,7 +359,6 @@ static int run_screen16(Join& J, Fmt fmt, bool split) {
     tp.stop(J.s);
     const double ms_center = tp.ms();
     const uint64_t n_pad = round_up(J.n, 128);
-    Learned L;
     if (J.opt.proj_k) EJ_TRY(prepare_learned(J, n_pad, L));
     tp.start(J.s);
     ScreenParams P;
@@ -466,6 +467,7 @@ static int self_join_impl(const double* points, uint64_t n, uint32_t d, double e
     J.perm = nullptr;
     DBuf<double> xbuf;
     DBuf<int32_t> cbuf;
+    Learned learned;  // owns J.perm when the learned ordering is used
     const uint64_t n_pad = round_up(std::max<uint64_t>(n, 1), 128);
     EJ_TRY(cbuf.alloc(n_pad, s, "counts"));
     EJ_TRY(cbuf.zero(s));
@@ -478,9 +480,9 @@ static int self_join_impl(const double* points, uint64_t n, uint32_t d, double e
         switch (prec) {
             case EJOIN_FP64_DIRECT: EJ_TRY(run_direct(J)); break;
             case EJOIN_FP64_DMMA: EJ_TRY(run_dmma(J)); break;
-            case EJOIN_FP16: EJ_TRY(run_screen16(J, Fmt::FP16, false)); break;
-            case EJOIN_BF16: EJ_TRY(run_screen16(J, Fmt::BF16, false)); break;
-            case EJOIN_BF16_SPLIT: EJ_TRY(run_screen16(J, Fmt::BF16, true)); break;
+            case EJOIN_FP16: EJ_TRY(run_screen16(J, Fmt::FP16, false, learned)); break;
+            case EJOIN_BF16: EJ_TRY(run_screen16(J, Fmt::BF16, false, learned)); break;
+            case EJOIN_BF16_SPLIT: EJ_TRY(run_screen16(J, Fmt::BF16, true, learned)); break;
             case EJOIN_FP8_E4M3:
                 return set_error(EJOIN_EUNSUPPORTED, "FP8 screen not available in this build");
             default: return set_error(EJOIN_EINVAL, "unknown precision %d", prec);
