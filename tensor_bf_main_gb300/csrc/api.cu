@@ -196,14 +196,14 @@ static uint64_t band_budget(uint64_t want) {
 }
 
 // Runs `screen` (which fills counts and the band queue), re-running it with a
-// larger queue on overflow, then rechecks the band in FP64.
-template <typename Screen>
-static int screen_and_recheck(Join& J, uint64_t cap0, Screen&& screen, uint64_t n_pad,
-                              EventTimer& tg, EventTimer& tr) {
+// larger queue on overflow, then `recheck` resolves the band exactly.
+template <typename Screen, typename Recheck>
+static int screen_and_recheck(Join& J, uint64_t cap0, Screen&& screen, Recheck&& recheck,
+                              uint64_t n_pad, EventTimer& tg, EventTimer& tr) {
     DBuf<BandPair> band;
     DBuf<DevStatus> dst;
     EJ_TRY(dst.alloc(1, J.s, "status"));
-    uint64_t cap = band_budget(cap0);
+    uint64_t cap = band_budget(J.opt.band_capacity ? J.opt.band_capacity : cap0);
     for (int attempt = 0;; ++attempt) {
         EJ_TRY(band.alloc(cap, J.s, "band queue"));
         EJ_TRY(dst.zero(J.s));
@@ -218,12 +218,13 @@ static int screen_and_recheck(Join& J, uint64_t cap0, Screen&& screen, uint64_t 
             return set_error(EJOIN_ETIMEOUT, "Gram kernel: a bounded device wait expired (site %u)", h.where);
         if (h.band_count <= cap) {
             tr.start(J.s);
-            EJ_TRY(launch_band_recheck(J.X, J.n, J.d, J.perm, J.T, band.p, h.band_count, J.counts, dst.p, J.s));
+            EJ_TRY(recheck(band.p, h.band_count, dst.p));
             tr.stop(J.s);
             EJ_CUDA(cudaMemcpyAsync(&h, dst.p, sizeof h, cudaMemcpyDeviceToHost, J.s));
             EJ_CUDA(cudaStreamSynchronize(J.s));
             J.st->band_pairs = h.band_count;
             J.st->band_hits = h.band_hits;
+            J.st->reserved[0] = (double)h.exact_rechecks;
             J.st->ms_gram = tg.ms();
             J.st->ms_recheck = tr.ms();
             return EJOIN_OK;
@@ -284,7 +285,10 @@ static int run_dmma(Join& J) {
     auto screen = [&](BandPair* band, uint64_t cap, DevStatus* st) {
         return launch_dmma_join(Y.p, n_pad, P.dp, h.p, g.p, J.counts, band, cap, st, J.s);
     };
-    return screen_and_recheck(J, std::max<uint64_t>(1u << 20, J.n), screen, n_pad, tg, tr);
+    auto recheck = [&](const BandPair* band, uint64_t nb, DevStatus* st) {
+        return launch_band_recheck(J.X, J.n, J.d, J.perm, J.T, band, nb, J.counts, st, J.s);
+    };
+    return screen_and_recheck(J, std::max<uint64_t>(1u << 20, J.n), screen, recheck, n_pad, tg, tr);
 }
 
 // Learned ordering: projection P (given or trained on the GPU), its certified
@@ -294,12 +298,12 @@ static int run_dmma(Join& J) {
 // delta^2 >= gap^2 / sigma^2 > T_hi, i.e. d2 > T.
 struct Learned {
     DBuf<uint32_t> perm;
-    DBuf<double> lo, hi;
-    double thr = 0.0;
+    LearnedBoxes boxes;
+    float thr = 0.0f;
     uint32_t k = 0;
 };
 
-static int prepare_learned(Join& J, uint64_t n_pad, Learned& L) {
+static int prepare_learned(Join& J, const double* mu, uint64_t n_pad, Learned& L) {
     const uint32_t k = J.opt.proj_k;
     if (k == 0 || k > 16) return set_error(EJOIN_EINVAL, "proj_k must be in 0..16 (got %u)", k);
     EventTimer tt, to;
@@ -311,8 +315,9 @@ static int prepare_learned(Join& J, uint64_t n_pad, Learned& L) {
         EJ_TRY(cert_spectral_norm(P.data(), k, J.d, &sigma));
     } else {
         TrainResult tr;
-        EJ_TRY(train_projection_dev(J.X, J.n, J.d, J.eps, k, J.opt.train_pairs, J.opt.train_steps,
-                                    J.opt.seed, J.opt.order == EJOIN_ORDER_LEAD, J.s, tr));
+        EJ_TRY(train_projection_dev(J.X, mu, J.n, J.d, J.eps, k, J.opt.train_pairs,
+                                    J.opt.train_steps, J.opt.seed, J.opt.order == EJOIN_ORDER_LEAD,
+                                    J.s, tr));
         P.swap(tr.P);
         sigma = tr.sigma_cert;
     }
@@ -321,12 +326,17 @@ static int prepare_learned(Join& J, uint64_t n_pad, Learned& L) {
     DBuf<float> Pd;
     EJ_TRY(Pd.alloc(P.size(), J.s, "projection"));
     EJ_CUDA(cudaMemcpyAsync(Pd.p, P.data(), P.size() * sizeof(float), cudaMemcpyHostToDevice, J.s));
-    EJ_TRY(learned_order(J.X, J.n, n_pad, J.d, Pd.p, k, J.opt.order == EJOIN_ORDER_LEAD, L.perm,
-                         &L.lo, &L.hi, J.s));
+    EJ_TRY(learned_order(J.X, mu, J.n, n_pad, J.d, Pd.p, k, J.opt.order == EJOIN_ORDER_LEAD,
+                         L.perm, &L.boxes, J.s));
     to.stop(J.s);
     double Tlo, Thi;
     oracle_band(J.T, J.d, &Tlo, &Thi);
-    L.thr = Thi * sigma * sigma * (1.0 + 32 * kU);
+    // FP32 threshold rounded up: the box-gap test then never prunes a pair
+    // that the exact bound would keep
+    const double thr = Thi * sigma * sigma * (1.0 + 32 * kU);
+    float tf = (float)thr;
+    if ((double)tf < thr) tf = nextafterf(tf, INFINITY);
+    L.thr = tf;
     L.k = k;
     J.perm = L.perm.p;
     J.st->sigma_cert = sigma;
@@ -359,7 +369,7 @@ static int run_screen16(Join& J, Fmt fmt, bool split, Learned& L) {
     tp.stop(J.s);
     const double ms_center = tp.ms();
     const uint64_t n_pad = round_up(J.n, 128);
-    if (J.opt.proj_k) EJ_TRY(prepare_learned(J, n_pad, L));
+    if (J.opt.proj_k) EJ_TRY(prepare_learned(J, mu.p, n_pad, L));
     tp.start(J.s);
     ScreenParams P;
     P.fmt = fmt;
@@ -385,11 +395,13 @@ static int run_screen16(Join& J, Fmt fmt, bool split, Learned& L) {
     P.absacc = (kprod + 16.0) * ldexp(1.0, -125);
     P.clamp_lo = (fmt == Fmt::FP16) ? -16384.0 : -kTwo100;
     DBuf<uint16_t> Q;
-    DBuf<float> beta, tmax;
+    DBuf<float> beta, tmax, Xf, rad;
     EJ_TRY(Q.alloc(n_pad * P.width, J.s, "packed operands"));
     EJ_TRY(beta.alloc(n_pad, J.s, "out margins"));
     EJ_TRY(tmax.alloc(n_pad / 128, J.s, "tile margins"));
-    EJ_TRY(launch_pack16(J.X, J.n, n_pad, J.perm, bad.p, mu.p, P, Q.p, beta.p, J.s));
+    EJ_TRY(Xf.alloc(n_pad * J.d, J.s, "FP32 coordinates"));
+    EJ_TRY(rad.alloc(n_pad, J.s, "FP32 radii"));
+    EJ_TRY(launch_pack16(J.X, J.n, n_pad, J.perm, bad.p, mu.p, P, Q.p, beta.p, Xf.p, rad.p, J.s));
     EJ_TRY(launch_tile_max(beta.p, nullptr, n_pad, tmax.p, J.s));
     tp.stop(J.s);
     J.st->ms_prep = ms_center + tp.ms();
@@ -398,8 +410,7 @@ static int run_screen16(Join& J, Fmt fmt, bool split, Learned& L) {
     uint64_t nwork = 0;
     EventTimer tw;
     tw.start(J.s);
-    EJ_TRY(build_worklist(nT, L.k ? L.lo.p : nullptr, L.k ? L.hi.p : nullptr, L.k, L.thr, work,
-                          &nwork, nullptr, J.s));
+    EJ_TRY(build_worklist(nT, L.k ? &L.boxes : nullptr, L.thr, work, &nwork, J.s));
     tw.stop(J.s);
     J.st->ms_order += tw.ms();
     J.st->tile_pairs_total = nT * (nT + 1) / 2;
@@ -410,8 +421,18 @@ static int run_screen16(Join& J, Fmt fmt, bool split, Learned& L) {
         return launch_gram16(Q.p, n_pad, P, work.p, nwork, tmax.p, J.counts, band, cap, st, J.sms,
                              J.s);
     };
+    Recheck32 R;
+    R.Xf = Xf.p;
+    R.rad = rad.p;
+    R.sTlo = P.sTlo;
+    R.sThi = P.sThi;
+    R.c32 = (J.d + 8) * ldexp(1.0, -24) * 1.01;
+    R.abs32 = (J.d + 8) * ldexp(1.0, -148);
+    auto recheck = [&](const BandPair* band, uint64_t nb, DevStatus* st) {
+        return launch_band_recheck2(J.X, J.n, J.d, J.perm, J.T, R, band, nb, J.counts, st, J.s);
+    };
     const uint64_t cap0 = std::max<uint64_t>(1u << 22, 32 * J.n);
-    return screen_and_recheck(J, cap0, screen, n_pad, tg, tr);
+    return screen_and_recheck(J, cap0, screen, recheck, n_pad, tg, tr);
 }
 
 static int resolve_precision(int p, uint32_t d) {
@@ -618,9 +639,16 @@ int ejoin_train_projection(const double* points, uint64_t n, uint32_t d, double 
     EJ_TRY(stage_points(points, n, d, ld, xbuf, &X, s));
     EventTimer t;
     t.start(s);
+    DBuf<uint8_t> bad;
+    DBuf<double> mu;
+    EJ_TRY(bad.alloc(n, s, "row flags"));
+    EJ_TRY(mu.alloc(d, s, "mean"));
+    double maxabs = 0;
+    uint64_t ngood = 0;
+    EJ_TRY(launch_center_stats(X, n, d, bad.p, mu.p, &maxabs, &ngood, s));
     TrainResult tr;
-    EJ_TRY(train_projection_dev(X, n, d, eps, opt.proj_k, opt.train_pairs, opt.train_steps, opt.seed,
-                                opt.order == EJOIN_ORDER_LEAD, s, tr));
+    EJ_TRY(train_projection_dev(X, mu.p, n, d, eps, opt.proj_k, opt.train_pairs, opt.train_steps,
+                                opt.seed, opt.order == EJOIN_ORDER_LEAD, s, tr));
     t.stop(s);
     memcpy(P_out, tr.P.data(), tr.P.size() * sizeof(float));
     if (sigma_cert_out) *sigma_cert_out = tr.sigma_cert;

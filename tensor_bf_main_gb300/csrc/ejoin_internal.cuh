@@ -116,6 +116,16 @@ struct DevStatus {
     unsigned int where;
     unsigned long long band_count;  // band pairs produced (may exceed capacity)
     unsigned long long band_hits;
+    unsigned long long exact_rechecks;  // band pairs the FP32 pre-check left to FP64
+};
+
+// Constants of the FP32 band pre-check (scaled space of the 16-bit screen).
+struct Recheck32 {
+    const float* Xf;   // [n_pad][d] FP32 coordinates, packed order
+    const float* rad;  // per-row radius (|zf - s (x - mu)| bound; inf = undecidable row)
+    double sTlo, sThi; // sqrt of the scaled oracle thresholds (down / up)
+    double c32;        // relative bound of the FP32 squared-difference sum
+    double abs32;      // absolute bound (FP32 underflow)
 };
 
 // --------------------------------------------------------- device math --
@@ -192,6 +202,14 @@ struct DmmaParams {
     uint32_t d, dp;
 };
 
+// Boxes of the projected 128-row tiles and of super-blocks of kSuperTiles
+// consecutive tiles ([tiles][k] FP32, outward rounded).
+constexpr uint32_t kSuperTiles = 16;
+struct LearnedBoxes {
+    DBuf<float> lo, hi, slo, shi;
+    uint32_t k = 0;
+};
+
 // --------------------------------------------------- host entry points --
 // (implemented in the kernel translation units)
 
@@ -217,8 +235,11 @@ int launch_gram16(const void* Q, uint64_t n_pad, const ScreenParams& P, const ui
                   uint64_t band_cap, DevStatus* st, int num_sms, cudaStream_t s);
 
 // k_misc.cu
-int build_worklist(uint64_t nT, const double* lo, const double* hi, uint32_t k, double thr,
-                   DBuf<uint2>& work, uint64_t* nwork_out, uint64_t* ncand_out, cudaStream_t s);
+// Ordered list of the upper-triangle 128-row tile pairs (I <= J), grouped by
+// super-block pairs; with `boxes`, pairs whose squared box gap exceeds thr
+// are dropped (super-block pairs first).
+int build_worklist(uint64_t nT, const LearnedBoxes* boxes, float thr, DBuf<uint2>& work,
+                   uint64_t* nwork_out, cudaStream_t s);
 int sum_counts(const int32_t* counts, uint64_t n, unsigned long long* dev_total, cudaStream_t s);
 int scatter_counts(const int32_t* src, const uint32_t* perm, uint64_t n, int32_t* dst,
                    cudaStream_t s);
@@ -229,14 +250,18 @@ struct TrainResult {
     double loss_first = 0, loss_last = 0;
     double sigma_cert = 0;
 };
-int train_projection_dev(const double* X, uint64_t n, uint32_t d, double eps, uint32_t k,
-                         uint64_t pairs, uint32_t steps, uint64_t seed, int lead_only,
+int train_projection_dev(const double* X, const double* mu, uint64_t n, uint32_t d, double eps,
+                         uint32_t k, uint64_t pairs, uint32_t steps, uint64_t seed, int lead_only,
                          cudaStream_t s, TrainResult& out);
-int learned_order(const double* X, uint64_t n, uint64_t n_pad, uint32_t d, const float* P_dev,
-                  uint32_t k, int lead_only, DBuf<uint32_t>& perm, DBuf<double>* lo,
-                  DBuf<double>* hi, cudaStream_t s);
+int learned_order(const double* X, const double* mu, uint64_t n, uint64_t n_pad, uint32_t d,
+                  const float* P_dev, uint32_t k, int lead_only, DBuf<uint32_t>& perm,
+                  LearnedBoxes* boxes, cudaStream_t s);
 // host.cpp: certified upper bound of ||P||_2
 int cert_spectral_norm(const float* P, uint32_t k, uint32_t d, double* out);
+
+int launch_band_recheck2(const double* X, uint64_t n, uint32_t d, const uint32_t* perm, double T,
+                         const Recheck32& R, const BandPair* band, uint64_t nband, int32_t* counts,
+                         DevStatus* st, cudaStream_t s);
 
 // k_prep.cu
 // bad[i] = 1 for rows with a non-finite coordinate; mean over the good rows
@@ -247,10 +272,11 @@ int launch_center_stats(const double* X, uint64_t n, uint32_t d, uint8_t* bad, d
 int launch_pack_dmma(const double* X, uint64_t n, uint64_t n_pad, const uint32_t* perm,
                      const uint8_t* bad, const double* mu, const DmmaParams& P, double* Y,
                      double* h, double* g, cudaStream_t s);
-// 16-bit operand rows [hi | lo | aug] and per-row out-margins beta.
+// 16-bit operand rows [hi | lo | aug], per-row out-margins beta, FP32
+// coordinates Xf ([n_pad][d], scaled, centred) and their per-row error radius.
 int launch_pack16(const double* X, uint64_t n, uint64_t n_pad, const uint32_t* perm,
                   const uint8_t* bad, const double* mu, const ScreenParams& P, void* Q,
-                  float* beta, cudaStream_t s);
+                  float* beta, float* Xf, float* rad, cudaStream_t s);
 // FP8 operand rows and per-row (sigma, alpha, beta, 0).
 int launch_pack8(const double* X, uint64_t n, uint64_t n_pad, const uint32_t* perm,
                  const uint8_t* bad, const double* mu, const ScreenParams& P, uint8_t* Q,

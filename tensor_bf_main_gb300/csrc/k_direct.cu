@@ -13,6 +13,8 @@
 //  * band_recheck_kernel: one thread per band pair, the same chain.
 //
 // Zero padding of the k loop is exact: fma(0, 0, acc) == acc for acc >= +0.
+#include <algorithm>
+
 #include "ejoin_internal.cuh"
 
 namespace ejoin {
@@ -174,7 +176,93 @@ __global__ void __launch_bounds__(256) band_recheck_kernel(const double* __restr
     if ((threadIdx.x & 31) == 0 && c) atomicAdd(&st->band_hits, (unsigned long long)c);
 }
 
+// Two-stage recheck of the band of the 16-bit screen.  A warp takes 32 band
+// pairs; for each pair the lanes form S = sum_c fl32(zf_ic - zf_jc)^2 over the
+// FP32 coordinates of the packed rows (any order), and lane p then decides
+// pair p with a rigorous bound that scales with the pair's own distance:
+//   |w| = |zf_i - zf_j| differs from the exact scaled distance by at most
+//   rad_i + rad_j, and S from |w|^2 by the relative c32 (+ abs32), so
+//   S / (1 - c32) <= (sqrt(Tlo) - rad)^2   => neighbour
+//   S / (1 + c32) >  (sqrt(Thi) + rad)^2   => not a neighbour
+// Only the pairs left undecided (a tiny fraction) run the exact FP64 chain of
+// the reference arithmetic on the original rows.
+__global__ void __launch_bounds__(256) band_recheck2_kernel(const double* __restrict__ X,
+                                                            uint32_t d,
+                                                            const uint32_t* __restrict__ perm,
+                                                            double T, Recheck32 R,
+                                                            const BandPair* __restrict__ band,
+                                                            uint64_t nband, uint64_t n,
+                                                            int32_t* counts, DevStatus* st) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / 32;
+    const uint64_t nwarps = (uint64_t)gridDim.x * blockDim.x / 32;
+    unsigned hits = 0, exact_runs = 0;
+    for (uint64_t base = warp * 32; base < nband; base += nwarps * 32) {
+        const uint64_t e = base + lane;
+        BandPair bp = {0xffffffffu, 0xffffffffu};
+        if (e < nband) bp = band[e];
+        const uint32_t mi = bp.i, mj = bp.j & ~kBandBoth;
+        const bool valid = e < nband && mi < n && mj < n;
+        float mine = 0.0f;
+        for (uint32_t q = 0; q < 32; ++q) {
+            const uint32_t i = __shfl_sync(0xffffffffu, mi, q);
+            const uint32_t j = __shfl_sync(0xffffffffu, mj, q);
+            const bool v = __shfl_sync(0xffffffffu, valid, q);
+            if (!v) continue;  // warp-uniform
+            const float* a = R.Xf + (uint64_t)i * d;
+            const float* b = R.Xf + (uint64_t)j * d;
+            float S = 0.0f;
+            for (uint32_t c = lane; c < d; c += 32) {
+                const float t = a[c] - b[c];
+                S = fmaf(t, t, S);
+            }
+            for (int o = 16; o; o >>= 1) S += __shfl_xor_sync(0xffffffffu, S, o);
+            if (lane == q) mine = S;
+        }
+        bool hit = false;
+        if (valid) {
+            const double rr = (double)R.rad[mi] + (double)R.rad[mj];
+            const double Sd = (double)mine;
+            const double lo = R.sTlo - rr;
+            const bool in = lo >= 0.0 && (Sd + R.abs32) / (1.0 - R.c32) <= lo * lo * (1.0 - 8 * kU);
+            const double hi = R.sThi + rr;
+            const bool out = (Sd - R.abs32) / (1.0 + R.c32) > hi * hi * (1.0 + 8 * kU);
+            if (in) {
+                hit = true;
+            } else if (!out) {
+                ++exact_runs;
+                const uint64_t oi = perm ? perm[mi] : mi, oj = perm ? perm[mj] : mj;
+                hit = exact_d2(X + oi * (uint64_t)d, X + oj * (uint64_t)d, d) <= T;
+            }
+        }
+        if (hit) {
+            atomicAdd(&counts[mi], 1);
+            if (bp.j & kBandBoth) atomicAdd(&counts[mj], 1);
+            ++hits;
+        }
+    }
+    const unsigned c = __reduce_add_sync(0xffffffffu, hits);
+    const unsigned x = __reduce_add_sync(0xffffffffu, exact_runs);
+    if (lane == 0) {
+        if (c) atomicAdd(&st->band_hits, (unsigned long long)c);
+        if (x) atomicAdd(&st->exact_rechecks, (unsigned long long)x);
+    }
+}
+
 }  // namespace
+
+int launch_band_recheck2(const double* X, uint64_t n, uint32_t d, const uint32_t* perm, double T,
+                         const Recheck32& R, const BandPair* band, uint64_t nband, int32_t* counts,
+                         DevStatus* st, cudaStream_t s) {
+    if (nband == 0) return EJOIN_OK;
+    const uint64_t warps = (nband + 31) / 32;
+    const uint64_t blocks = std::min<uint64_t>((warps + 7) / 8, 152ull * 64);
+    band_recheck2_kernel<<<(unsigned)blocks, 256, 0, s>>>(X, d, perm, T, R, band, nband, n, counts,
+                                                          st);
+    EJ_CUDA(cudaGetLastError());
+    note_launch();
+    return EJOIN_OK;
+}
 
 int launch_direct_selfjoin(const double* X, uint64_t n, uint32_t d, double T, int32_t* counts,
                            cudaStream_t s) {

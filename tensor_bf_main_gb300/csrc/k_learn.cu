@@ -27,6 +27,7 @@
 #include <math.h>
 #include <string.h>
 
+#include <algorithm>
 #include <vector>
 
 #include "ejoin_internal.cuh"
@@ -46,59 +47,69 @@ __host__ __device__ __forceinline__ uint64_t splitmix64(uint64_t x) {
 
 // ------------------------------------------------------------ projection --
 
-// proj[i][a] = sum_c P[a][c] x[i][c] in FP64 (FP32 P values are exact in
-// FP64), and err[i] >= max_a |computed - exact| = gamma_{d+2} sum_c |P x|.
-// Non-finite rows get NaN (they are never neighbours of anything).
-__global__ void project_kernel(const double* __restrict__ X, uint64_t n, uint32_t d,
-                               const float* __restrict__ P, uint32_t k, double* proj, double* err) {
-    const uint64_t i = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / 32;
-    const int lane = threadIdx.x & 31;
+// proj[i][a] = fl32(sum_c P[a][c] * yf[i][c]) with yf = fl32(fl64(x - mu)),
+// thread per point, P in shared memory.  err[i] bounds the distance from the
+// exact P (x_i - mu) in every coordinate:
+//   |yf_c - (x_c - mu_c)| <= 1.0001 * 2^-24 |yf_c| (+ 2^-149 if subnormal),
+//   FP32 fma accumulation of d terms <= (d + 2) 2^-24 sum |P yf|,
+// so err = (d + 4) 2^-24 S (1 + 2^-16) + d 2^-148, S = sum_c |P_ac| |yf_c|
+// (itself computed with upward rounding).  Projections of x - mu give the
+// same differences P(x_i - x_j) as projections of x.  Non-finite rows get NaN.
+__global__ void project_kernel(const double* __restrict__ X, const double* __restrict__ mu,
+                               uint64_t n, uint32_t d, const float* __restrict__ P, uint32_t k,
+                               float* proj, float* err) {
+    extern __shared__ float sP[];
+    for (uint32_t e = threadIdx.x; e < k * d; e += blockDim.x) sP[e] = P[e];
+    __syncthreads();
+    const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double* x = X + i * d;
-    const double g = (d + 8) * kU * 1.01;
-    double emax = 0.0;
+    float acc[16], sabs[16];
+#pragma unroll
+    for (int a = 0; a < 16; ++a) acc[a] = sabs[a] = 0.0f;
     bool finite = true;
-    for (uint32_t a = 0; a < k; ++a) {
-        double s = 0.0, sa = 0.0;
-        for (uint32_t c = lane; c < d; c += 32) {
-            const double pc = (double)P[(uint64_t)a * d + c];
-            const double xc = x[c];
-            s = __fma_rn(pc, xc, s);
-            sa += fabs(pc * xc);
-        }
-        for (int o = 16; o; o >>= 1) {
-            s += __shfl_xor_sync(0xffffffffu, s, o);
-            sa += __shfl_xor_sync(0xffffffffu, sa, o);
-        }
-        finite &= isfinite(s) && isfinite(sa);
-        emax = fmax(emax, g * sa);
-        if (lane == 0) proj[i * k + a] = s;
+    for (uint32_t c = 0; c < d; ++c) {
+        const double y = __dsub_rn(x[c], mu[c]);
+        finite &= isfinite(y) != 0;
+        const float yf = (float)y;
+        const float ay = fabsf(yf);
+#pragma unroll
+        for (int a = 0; a < 16; ++a)
+            if (a < (int)k) {
+                const float pc = sP[a * d + c];
+                acc[a] = fmaf(pc, yf, acc[a]);
+                sabs[a] = __fmaf_ru(fabsf(pc), ay, sabs[a]);
+            }
     }
-    if (lane == 0) {
-        err[i] = finite ? emax * (1 + 8 * kU) : NAN;
-        if (!finite)
-            for (uint32_t a = 0; a < k; ++a) proj[i * k + a] = NAN;
-    }
+    float smax = 0.0f;
+#pragma unroll
+    for (int a = 0; a < 16; ++a)
+        if (a < (int)k) {
+            proj[i * k + a] = finite ? acc[a] : __int_as_float(0x7fc00000);
+            smax = fmaxf(smax, sabs[a]);
+        }
+    const float c1 = (float)(d + 4) * 5.9604644775390625e-08f * 1.0000153f;  // (d+4) 2^-24 (1+2^-16)
+    err[i] = finite ? __fmaf_ru(c1, smax, (float)d * 3.5873240686715317e-43f) : __int_as_float(0x7fc00000);
 }
 
-__device__ __forceinline__ unsigned long long ordered_bits(double v) {
-    unsigned long long b = (unsigned long long)__double_as_longlong(v);
-    return (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
+__device__ __forceinline__ uint32_t ordered_bits32(float v) {
+    const uint32_t b = __float_as_uint(v);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
 }
-__device__ __forceinline__ double from_ordered_bits(unsigned long long b) {
-    b = (b & 0x8000000000000000ull) ? (b & 0x7fffffffffffffffull) : ~b;
-    return __longlong_as_double((long long)b);
+__device__ __forceinline__ float from_ordered_bits32(uint32_t b) {
+    b = (b & 0x80000000u) ? (b & 0x7fffffffu) : ~b;
+    return __uint_as_float(b);
 }
 
-__global__ void range_kernel(const double* __restrict__ proj, uint64_t n, uint32_t k,
-                             unsigned long long* mn, unsigned long long* mx) {
+__global__ void range_kernel(const float* __restrict__ proj, uint64_t n, uint32_t k,
+                             unsigned int* mn, unsigned int* mx) {
     const uint32_t a = blockIdx.y;
-    unsigned long long lo = ~0ull, hi = 0ull;
+    uint32_t lo = 0xffffffffu, hi = 0u;
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
          i += (uint64_t)gridDim.x * blockDim.x) {
-        const double v = proj[i * k + a];
+        const float v = proj[i * k + a];
         if (!isnan(v)) {
-            const unsigned long long b = ordered_bits(v);
+            const uint32_t b = ordered_bits32(v);
             lo = min(lo, b);
             hi = max(hi, b);
         }
@@ -116,65 +127,83 @@ __global__ void range_kernel(const double* __restrict__ proj, uint64_t n, uint32
 // Sort keys: Morton interleave of the leading min(k, 8) coordinates quantised
 // to 64 / m bits each, or the order-preserving bits of coordinate 0.  NaN
 // rows sort last.
-__global__ void key_kernel(const double* __restrict__ proj, uint64_t n, uint32_t k, int lead_only,
-                           const unsigned long long* mn, const unsigned long long* mx,
+__global__ void key_kernel(const float* __restrict__ proj, uint64_t n, uint32_t k, int lead_only,
+                           const unsigned int* mn, const unsigned int* mx,
                            unsigned long long* keys, uint32_t* idx) {
     const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
     idx[i] = (uint32_t)i;
-    const double p0 = proj[i * k];
+    const float p0 = proj[i * k];
     if (isnan(p0)) {
         keys[i] = ~0ull;
         return;
     }
     if (lead_only) {
-        keys[i] = ordered_bits(p0);
+        keys[i] = ordered_bits32(p0);
         return;
     }
     const uint32_t m = k < 8 ? k : 8;
     const uint32_t bits = 64 / m;
-    unsigned long long key = 0;
+    const double levels = ldexp(1.0, (int)(bits > 31 ? 31 : bits)) - 1.0;
     uint32_t q[8];
     for (uint32_t a = 0; a < m; ++a) {
-        const double lo = from_ordered_bits(mn[a]), hi = from_ordered_bits(mx[a]);
-        const double span = hi - lo;
-        double t = span > 0 ? (proj[i * k + a] - lo) / span : 0.0;
-        t = fmin(fmax(t, 0.0), 1.0);
-        const double levels = ldexp(1.0, (int)bits) - 1.0;
-        q[a] = (uint32_t)(t * levels);
+        const float lo = from_ordered_bits32(mn[a]), hi = from_ordered_bits32(mx[a]);
+        const float span = hi - lo;
+        float t = span > 0.0f ? (proj[i * k + a] - lo) / span : 0.0f;
+        t = fminf(fmaxf(t, 0.0f), 1.0f);
+        q[a] = (uint32_t)((double)t * levels);
     }
-    for (int b = (int)bits - 1; b >= 0; --b)
+    unsigned long long key = 0;
+    const uint32_t qb = bits > 31 ? 31 : bits;
+    for (int b = (int)qb - 1; b >= 0; --b)
         for (uint32_t a = 0; a < m; ++a) key = (key << 1) | ((q[a] >> b) & 1u);
     keys[i] = key;
 }
 
 // Per 128-row tile of the sorted order: [lo, hi] of every projected
-// coordinate, widened by each row's rounding bound; non-finite and padding
-// rows are left out (they are never neighbours).
-__global__ void boxes_kernel(const double* __restrict__ proj, const double* __restrict__ err,
+// coordinate, widened by each row's error bound (outward rounding);
+// non-finite and padding rows are left out (they are never neighbours).
+__global__ void boxes_kernel(const float* __restrict__ proj, const float* __restrict__ err,
                              const uint32_t* __restrict__ perm, uint64_t n, uint32_t k,
-                             double* lo, double* hi) {
+                             float* lo, float* hi) {
     const uint64_t t = blockIdx.x;
     for (uint32_t a = threadIdx.y; a < k; a += blockDim.y) {
-        double l = INFINITY, h = -INFINITY;
+        float l = INFINITY, h = -INFINITY;
         for (uint32_t r = threadIdx.x; r < 128; r += blockDim.x) {
             const uint64_t p = t * 128 + r;
             if (p >= n) continue;
             const uint64_t i = perm[p];
-            const double v = proj[i * k + a], e = err[i];
+            const float v = proj[i * k + a], e = err[i];
             if (isnan(v) || isnan(e)) continue;
-            l = fmin(l, __dsub_rd(v, e));
-            h = fmax(h, __dadd_ru(v, e));
+            l = fminf(l, __fsub_rd(v, e));
+            h = fmaxf(h, __fadd_ru(v, e));
         }
         for (int o = 16; o; o >>= 1) {
-            l = fmin(l, __shfl_xor_sync(0xffffffffu, l, o));
-            h = fmax(h, __shfl_xor_sync(0xffffffffu, h, o));
+            l = fminf(l, __shfl_xor_sync(0xffffffffu, l, o));
+            h = fmaxf(h, __shfl_xor_sync(0xffffffffu, h, o));
         }
         if (threadIdx.x == 0) {
             lo[t * k + a] = l;
             hi[t * k + a] = h;
         }
     }
+}
+
+// Boxes of super-blocks of `sb` consecutive tiles (union of the tile boxes).
+__global__ void superbox_kernel(const float* __restrict__ lo, const float* __restrict__ hi,
+                                uint64_t nt, uint32_t k, uint32_t sb, float* slo, float* shi) {
+    const uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    const uint64_t ns = (nt + sb - 1) / sb;
+    if (e >= ns * k) return;
+    const uint64_t S = e / k;
+    const uint32_t a = (uint32_t)(e % k);
+    float l = INFINITY, h = -INFINITY;
+    for (uint64_t t = S * sb; t < min(nt, (S + 1) * sb); ++t) {
+        l = fminf(l, lo[t * k + a]);
+        h = fmaxf(h, hi[t * k + a]);
+    }
+    slo[e] = l;
+    shi[e] = h;
 }
 
 // --------------------------------------------------------------- training --
@@ -280,79 +309,90 @@ __global__ void __launch_bounds__(TRAIN_THREADS) train_step_kernel(const float* 
     if ((threadIdx.x & 31) == 0 && lsum != 0.0f) atomicAdd(loss, lsum * invM);
 }
 
-__global__ void adam_kernel(float* P, const float* G, float* m1, float* m2, uint32_t nel, float lr,
-                            float b1, float b2, float c1, float c2) {
-    const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= nel) return;
-    const float g = G[e];
-    const float a = b1 * m1[e] + (1.0f - b1) * g;
-    const float b = b2 * m2[e] + (1.0f - b2) * g * g;
-    m1[e] = a;
-    m2[e] = b;
-    P[e] -= lr * (a / c1) / (sqrtf(b / c2) + 1e-8f);
-}
-
-// Power iteration on P P^T (k x k), then P /= max(1, 1.02 * sigma_est).
-// The iteration runs on (P P^T)^32, formed by five normalised squarings, so it
-// converges even when the leading eigenvalues are close; the estimate is the
-// Rayleigh quotient of the original P P^T.  One block; k <= 16.
-__global__ void renorm_kernel(float* P, uint32_t k, uint32_t d, float* sigma_out) {
-    __shared__ double M[16 * 16], A[16 * 16], B[16 * 16];
-    __shared__ double v[16], w[16];
-    __shared__ double lam;
-    for (uint32_t e = threadIdx.x; e < k * k; e += blockDim.x) {
+// One Adam step on P from G (G is cleared for the next step), then the
+// power-iteration renormalisation P <- P / max(1, 1.02 s): s is the Rayleigh
+// quotient estimate of ||P||_2 from (P P^T)^32 (five normalised squarings, so
+// it converges when the leading eigenvalues are close).  One block; k <= 16.
+__global__ void adam_renorm_kernel(float* P, float* G, float* m1, float* m2, uint32_t k,
+                                   uint32_t d, float lr, float b1, float b2, float c1, float c2,
+                                   int renorm, float* sigma_out) {
+    __shared__ float M[16 * 16], A[16 * 16], B[16 * 16];
+    __shared__ float v[16], w[16];
+    __shared__ float lam, amax;
+    const uint32_t nel = k * d;
+    for (uint32_t e = threadIdx.x; e < nel; e += blockDim.x) {
+        const float g = G[e];
+        G[e] = 0.0f;
+        const float a = b1 * m1[e] + (1.0f - b1) * g;
+        const float b = b2 * m2[e] + (1.0f - b2) * g * g;
+        m1[e] = a;
+        m2[e] = b;
+        P[e] -= lr * (a / c1) / (sqrtf(b / c2) + 1e-8f);
+    }
+    if (!renorm) return;
+    __syncthreads();
+    // M = P P^T: warp per entry
+    const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x / 32, nw = blockDim.x / 32;
+    for (uint32_t e = wid; e < k * k; e += nw) {
         const uint32_t a = e / k, b = e % k;
-        double s = 0.0;
-        for (uint32_t c = 0; c < d; ++c) s += (double)P[a * d + c] * (double)P[b * d + c];
-        M[e] = s;
-        A[e] = s;
+        float s = 0.0f;
+        for (uint32_t c = lane; c < d; c += 32) s = fmaf(P[a * d + c], P[b * d + c], s);
+        for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) {
+            M[e] = s;
+            A[e] = s;
+        }
     }
     __syncthreads();
     for (int sq = 0; sq < 5; ++sq) {
-        double mx = 0.0;
-        for (uint32_t e = 0; e < k * k; ++e) mx = fmax(mx, fabs(A[e]));
-        const double inv = mx > 0 ? 1.0 / mx : 0.0;
+        if (threadIdx.x == 0) {
+            float mx = 0.0f;
+            for (uint32_t e = 0; e < k * k; ++e) mx = fmaxf(mx, fabsf(A[e]));
+            amax = mx > 0.0f ? 1.0f / mx : 0.0f;
+        }
+        __syncthreads();
+        const float inv = amax;
         for (uint32_t e = threadIdx.x; e < k * k; e += blockDim.x) {
             const uint32_t a = e / k, b = e % k;
-            double s = 0.0;
-            for (uint32_t c = 0; c < k; ++c) s += (A[a * k + c] * inv) * (A[c * k + b] * inv);
+            float s = 0.0f;
+            for (uint32_t c = 0; c < k; ++c) s = fmaf(A[a * k + c] * inv, A[c * k + b] * inv, s);
             B[e] = s;
         }
         __syncthreads();
         for (uint32_t e = threadIdx.x; e < k * k; e += blockDim.x) A[e] = B[e];
         __syncthreads();
     }
-    if (threadIdx.x < k) v[threadIdx.x] = 1.0 + 0.01 * threadIdx.x;
+    if (threadIdx.x < k) v[threadIdx.x] = 1.0f + 0.01f * threadIdx.x;
     __syncthreads();
     for (int it = 0; it < 8; ++it) {
         if (threadIdx.x < k) {
-            double s = 0.0;
-            for (uint32_t b = 0; b < k; ++b) s += A[threadIdx.x * k + b] * v[b];
+            float s = 0.0f;
+            for (uint32_t b = 0; b < k; ++b) s = fmaf(A[threadIdx.x * k + b], v[b], s);
             w[threadIdx.x] = s;
         }
         __syncthreads();
         if (threadIdx.x == 0) {
-            double nn = 0.0;
-            for (uint32_t b = 0; b < k; ++b) nn += w[b] * w[b];
-            const double inv = nn > 0 ? 1.0 / sqrt(nn) : 0.0;
+            float nn = 0.0f;
+            for (uint32_t b = 0; b < k; ++b) nn = fmaf(w[b], w[b], nn);
+            const float inv = nn > 0.0f ? rsqrtf(nn) : 0.0f;
             for (uint32_t b = 0; b < k; ++b) v[b] = w[b] * inv;
         }
         __syncthreads();
     }
     if (threadIdx.x == 0) {
-        double num = 0.0, den = 0.0;
+        float num = 0.0f, den = 0.0f;
         for (uint32_t a = 0; a < k; ++a) {
-            double s = 0.0;
-            for (uint32_t b = 0; b < k; ++b) s += M[a * k + b] * v[b];
-            num += v[a] * s;
-            den += v[a] * v[a];
+            float s = 0.0f;
+            for (uint32_t b = 0; b < k; ++b) s = fmaf(M[a * k + b], v[b], s);
+            num = fmaf(v[a], s, num);
+            den = fmaf(v[a], v[a], den);
         }
-        lam = den > 0 ? num / den : 0.0;
+        lam = den > 0.0f ? num / den : 0.0f;
     }
     __syncthreads();
-    const float sig = (float)(sqrt(fmax(lam, 0.0)) * 1.02);
+    const float sig = sqrtf(fmaxf(lam, 0.0f)) * 1.02f;
     const float scale = sig > 1.0f ? 1.0f / sig : 1.0f;
-    for (uint32_t e = threadIdx.x; e < k * d; e += blockDim.x) P[e] *= scale;
+    for (uint32_t e = threadIdx.x; e < nel; e += blockDim.x) P[e] *= scale;
     if (threadIdx.x == 0 && sigma_out) *sigma_out = sig;
 }
 
@@ -360,23 +400,26 @@ __global__ void renorm_kernel(float* P, uint32_t k, uint32_t d, float* sigma_out
 
 // ------------------------------------------------------------ host side --
 
-// Projects all points with P (host k x d), orders them and computes the tile
-// boxes.  perm (n entries, sorted position -> original row), lo/hi
-// ([n_pad/128][k]) are allocated here.
-int learned_order(const double* X, uint64_t n, uint64_t n_pad, uint32_t d, const float* P_dev,
-                  uint32_t k, int lead_only, DBuf<uint32_t>& perm, DBuf<double>* lo,
-                  DBuf<double>* hi, cudaStream_t s) {
-    DBuf<double> proj, err;
+// Projects all points with P (device k x d), orders them and, when `boxes` is
+// given, computes the boxes of the 128-row tiles and of super-blocks of
+// kSuperTiles tiles (FP32, outward rounded).  perm: sorted position ->
+// original row.
+int learned_order(const double* X, const double* mu, uint64_t n, uint64_t n_pad, uint32_t d,
+                  const float* P_dev, uint32_t k, int lead_only, DBuf<uint32_t>& perm,
+                  LearnedBoxes* boxes, cudaStream_t s) {
+    DBuf<float> proj, err;
     EJ_TRY(proj.alloc(n * k, s, "projections"));
     EJ_TRY(err.alloc(n, s, "projection error bounds"));
-    project_kernel<<<(unsigned)((n * 32 + 255) / 256), 256, 0, s>>>(X, n, d, P_dev, k, proj.p, err.p);
+    const size_t shm = (size_t)k * d * sizeof(float);
+    EJ_CUDA(cudaFuncSetAttribute(project_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
+    project_kernel<<<(unsigned)((n + 127) / 128), 128, shm, s>>>(X, mu, n, d, P_dev, k, proj.p, err.p);
     EJ_CUDA(cudaGetLastError());
     note_launch();
-    DBuf<unsigned long long> rng;
+    DBuf<unsigned int> rng;
     EJ_TRY(rng.alloc(2 * k, s, "projection ranges"));
-    EJ_CUDA(cudaMemsetAsync(rng.p, 0xff, k * sizeof(unsigned long long), s));
-    EJ_CUDA(cudaMemsetAsync(rng.p + k, 0, k * sizeof(unsigned long long), s));
-    range_kernel<<<dim3(256, k), 256, 0, s>>>(proj.p, n, k, rng.p, rng.p + k);
+    EJ_CUDA(cudaMemsetAsync(rng.p, 0xff, k * sizeof(unsigned int), s));
+    EJ_CUDA(cudaMemsetAsync(rng.p + k, 0, k * sizeof(unsigned int), s));
+    range_kernel<<<dim3(128, k), 256, 0, s>>>(proj.p, n, k, rng.p, rng.p + k);
     EJ_CUDA(cudaGetLastError());
     note_launch();
     DBuf<unsigned long long> keys, keys2;
@@ -396,25 +439,33 @@ int learned_order(const double* X, uint64_t n, uint64_t n_pad, uint32_t d, const
     EJ_TRY(tmp.alloc(tmp_bytes, s, "sort scratch"));
     EJ_CUDA(cub::DeviceRadixSort::SortPairs(tmp.p, tmp_bytes, keys.p, keys2.p, idx.p, perm.p,
                                             (int)n, 0, 64, s));
-    note_launch(8);  // onesweep passes (library kernels, counted approximately)
-    if (lo && hi) {
+    note_launch(11);  // histogram, scan and one-sweep passes of the library sort
+    if (boxes) {
         const uint64_t nt = n_pad / 128;
-        EJ_TRY(lo->alloc(nt * k, s, "tile boxes"));
-        EJ_TRY(hi->alloc(nt * k, s, "tile boxes"));
-        boxes_kernel<<<(unsigned)nt, dim3(32, 8), 0, s>>>(proj.p, err.p, perm.p, n, k, lo->p, hi->p);
+        const uint64_t ns = (nt + kSuperTiles - 1) / kSuperTiles;
+        EJ_TRY(boxes->lo.alloc(nt * k, s, "tile boxes"));
+        EJ_TRY(boxes->hi.alloc(nt * k, s, "tile boxes"));
+        EJ_TRY(boxes->slo.alloc(ns * k, s, "super-block boxes"));
+        EJ_TRY(boxes->shi.alloc(ns * k, s, "super-block boxes"));
+        boxes_kernel<<<(unsigned)nt, dim3(32, 8), 0, s>>>(proj.p, err.p, perm.p, n, k,
+                                                          boxes->lo.p, boxes->hi.p);
         EJ_CUDA(cudaGetLastError());
-        note_launch();
+        superbox_kernel<<<(unsigned)((ns * k + 255) / 256), 256, 0, s>>>(
+            boxes->lo.p, boxes->hi.p, nt, k, kSuperTiles, boxes->slo.p, boxes->shi.p);
+        EJ_CUDA(cudaGetLastError());
+        note_launch(2);
+        boxes->k = k;
     }
     return EJOIN_OK;
 }
 
-int train_projection_dev(const double* X, uint64_t n, uint32_t d, double eps, uint32_t k,
-                         uint64_t pairs, uint32_t steps, uint64_t seed, int lead_only,
+int train_projection_dev(const double* X, const double* mu, uint64_t n, uint32_t d, double eps,
+                         uint32_t k, uint64_t pairs, uint32_t steps, uint64_t seed, int lead_only,
                          cudaStream_t s, TrainResult& out) {
     if (k == 0 || k > 16) return set_error(EJOIN_EINVAL, "proj_k must be in 1..16");
     if (n < 2) return set_error(EJOIN_EINVAL, "training needs at least 2 points");
     const uint32_t nel = k * d;
-    // seeded Gaussian initialisation (Box-Muller on splitmix64), then certified scaling
+    // seeded Gaussian initialisation (Box-Muller on splitmix64), certified scaling
     std::vector<float> P0(nel);
     for (uint32_t e = 0; e < nel; ++e) {
         const uint64_t a = splitmix64(seed * 0x2545F4914F6CDD1Dull + 2 * e);
@@ -426,51 +477,52 @@ int train_projection_dev(const double* X, uint64_t n, uint32_t d, double eps, ui
     double s0 = 0;
     EJ_TRY(cert_spectral_norm(P0.data(), k, d, &s0));
     for (auto& v : P0) v = (float)(v / (s0 * 1.0001));
-    DBuf<float> P, G, m1, m2, loss, sig;
+    DBuf<float> P, G, m1, m2, loss;
     EJ_TRY(P.alloc(nel, s, "projection"));
     EJ_TRY(G.alloc(nel, s, "gradient"));
     EJ_TRY(m1.alloc(nel, s, "adam m"));
     EJ_TRY(m2.alloc(nel, s, "adam v"));
     EJ_TRY(loss.alloc(steps + 1, s, "loss"));
-    EJ_TRY(sig.alloc(1, s, "sigma"));
     EJ_CUDA(cudaMemcpyAsync(P.p, P0.data(), nel * sizeof(float), cudaMemcpyHostToDevice, s));
+    EJ_TRY(G.zero(s));
     EJ_TRY(m1.zero(s));
     EJ_TRY(m2.zero(s));
     EJ_TRY(loss.zero(s));
-    const uint64_t M = pairs ? pairs : (1u << 20);
+    const uint64_t M = std::max<uint64_t>(pairs ? pairs : (1u << 20), 256);
+    const uint64_t B = std::min<uint64_t>(M, 65536);  // minibatch
     DBuf<float> V, tgt;
     EJ_TRY(V.alloc(M * d, s, "training pair differences"));
     EJ_TRY(tgt.alloc(M, s, "training pair targets"));
-    PairBatch pb{V.p, tgt.p};
-    const uint32_t rounds = steps >= 4 ? 4 : (steps ? steps : 1);
+    const uint32_t rounds = steps >= 2 ? 2 : 1;
     const uint64_t n_pad = (n + 127) / 128 * 128;
-    const float b1 = 0.9f, b2 = 0.999f;
-    const float lr = 0.02f;
+    const float b1 = 0.9f, b2 = 0.999f, lr = 0.02f;
     const size_t shm = (size_t)(k * d + TRAIN_THREADS * k) * sizeof(float);
     if (shm > 200 * 1024) return set_error(EJOIN_EUNSUPPORTED, "projection too large for training");
     auto step_fn = k <= 8 ? train_step_kernel<8> : train_step_kernel<16>;
     EJ_CUDA(cudaFuncSetAttribute(step_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
+    const unsigned grid = (unsigned)std::min<uint64_t>((B + TRAIN_THREADS - 1) / TRAIN_THREADS, 1024);
     uint32_t t_step = 0;
+    uint64_t cursor = 0;
     for (uint32_t r = 0; r < rounds; ++r) {
         DBuf<uint32_t> perm;
-        EJ_TRY(learned_order(X, n, n_pad, d, P.p, k, lead_only, perm, nullptr, nullptr, s));
+        EJ_TRY(learned_order(X, mu, n, n_pad, d, P.p, k, lead_only, perm, nullptr, s));
         sample_pairs_kernel<<<(unsigned)((M + 255) / 256), 256, 0, s>>>(
-            X, n, d, perm.p, M, seed + 7919ull * (r + 1), eps, 256, pb);
+            X, n, d, perm.p, M, seed + 7919ull * (r + 1), eps, 256, PairBatch{V.p, tgt.p});
         EJ_CUDA(cudaGetLastError());
         note_launch();
         const uint32_t nsteps = steps / rounds + (r < steps % rounds ? 1 : 0);
         for (uint32_t it = 0; it < nsteps; ++it, ++t_step) {
-            EJ_TRY(G.zero(s));
-            step_fn<<<304, TRAIN_THREADS, shm, s>>>(P.p, k, d, pb, M, G.p, loss.p + t_step);
+            if (cursor + B > M) cursor = 0;
+            PairBatch pb{V.p + cursor * d, tgt.p + cursor};
+            cursor += B;
+            step_fn<<<grid, TRAIN_THREADS, shm, s>>>(P.p, k, d, pb, B, G.p, loss.p + t_step);
             EJ_CUDA(cudaGetLastError());
             const float c1 = 1.0f - powf(b1, (float)(t_step + 1));
             const float c2 = 1.0f - powf(b2, (float)(t_step + 1));
-            adam_kernel<<<(nel + 255) / 256, 256, 0, s>>>(P.p, G.p, m1.p, m2.p, nel, lr, b1, b2,
-                                                          c1, c2);
+            adam_renorm_kernel<<<1, 256, 0, s>>>(P.p, G.p, m1.p, m2.p, k, d, lr, b1, b2, c1, c2, 1,
+                                                 nullptr);
             EJ_CUDA(cudaGetLastError());
-            renorm_kernel<<<1, 256, 0, s>>>(P.p, k, d, sig.p);
-            EJ_CUDA(cudaGetLastError());
-            note_launch(3);
+            note_launch(2);
         }
     }
     out.P.resize(nel);
@@ -478,8 +530,15 @@ int train_projection_dev(const double* X, uint64_t n, uint32_t d, double eps, ui
     EJ_CUDA(cudaMemcpyAsync(out.P.data(), P.p, nel * sizeof(float), cudaMemcpyDeviceToHost, s));
     EJ_CUDA(cudaMemcpyAsync(L.data(), loss.p, L.size() * sizeof(float), cudaMemcpyDeviceToHost, s));
     EJ_CUDA(cudaStreamSynchronize(s));
-    out.loss_first = L.front();
-    out.loss_last = L.back();
+    // first / last loss averaged over a few steps (minibatch noise)
+    const size_t w = std::min<size_t>(8, L.size());
+    double a = 0, b = 0;
+    for (size_t i = 0; i < w; ++i) {
+        a += L[i];
+        b += L[L.size() - 1 - i];
+    }
+    out.loss_first = a / w;
+    out.loss_last = b / w;
     EJ_TRY(cert_spectral_norm(out.P.data(), k, d, &out.sigma_cert));
     return EJOIN_OK;
 }
@@ -524,13 +583,18 @@ extern "C" int ejoin_testing_renormalise(float* P, uint32_t k, uint32_t d, float
     clear_error();
     if (!P || k == 0 || k > 16 || d == 0) return set_error(EJOIN_EINVAL, "bad arguments");
     cudaStream_t s = cudaStreamPerThread;
-    DBuf<float> dP, dS;
-    EJ_TRY(dP.alloc((size_t)k * d, s, "P"));
+    DBuf<float> dP, dZ, dS;
+    const size_t nel = (size_t)k * d;
+    EJ_TRY(dP.alloc(nel, s, "P"));
+    EJ_TRY(dZ.alloc(3 * nel, s, "zero state"));
     EJ_TRY(dS.alloc(1, s, "sigma"));
-    EJ_CUDA(cudaMemcpyAsync(dP.p, P, (size_t)k * d * sizeof(float), cudaMemcpyHostToDevice, s));
-    renorm_kernel<<<1, 256, 0, s>>>(dP.p, k, d, dS.p);
+    EJ_TRY(dZ.zero(s));
+    EJ_CUDA(cudaMemcpyAsync(dP.p, P, nel * sizeof(float), cudaMemcpyHostToDevice, s));
+    // zero gradient and learning rate: the Adam part leaves P unchanged
+    adam_renorm_kernel<<<1, 256, 0, s>>>(dP.p, dZ.p, dZ.p + nel, dZ.p + 2 * nel, k, d, 0.0f, 0.9f,
+                                         0.999f, 1.0f, 1.0f, 1, dS.p);
     EJ_CUDA(cudaGetLastError());
-    EJ_CUDA(cudaMemcpyAsync(P, dP.p, (size_t)k * d * sizeof(float), cudaMemcpyDeviceToHost, s));
+    EJ_CUDA(cudaMemcpyAsync(P, dP.p, nel * sizeof(float), cudaMemcpyDeviceToHost, s));
     if (sigma_est_out)
         EJ_CUDA(cudaMemcpyAsync(sigma_est_out, dS.p, sizeof(float), cudaMemcpyDeviceToHost, s));
     EJ_CUDA(cudaStreamSynchronize(s));

@@ -11,116 +11,87 @@
 namespace ejoin {
 namespace {
 
-constexpr uint32_t SB = 16;           // super-block edge (tiles)
-constexpr int CAND_PER_THREAD = 16;
-constexpr int CAND_THREADS = 256;
-constexpr uint64_t CAND_PER_BLOCK = (uint64_t)CAND_PER_THREAD * CAND_THREADS;
+constexpr uint32_t SB = kSuperTiles;  // super-block edge (tiles)
 
-struct PruneArgs {
-    const double* lo;    // [ntiles][k] lower corners of the projected boxes (may be null)
-    const double* hi;    // [ntiles][k]
+// Squared gap between two projected boxes, rounded down (so `> thr` proves
+// that every pair of points drawn from the two boxes is farther apart than
+// the projected threshold).  Empty boxes (lo = +inf, hi = -inf) are far from
+// everything.
+__device__ __forceinline__ bool boxes_far(const float* __restrict__ lo, const float* __restrict__ hi,
+                                          uint64_t I, uint64_t J, uint32_t k, float thr) {
+    float g2 = 0.0f;
+    for (uint32_t a = 0; a < k; ++a) {
+        const float l1 = lo[I * k + a], h1 = hi[I * k + a];
+        const float l2 = lo[J * k + a], h2 = hi[J * k + a];
+        const float gap = fmaxf(0.0f, fmaxf(__fsub_rd(l2, h1), __fsub_rd(l1, h2)));
+        g2 = __fmaf_rd(gap, gap, g2);
+    }
+    return g2 > thr;
+}
+
+struct BoxArgs {
+    const float *lo, *hi, *slo, *shi;
     uint32_t k;
-    double thr;          // skip the pair when the squared box gap exceeds thr
+    float thr;
 };
 
-__device__ __forceinline__ bool candidate(uint64_t c, uint64_t nT, uint64_t nS, const PruneArgs& p,
-                                          uint2& out) {
-    const uint64_t sp = c / (SB * SB);
-    const uint32_t r = (uint32_t)(c % (SB * SB));
-    uint64_t SI, SJ;
-    tri_decode(sp, nS, SI, SJ);
-    const uint64_t I = SI * SB + r / SB, J = SJ * SB + r % SB;
-    if (I >= nT || J >= nT || I > J) return false;
-    if (p.lo) {
-        // squared gap between the projected boxes, rounded down (see k_learn.cu)
-        double g2 = 0.0;
-        for (uint32_t a = 0; a < p.k; ++a) {
-            const double l1 = p.lo[I * p.k + a], h1 = p.hi[I * p.k + a];
-            const double l2 = p.lo[J * p.k + a], h2 = p.hi[J * p.k + a];
-            const double gap = fmax(0.0, fmax(__dsub_rd(l2, h1), __dsub_rd(l1, h2)));
-            g2 = __fma_rd(gap, gap, g2);
+// Surviving super-block pairs (SI <= SJ), appended in warp-aggregated batches.
+__global__ void superpairs_kernel(uint64_t nS, BoxArgs b, uint32_t* out, unsigned long long* count) {
+    const uint64_t sp = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    const uint64_t nsp = nS * (nS + 1) / 2;
+    bool keep = false;
+    if (sp < nsp) {
+        keep = true;
+        if (b.slo) {
+            uint64_t SI, SJ;
+            tri_decode(sp, nS, SI, SJ);
+            keep = !boxes_far(b.slo, b.shi, SI, SJ, b.k, b.thr);
         }
-        if (g2 > p.thr) return false;
     }
-    out = make_uint2((uint32_t)I, (uint32_t)J);
-    return true;
+    const unsigned m = __ballot_sync(0xffffffffu, keep);
+    if (!m) return;
+    const unsigned lane = threadIdx.x & 31;
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(count, (unsigned long long)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (keep) out[base + __popc(m & ((1u << lane) - 1u))] = (uint32_t)sp;
 }
 
-__global__ void __launch_bounds__(CAND_THREADS) count_kernel(uint64_t ncand, uint64_t nT,
-                                                             uint64_t nS, PruneArgs p,
-                                                             uint32_t* block_counts) {
-    uint32_t cnt = 0;
-    const uint64_t base = blockIdx.x * CAND_PER_BLOCK + (uint64_t)threadIdx.x * CAND_PER_THREAD;
-    for (int e = 0; e < CAND_PER_THREAD; ++e) {
-        const uint64_t c = base + e;
-        uint2 w;
-        if (c < ncand && candidate(c, nT, nS, p, w)) ++cnt;
+// One block of SB*SB threads per surviving super-block pair: its tile pairs
+// (I <= J, in range, not proven empty) in row-major order.
+__global__ void __launch_bounds__(SB * SB) expand_kernel(const uint32_t* __restrict__ sps,
+                                                         uint64_t nT, uint64_t nS, BoxArgs b,
+                                                         uint2* out, unsigned long long* count) {
+    __shared__ uint64_t sSI, sSJ;
+    __shared__ unsigned wsum[SB * SB / 32];
+    __shared__ unsigned long long sbase;
+    if (threadIdx.x == 0) {
+        uint64_t SI, SJ;
+        tri_decode(sps[blockIdx.x], nS, SI, SJ);
+        sSI = SI;
+        sSJ = SJ;
     }
-    cnt = __reduce_add_sync(0xffffffffu, cnt);
-    __shared__ uint32_t ws[CAND_THREADS / 32];
-    if ((threadIdx.x & 31) == 0) ws[threadIdx.x / 32] = cnt;
+    __syncthreads();
+    const uint64_t I = sSI * SB + threadIdx.x / SB, J = sSJ * SB + threadIdx.x % SB;
+    bool keep = I < nT && J < nT && I <= J;
+    if (keep && b.lo) keep = !boxes_far(b.lo, b.hi, I, J, b.k, b.thr);
+    const unsigned m = __ballot_sync(0xffffffffu, keep);
+    const unsigned lane = threadIdx.x & 31, wid = threadIdx.x / 32;
+    if (lane == 0) wsum[wid] = __popc(m);
     __syncthreads();
     if (threadIdx.x == 0) {
-        uint32_t s = 0;
-        for (int i = 0; i < CAND_THREADS / 32; ++i) s += ws[i];
-        block_counts[blockIdx.x] = s;
-    }
-}
-
-// exclusive scan of block counts (single block, sequential chunks)
-__global__ void scan_kernel(const uint32_t* in, uint64_t n, uint64_t* out, uint64_t* total) {
-    __shared__ uint64_t carry;
-    __shared__ uint64_t buf[1024];
-    if (threadIdx.x == 0) carry = 0;
-    __syncthreads();
-    for (uint64_t base = 0; base < n; base += 1024) {
-        const uint64_t i = base + threadIdx.x;
-        buf[threadIdx.x] = i < n ? in[i] : 0;
-        __syncthreads();
-        for (int o = 1; o < 1024; o <<= 1) {
-            uint64_t v = threadIdx.x >= (unsigned)o ? buf[threadIdx.x - o] : 0;
-            __syncthreads();
-            buf[threadIdx.x] += v;
-            __syncthreads();
+        unsigned tot = 0;
+        for (unsigned w = 0; w < SB * SB / 32; ++w) {
+            const unsigned c = wsum[w];
+            wsum[w] = tot;
+            tot += c;
         }
-        const uint64_t incl = buf[threadIdx.x];
-        const uint64_t own = i < n ? in[i] : 0;
-        if (i < n) out[i] = carry + incl - own;
-        __syncthreads();
-        if (threadIdx.x == 1023) carry += incl;
-        __syncthreads();
+        sbase = tot ? atomicAdd(count, (unsigned long long)tot) : 0ull;
     }
-    if (threadIdx.x == 0) *total = carry;
-}
-
-__global__ void __launch_bounds__(CAND_THREADS) write_kernel(uint64_t ncand, uint64_t nT,
-                                                             uint64_t nS, PruneArgs p,
-                                                             const uint64_t* offsets, uint2* out) {
-    const uint64_t base = blockIdx.x * CAND_PER_BLOCK + (uint64_t)threadIdx.x * CAND_PER_THREAD;
-    uint32_t cnt = 0;
-    for (int e = 0; e < CAND_PER_THREAD; ++e) {
-        const uint64_t c = base + e;
-        uint2 w;
-        if (c < ncand && candidate(c, nT, nS, p, w)) ++cnt;
-    }
-    // block exclusive scan of cnt (thread order == candidate order)
-    __shared__ uint32_t ws[CAND_THREADS / 32];
-    const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x / 32;
-    uint32_t incl = cnt;
-    for (int o = 1; o < 32; o <<= 1) {
-        uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= (uint32_t)o) incl += v;
-    }
-    if (lane == 31) ws[wid] = incl;
     __syncthreads();
-    uint32_t wbase = 0;
-    for (uint32_t i = 0; i < wid; ++i) wbase += ws[i];
-    uint64_t pos = offsets[blockIdx.x] + wbase + incl - cnt;
-    for (int e = 0; e < CAND_PER_THREAD; ++e) {
-        const uint64_t c = base + e;
-        uint2 w;
-        if (c < ncand && candidate(c, nT, nS, p, w)) out[pos++] = w;
-    }
+    if (keep)
+        out[sbase + wsum[wid] + __popc(m & ((1u << lane) - 1u))] =
+            make_uint2((uint32_t)I, (uint32_t)J);
 }
 
 __global__ void sum_counts_kernel(const int32_t* counts, uint64_t n, unsigned long long* total) {
@@ -140,37 +111,38 @@ __global__ void scatter_counts_kernel(const int32_t* src, const uint32_t* perm, 
 
 }  // namespace
 
-// Builds the ordered list of surviving tile pairs.  lo/hi may be null (plain
-// join).  *nwork_out receives the count; `work` is allocated here.
-int build_worklist(uint64_t nT, const double* lo, const double* hi, uint32_t k, double thr,
-                   DBuf<uint2>& work, uint64_t* nwork_out, uint64_t* ncand_out, cudaStream_t s) {
+// Builds the list of surviving tile pairs: super-block pairs first (one
+// thread each), then the tile pairs of the survivors (one block each).
+int build_worklist(uint64_t nT, const LearnedBoxes* boxes, float thr, DBuf<uint2>& work,
+                   uint64_t* nwork_out, cudaStream_t s) {
     *nwork_out = 0;
     if (nT == 0) return EJOIN_OK;
     const uint64_t nS = (nT + SB - 1) / SB;
-    const uint64_t ncand = nS * (nS + 1) / 2 * SB * SB;
-    if (ncand_out) *ncand_out = ncand;
-    const uint64_t nblocks = (ncand + CAND_PER_BLOCK - 1) / CAND_PER_BLOCK;
-    if (nblocks > 0x7fffffffull) return set_error(EJOIN_EUNSUPPORTED, "work list too large");
-    PruneArgs p{lo, hi, k, thr};
-    DBuf<uint32_t> bc;
-    DBuf<uint64_t> off;
-    EJ_TRY(bc.alloc(nblocks, s, "work-list block counts"));
-    EJ_TRY(off.alloc(nblocks + 1, s, "work-list offsets"));
-    count_kernel<<<(unsigned)nblocks, CAND_THREADS, 0, s>>>(ncand, nT, nS, p, bc.p);
+    const uint64_t nsp = nS * (nS + 1) / 2;
+    if (nsp > 0xffffffffull) return set_error(EJOIN_EUNSUPPORTED, "work list too large");
+    BoxArgs b{nullptr, nullptr, nullptr, nullptr, 0, thr};
+    if (boxes) b = BoxArgs{boxes->lo.p, boxes->hi.p, boxes->slo.p, boxes->shi.p, boxes->k, thr};
+    DBuf<uint32_t> sps;
+    DBuf<unsigned long long> cnt;
+    EJ_TRY(sps.alloc(nsp, s, "super-block pairs"));
+    EJ_TRY(cnt.alloc(2, s, "work-list counters"));
+    EJ_TRY(cnt.zero(s));
+    superpairs_kernel<<<(unsigned)((nsp + 255) / 256), 256, 0, s>>>(nS, b, sps.p, cnt.p);
     EJ_CUDA(cudaGetLastError());
     note_launch();
-    scan_kernel<<<1, 1024, 0, s>>>(bc.p, nblocks, off.p, off.p + nblocks);
-    EJ_CUDA(cudaGetLastError());
-    note_launch();
-    uint64_t total = 0;
-    EJ_CUDA(cudaMemcpyAsync(&total, off.p + nblocks, sizeof total, cudaMemcpyDeviceToHost, s));
+    unsigned long long nkeep = 0;
+    EJ_CUDA(cudaMemcpyAsync(&nkeep, cnt.p, sizeof nkeep, cudaMemcpyDeviceToHost, s));
     EJ_CUDA(cudaStreamSynchronize(s));
-    EJ_TRY(work.alloc(total ? total : 1, s, "work list"));
-    if (total) {
-        write_kernel<<<(unsigned)nblocks, CAND_THREADS, 0, s>>>(ncand, nT, nS, p, off.p, work.p);
+    EJ_TRY(work.alloc(nkeep ? nkeep * SB * SB : 1, s, "work list"));
+    if (nkeep) {
+        if (nkeep > 0x7fffffffull) return set_error(EJOIN_EUNSUPPORTED, "work list too large");
+        expand_kernel<<<(unsigned)nkeep, SB * SB, 0, s>>>(sps.p, nT, nS, b, work.p, cnt.p + 1);
         EJ_CUDA(cudaGetLastError());
         note_launch();
     }
+    unsigned long long total = 0;
+    EJ_CUDA(cudaMemcpyAsync(&total, cnt.p + 1, sizeof total, cudaMemcpyDeviceToHost, s));
+    EJ_CUDA(cudaStreamSynchronize(s));
     *nwork_out = total;
     return EJOIN_OK;
 }

@@ -169,63 +169,116 @@ __global__ void pack_dmma_kernel(const double* __restrict__ X, uint64_t n, uint6
 
 // --------------------------------------------------- 16-bit screen pack --
 
-template <Fmt F>
-__global__ void pack16_kernel(const double* __restrict__ X, uint64_t n, uint64_t n_pad,
-                              const uint32_t* __restrict__ perm, const uint8_t* __restrict__ bad,
-                              const double* __restrict__ mu, ScreenParams P, uint16_t* Q,
-                              float* beta) {
-    const uint64_t p = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / 32;
-    const int lane = threadIdx.x & 31;
-    if (p >= n_pad) return;
-    const FmtInfo fi = fmt_info(F);
-    const uint64_t src = p < n ? (perm ? perm[p] : p) : 0;
-    const bool good = p < n && !bad[src];
-    uint16_t* row = Q + p * (uint64_t)P.width;
-    double z2 = 0, e2 = 0, nq = 0, a2 = 0, l2 = 0;
-    for (uint32_t k = lane; k < P.dp; k += 32) {
-        double hi = 0.0, lo = 0.0;
-        if (good && k < P.d) {
-            double z = __dsub_rn(X[src * P.d + k], mu[k]) * P.scale;  // exact scaling
-            hi = round_fmt(z, fi);
-            double r = __dsub_rn(z, hi);  // exact
-            double e = r;
-            if (P.split) {
-                lo = round_fmt(r, fi);
-                e = __dsub_rn(r, lo);  // exact
-            }
-            double q = __dadd_rn(hi, lo);  // exact (<= 2 * fbits + 2 significant bits)
-            double aq = fabs(hi) + fabs(lo);
-            z2 = __fma_rn(z, z, z2);
-            e2 = __fma_rn(e, e, e2);
-            nq = __fma_rn(q, q, nq);
-            a2 = __fma_rn(aq, aq, a2);
-            l2 = __fma_rn(lo, lo, l2);
-        }
-        row[k] = to_bits16(hi, F);
-        if (P.split) row[P.dp + k] = to_bits16(lo, F);
-    }
-    z2 = warp_sum(z2);
-    e2 = warp_sum(e2);
-    nq = warp_sum(nq);
-    a2 = warp_sum(a2);
-    l2 = warp_sum(l2);
+// Round a float to `fbits` fraction bits (ties to even); results below the
+// format's smallest normal are flushed to zero.
+__device__ __forceinline__ float round_fmt_f(float v, int fbits, float min_normal) {
+    if (fabsf(v) < min_normal) return 0.0f;
+    uint32_t b = __float_as_uint(v);
+    const int sh = 23 - fbits;
+    const uint32_t lsb = (b >> sh) & 1u;
+    b += ((1u << (sh - 1)) - 1u) + lsb;
+    b &= ~((1u << sh) - 1u);
+    const float r = __uint_as_float(b);
+    return fabsf(r) < min_normal ? 0.0f : r;
+}
 
+// A warp packs 32 consecutive rows.  Phase 1 (lanes over coordinates, one row
+// at a time): z = s * fl64(x - mu) (exact scaling), zf = fl32(z),
+// hi = round(zf), lo = round(zf - hi) (split), ef = zf - hi - lo; every
+// FP32 subtraction here is exact, and the residual z - q = (z - zf) + ef with
+// |z - zf| <= 2^-24 |z|.  Per row: nq = |q|^2 in FP64, and in FP32 rounded
+// up: |zf|^2, |ef|^2, |(|hi| + |lo|)|^2, |lo|^2.  The FP32 coordinates zf and
+// a per-row radius go to Xf / rad for the FP32 band pre-check.  Phase 2 (lane
+// = row): the FP64 threshold arithmetic (alpha, beta), the aug slab.
+template <Fmt F>
+__global__ void __launch_bounds__(256) pack16_kernel(const double* __restrict__ X, uint64_t n,
+                                                     uint64_t n_pad,
+                                                     const uint32_t* __restrict__ perm,
+                                                     const uint8_t* __restrict__ bad,
+                                                     const double* __restrict__ mu, ScreenParams P,
+                                                     uint16_t* Q, float* beta, float* Xf,
+                                                     float* rad) {
+    const uint64_t p0 = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / 32 * 32;
+    const uint32_t lane = threadIdx.x & 31;
+    if (p0 >= n_pad) return;
+    const FmtInfo fi = fmt_info(F);
+    const float mnf = (float)fi.min_normal;
+    const float sf = (float)P.scale;
+    float m_z2 = 0, m_e2 = 0, m_a2 = 0, m_l2 = 0;
+    double m_nq = 0;
+    bool m_good = false;
+    for (uint32_t r = 0; r < 32; ++r) {
+        const uint64_t p = p0 + r;
+        const uint64_t src = p < n ? (perm ? perm[p] : p) : 0;
+        const bool good = p < n && !bad[src];
+        uint16_t* row = Q + p * (uint64_t)P.width;
+        float z2 = 0, e2 = 0, a2 = 0, l2 = 0;
+        double nq = 0;
+        for (uint32_t k = lane; k < P.dp; k += 32) {
+            float hi = 0.0f, lo = 0.0f, zf = 0.0f;
+            if (good && k < P.d) {
+                const double z = __dmul_rn(__dsub_rn(X[src * P.d + k], mu[k]), P.scale);
+                zf = (float)z;
+                if (fabsf(zf) < 1.1754944e-38f) zf = 0.0f;  // keep Xf free of FP32 subnormals
+                hi = round_fmt_f(zf, fi.fbits, mnf);
+                float ef = zf - hi;  // exact
+                if (P.split) {
+                    lo = round_fmt_f(ef, fi.fbits, mnf);
+                    ef = ef - lo;  // exact
+                }
+                const double q = (double)(hi + lo);  // hi + lo exact in FP32
+                nq = __fma_rn(q, q, nq);
+                const float aq = fabsf(hi) + fabsf(lo);  // exact
+                z2 = __fmaf_ru(zf, zf, z2);
+                e2 = __fmaf_ru(ef, ef, e2);
+                a2 = __fmaf_ru(aq, aq, a2);
+                l2 = __fmaf_ru(lo, lo, l2);
+            }
+            row[k] = to_bits16(hi, F);
+            if (P.split) row[P.dp + k] = to_bits16(lo, F);
+            if (k < P.d) Xf[p * P.d + k] = zf;
+        }
+        for (int o = 16; o; o >>= 1) {
+            nq += __shfl_xor_sync(0xffffffffu, nq, o);
+            z2 = __fadd_ru(z2, __shfl_xor_sync(0xffffffffu, z2, o));
+            e2 = __fadd_ru(e2, __shfl_xor_sync(0xffffffffu, e2, o));
+            a2 = __fadd_ru(a2, __shfl_xor_sync(0xffffffffu, a2, o));
+            l2 = __fadd_ru(l2, __shfl_xor_sync(0xffffffffu, l2, o));
+        }
+        if (lane == r) {
+            m_nq = nq;
+            m_z2 = z2;
+            m_e2 = e2;
+            m_a2 = a2;
+            m_l2 = l2;
+            m_good = good;
+        }
+    }
+    (void)sf;
+    // ---- phase 2: row p0 + lane
+    const uint64_t p = p0 + lane;
     double ah[3] = {0, 0, 0};
     double b = 0.0;
-    if (good) {
+    float radius = INFINITY;  // bad and padding rows: the FP32 pre-check never decides
+    if (m_good) {
         const double gs = (P.d + 4) * kU;
-        const double nup = nq * (1 + gs), ndn = nq * (1 - gs);
-        const double a2u = a2 * (1 + gs), lu = l2 * (1 + gs);
-        const double rho = (sqrt(e2 * (1 + gs)) + 1.0001 * kU * sqrt(z2 * (1 + gs))) * (1 + 8 * kU);
+        const double nup = m_nq * (1 + gs), ndn = m_nq * (1 - gs);
+        const double a2u = (double)m_a2, lu = (double)m_l2;
+        const double zn = sqrt((double)m_z2) * (1 + 1e-7);  // >= |zf|; |z| <= |zf| (1 + 2^-24)
+        // |z - q| <= |z - zf| + |ef|, plus the centring error u |z|
+        // FP32 rounding of z (relative 2^-24) or flush of values below 2^-126
+        const double zerr = (5.9604645e-08 + 2.0 * kU) * zn * 1.0001 + 1.18e-38 * sqrt((double)P.d);
+        const double rho = (sqrt((double)m_e2) * (1 + 1e-7) + zerr) * (1 + 8 * kU);
+        radius = __double2float_ru(zerr);
         double R = nup + P.cacc * a2u + lu + P.absacc - 0.5 * P.Tlo + 2.0 * P.sTlo * rho;
         R += 8 * kU * (nup + P.cacc * a2u + lu + P.absacc + 0.5 * P.Tlo + 2.0 * P.sTlo * rho);
         double at = R >= 0 ? R / (2.0 * (1.0 - P.cacc)) : R / (2.0 * (1.0 + P.cacc));
         at += fabs(at) * 4 * kU;
         at = fmax(at, P.clamp_lo);
         ah[0] = round_fmt(at, fi);
-        double r1 = __dsub_rn(at, ah[0]);
+        const double r1 = __dsub_rn(at, ah[0]);
         ah[1] = round_fmt(r1, fi);
-        double r2 = __dsub_rn(r1, ah[1]);
+        const double r2 = __dsub_rn(r1, ah[1]);
         ah[2] = round_fmt_up(r2, fi);
         const double alpha = ah[0] + ah[1] + ah[2];  // >= at (ah[2] >= r2)
         b = 0.5 * P.Thi + 2.0 * P.sThi * rho + 2.0 * rho * rho - ndn + 2.0 * alpha +
@@ -238,15 +291,33 @@ __global__ void pack16_kernel(const double* __restrict__ X, uint64_t n, uint64_t
         ah[0] = (F == Fmt::FP16) ? 32768.0 : kTwo100;
     }
     // aug slab: A side [a0 a1 a2 -1 -1 -1 0 ..] (16), B side [-1 -1 -1 a0 a1 a2 0 ..] (16), 0 x 32
-    uint16_t* aug = row + (P.split ? 2 * P.dp : P.dp);
-    double v0 = 0.0, v1 = 0.0;
-    if (lane < 3) v0 = ah[lane];
-    else if (lane < 6) v0 = -1.0;
-    else if (lane >= 16 && lane < 19) v0 = -1.0;
-    else if (lane >= 19 && lane < 22) v0 = ah[lane - 19];
-    aug[lane] = to_bits16(v0, F);
-    aug[lane + 32] = to_bits16(v1, F);
-    if (lane == 0) beta[p] = good ? __double2float_ru(b) : 0.0f;
+    uint16_t vals[32];
+#pragma unroll
+    for (int e = 0; e < 32; ++e) vals[e] = 0;
+    const uint16_t m1 = to_bits16(-1.0, F);
+    vals[0] = to_bits16(ah[0], F);
+    vals[1] = to_bits16(ah[1], F);
+    vals[2] = to_bits16(ah[2], F);
+    vals[3] = vals[4] = vals[5] = m1;
+    vals[16] = vals[17] = vals[18] = m1;
+    vals[19] = vals[0];
+    vals[20] = vals[1];
+    vals[21] = vals[2];
+    uint4* aug = reinterpret_cast<uint4*>(Q + p * (uint64_t)P.width + (P.split ? 2 * P.dp : P.dp));
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+        uint4 w;
+        w.x = vals[8 * v + 0] | ((uint32_t)vals[8 * v + 1] << 16);
+        w.y = vals[8 * v + 2] | ((uint32_t)vals[8 * v + 3] << 16);
+        w.z = vals[8 * v + 4] | ((uint32_t)vals[8 * v + 5] << 16);
+        w.w = vals[8 * v + 6] | ((uint32_t)vals[8 * v + 7] << 16);
+        aug[v] = w;
+    }
+    const uint4 zero = make_uint4(0, 0, 0, 0);
+#pragma unroll
+    for (int v = 4; v < 8; ++v) aug[v] = zero;
+    beta[p] = m_good ? __double2float_ru(b) : 0.0f;
+    rad[p] = radius;
 }
 
 __global__ void tile_max_kernel(const float* __restrict__ beta, const float4* __restrict__ meta,
@@ -314,14 +385,15 @@ int launch_pack_dmma(const double* X, uint64_t n, uint64_t n_pad, const uint32_t
 
 int launch_pack16(const double* X, uint64_t n, uint64_t n_pad, const uint32_t* perm,
                   const uint8_t* bad, const double* mu, const ScreenParams& P, void* Q,
-                  float* beta, cudaStream_t s) {
-    const uint64_t blocks = (n_pad * 32 + 255) / 256;
+                  float* beta, float* Xf, float* rad, cudaStream_t s) {
+    if (n_pad % 32) return set_error(EJOIN_EINTERNAL, "pack16: rows not padded");
+    const uint64_t blocks = (n_pad + 255) / 256;  // 8 warps x 32 rows per block
     if (P.fmt == Fmt::BF16)
         pack16_kernel<Fmt::BF16><<<(unsigned)blocks, 256, 0, s>>>(X, n, n_pad, perm, bad, mu, P,
-                                                                  (uint16_t*)Q, beta);
+                                                                  (uint16_t*)Q, beta, Xf, rad);
     else if (P.fmt == Fmt::FP16)
         pack16_kernel<Fmt::FP16><<<(unsigned)blocks, 256, 0, s>>>(X, n, n_pad, perm, bad, mu, P,
-                                                                  (uint16_t*)Q, beta);
+                                                                  (uint16_t*)Q, beta, Xf, rad);
     else
         return set_error(EJOIN_EINTERNAL, "pack16: bad format");
     EJ_CUDA(cudaGetLastError());

@@ -129,8 +129,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             uint32_t issued_ph[NST];
             uint32_t issued = 0;
             bool ok = true;
+            uint2 wn = blockIdx.x < a.nwork ? __ldg(&a.work[blockIdx.x]) : make_uint2(0, 0);
             for (uint64_t u = blockIdx.x; u < a.nwork && ok; u += gridDim.x) {
-                const uint2 w = a.work[u];
+                const uint2 w = wn;
+                if (u + gridDim.x < a.nwork) wn = __ldg(&a.work[u + gridDim.x]);  // prefetch
                 for (uint32_t step = 0; step < nsteps; ++step) {
                     if (!ptx::mbar_wait(&S.empty[st], ph ^ 1u, a.st, 10)) {
                         ok = false;
@@ -229,18 +231,31 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         const uint32_t hf = ew >> 2;           // column half
         const uint32_t et = ew * 32 + lane;    // 0..255
         uint32_t it = 0;
+        // the next tile's (I, J) and margins are loaded one tile ahead, so
+        // their latency hides behind the current tile
+        uint2 w = blockIdx.x < a.nwork ? __ldg(&a.work[blockIdx.x]) : make_uint2(0, 0);
+        float W = 0.0f;
+        if (blockIdx.x < a.nwork) {
+            const float s0 = __ldg(&a.tmax[w.x]) + __ldg(&a.tmax[w.y]);
+            W = fmaf(fabsf(s0), 9.5367431640625e-07f, s0);  // s + |s| 2^-20 >= beta_i + beta_j
+        }
         for (uint64_t u = blockIdx.x; u < a.nwork; u += gridDim.x, ++it) {
             const uint32_t b = it & 1u, use = it >> 1;
-            const uint2 w = a.work[u];
+            const bool has_next = u + gridDim.x < a.nwork;
+            uint2 wn = make_uint2(0, 0);
+            if (has_next) wn = __ldg(&a.work[u + gridDim.x]);
             const bool diag = (w.x == w.y);
-            const float s = a.tmax[w.x] + a.tmax[w.y];
-            const float W = fmaf(fabsf(s), 9.5367431640625e-07f, s);  // s + |s| 2^-20 >= beta_i + beta_j
             if (!ptx::mbar_wait(&S.tfull[b], use & 1u, a.st, 30)) break;
             ptx::tc_fence_after();
             uint32_t v[2][32];
             const uint32_t taddr = tmem + ((q * 32u) << 16) + b * 128u + hf * 64u;
             ptx::tmem_ld_32x32b_x32(taddr, v[0]);
             ptx::tmem_ld_32x32b_x32(taddr + 32u, v[1]);
+            float tnx = 0.0f, tny = 0.0f;
+            if (has_next) {
+                tnx = __ldg(&a.tmax[wn.x]);
+                tny = __ldg(&a.tmax[wn.y]);
+            }
             ptx::tmem_ld_wait();
             ptx::tc_fence_before();
             __syncwarp();
@@ -298,6 +313,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 if (c) atomicAdd(&a.counts[w.y * 128u + et - 128], c);
                 cacc[et - 128] = 0;
             }
+            const float sn = tnx + tny;
+            W = fmaf(fabsf(sn), 9.5367431640625e-07f, sn);
+            w = wn;
         }
     }
 
