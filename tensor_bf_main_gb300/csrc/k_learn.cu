@@ -250,60 +250,75 @@ __global__ void sample_pairs_kernel(const double* __restrict__ X, uint64_t n, ui
 
 constexpr int TRAIN_THREADS = 256;
 
-// Forward + hinge loss + backward for a block of pairs; G += dL/dP (atomics),
-// loss += sum of hinge terms.  P in shared memory; k <= K (rows >= k are zero).
+// Pairs per shared-memory tile of the training kernel.
+__host__ __device__ inline uint32_t train_tile_pairs(uint32_t d) {
+    uint32_t tp = 16384u / d;
+    tp = tp > 256u ? 256u : tp;
+    return tp < 8u ? 8u : tp;
+}
+__host__ inline size_t train_smem_bytes(uint32_t k, uint32_t d) {
+    const uint32_t tp = train_tile_pairs(d);
+    return (size_t)(k * d + tp * (d + 1) + tp * k) * sizeof(float);
+}
+
+// Forward + hinge loss + backward for M pairs; G += dL/dP (atomics),
+// loss += sum of hinge terms / M.  A tile of TP pairs is staged once in
+// shared memory (row pitch d + 1: conflict-free) and serves the forward pass
+// (thread per pair) and the backward pass (thread per element of G).
 template <int K>
 __global__ void __launch_bounds__(TRAIN_THREADS) train_step_kernel(const float* __restrict__ P,
                                                                    uint32_t k, uint32_t d,
                                                                    PairBatch pb, uint64_t M,
                                                                    float* G, float* loss) {
     extern __shared__ float sm[];
-    float* sP = sm;                        // k * d
-    float* sC = sm + k * d;                // TRAIN_THREADS * k coefficients
+    const uint32_t TP = train_tile_pairs(d);
+    const uint32_t pitch = d + 1;
+    float* sP = sm;                // k * d
+    float* sV = sP + k * d;        // TP * pitch
+    float* sC = sV + TP * pitch;   // TP * k coefficients
     for (uint32_t e = threadIdx.x; e < k * d; e += blockDim.x) sP[e] = P[e];
-    __syncthreads();
     const float invM = 1.0f / (float)M;
     float lsum = 0.0f;
-    for (uint64_t base = blockIdx.x * (uint64_t)TRAIN_THREADS; base < M;
-         base += (uint64_t)gridDim.x * TRAIN_THREADS) {
-        const uint64_t e = base + threadIdx.x;
-        float y[K];
-        float coef = 0.0f;
+    for (uint64_t base = blockIdx.x * (uint64_t)TP; base < M; base += (uint64_t)gridDim.x * TP) {
+        const uint32_t np = (M - base) < TP ? (uint32_t)(M - base) : TP;
+        __syncthreads();
+        for (uint32_t e = threadIdx.x; e < np * d; e += blockDim.x)
+            sV[(e / d) * pitch + e % d] = pb.V[base * d + e];
+        __syncthreads();
+        for (uint32_t p = threadIdx.x; p < TP; p += blockDim.x) {
+            float y[K];
 #pragma unroll
-        for (int a = 0; a < K; ++a) y[a] = 0.0f;
-        if (e < M && pb.tgt[e] > 0.0f) {
-            const float* v = pb.V + e * d;
-            for (uint32_t c = 0; c < d; ++c) {
-                const float vc = v[c];
+            for (int a = 0; a < K; ++a) y[a] = 0.0f;
+            float coef = 0.0f;
+            if (p < np && pb.tgt[base + p] > 0.0f) {
+                const float* v = sV + p * pitch;
+                for (uint32_t c = 0; c < d; ++c) {
+                    const float vc = v[c];
 #pragma unroll
-                for (int a = 0; a < K; ++a)
-                    if (a < (int)k) y[a] = fmaf(sP[a * d + c], vc, y[a]);
+                    for (int a = 0; a < K; ++a)
+                        if (a < (int)k) y[a] = fmaf(sP[a * d + c], vc, y[a]);
+                }
+                float r2 = 0.0f;
+#pragma unroll
+                for (int a = 0; a < K; ++a) r2 = fmaf(y[a], y[a], r2);
+                const float r = sqrtf(r2), t = pb.tgt[base + p];
+                if (r < t) {
+                    lsum += 1.0f - r / t;
+                    coef = r > 0.0f ? -invM / (t * r) : 0.0f;
+                }
             }
-            float r2 = 0.0f;
 #pragma unroll
-            for (int a = 0; a < K; ++a) r2 = fmaf(y[a], y[a], r2);
-            const float r = sqrtf(r2), t = pb.tgt[e];
-            if (r < t) {
-                lsum += 1.0f - r / t;
-                coef = r > 0.0f ? -invM / (t * r) : 0.0f;
-            }
+            for (int a = 0; a < K; ++a)
+                if (a < (int)k) sC[p * k + a] = coef * y[a];
         }
-#pragma unroll
-        for (int a = 0; a < K; ++a)
-            if (a < (int)k) sC[threadIdx.x * k + a] = coef != 0.0f ? coef * y[a] : 0.0f;
         __syncthreads();
         // G[a][c] += sum_p sC[p][a] * V[p][c]
-        const uint64_t np = (M - base) < TRAIN_THREADS ? (M - base) : TRAIN_THREADS;
         for (uint32_t el = threadIdx.x; el < k * d; el += blockDim.x) {
             const uint32_t a = el / d, c = el % d;
             float acc = 0.0f;
-            for (uint64_t p = 0; p < np; ++p) {
-                const float cf = sC[p * k + a];
-                if (cf != 0.0f) acc = fmaf(cf, pb.V[(base + p) * d + c], acc);
-            }
+            for (uint32_t p = 0; p < np; ++p) acc = fmaf(sC[p * k + a], sV[p * pitch + c], acc);
             if (acc != 0.0f) atomicAdd(&G[el], acc);
         }
-        __syncthreads();
     }
     for (int o = 16; o; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
     if ((threadIdx.x & 31) == 0 && lsum != 0.0f) atomicAdd(loss, lsum * invM);
@@ -496,11 +511,12 @@ int train_projection_dev(const double* X, const double* mu, uint64_t n, uint32_t
     const uint32_t rounds = steps >= 2 ? 2 : 1;
     const uint64_t n_pad = (n + 127) / 128 * 128;
     const float b1 = 0.9f, b2 = 0.999f, lr = 0.02f;
-    const size_t shm = (size_t)(k * d + TRAIN_THREADS * k) * sizeof(float);
-    if (shm > 200 * 1024) return set_error(EJOIN_EUNSUPPORTED, "projection too large for training");
+    const size_t shm = train_smem_bytes(k, d);
+    if (shm > 220 * 1024) return set_error(EJOIN_EUNSUPPORTED, "projection too large for training");
     auto step_fn = k <= 8 ? train_step_kernel<8> : train_step_kernel<16>;
     EJ_CUDA(cudaFuncSetAttribute(step_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
-    const unsigned grid = (unsigned)std::min<uint64_t>((B + TRAIN_THREADS - 1) / TRAIN_THREADS, 1024);
+    const uint32_t tp = train_tile_pairs(d);
+    const unsigned grid = (unsigned)std::min<uint64_t>((B + tp - 1) / tp, 1024);
     uint32_t t_step = 0;
     uint64_t cursor = 0;
     for (uint32_t r = 0; r < rounds; ++r) {
@@ -566,7 +582,7 @@ extern "C" int ejoin_testing_projection_grad(const float* V, const float* tgt, u
     EJ_CUDA(cudaMemcpyAsync(dP.p, P, (size_t)k * d * sizeof(float), cudaMemcpyHostToDevice, s));
     EJ_TRY(dG.zero(s));
     EJ_TRY(dL.zero(s));
-    const size_t shm = (size_t)(k * d + TRAIN_THREADS * k) * sizeof(float);
+    const size_t shm = train_smem_bytes(k, d);
     auto fn = k <= 8 ? train_step_kernel<8> : train_step_kernel<16>;
     EJ_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
     PairBatch pb{dV.p, dT.p};

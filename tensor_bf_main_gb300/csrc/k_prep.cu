@@ -35,10 +35,14 @@ __global__ void rowcheck_kernel(const double* __restrict__ X, uint64_t n, uint32
         for (uint32_t k = lane; k < d; k += 32) ok &= isfinite(X[row * d + k]) != 0;
     }
     ok = __all_sync(0xffffffffu, ok);
-    if (row < n && lane == 0) {
-        bad[row] = ok ? 0 : 1;
-        if (ok) atomicAdd(ngood, 1ull);
-    }
+    if (row < n && lane == 0) bad[row] = ok ? 0 : 1;
+    // one atomic per block
+    __shared__ unsigned cnt;
+    if (threadIdx.x == 0) cnt = 0;
+    __syncthreads();
+    if (row < n && lane == 0 && ok) atomicAdd(&cnt, 1u);
+    __syncthreads();
+    if (threadIdx.x == 0 && cnt) atomicAdd(ngood, (unsigned long long)cnt);
 }
 
 // partial[b][k] = sum over good rows of block b (fixed order: deterministic)
@@ -74,7 +78,13 @@ __global__ void maxabs_kernel(const double* __restrict__ X, uint64_t n, uint32_t
         for (uint32_t k = lane; k < d; k += 32) m = fmax(m, fabs(__dsub_rn(X[row * d + k], mu[k])));
     }
     for (int o = 16; o; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if (lane == 0 && m > 0.0) atomicMax(maxbits, (unsigned long long)__double_as_longlong(m));
+    // one atomic per block (non-negative doubles order like their bit patterns)
+    __shared__ unsigned long long bm;
+    if (threadIdx.x == 0) bm = 0;
+    __syncthreads();
+    if (lane == 0 && m > 0.0) atomicMax(&bm, (unsigned long long)__double_as_longlong(m));
+    __syncthreads();
+    if (threadIdx.x == 0 && bm) atomicMax(maxbits, bm);
 }
 
 __device__ __forceinline__ double warp_sum(double v) {

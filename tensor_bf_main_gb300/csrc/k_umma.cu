@@ -37,7 +37,7 @@ namespace {
 constexpr int NST = 6;                      // smem ring stages
 constexpr int SLAB_BYTES = 128 * 128;       // 128 rows x 128 bytes
 constexpr int STAGE_BYTES = 2 * SLAB_BYTES; // A slab + B slab
-constexpr int NUM_EPI_WARPS = 8;
+constexpr int NUM_EPI_WARPS = 16;          // 4 per SM sub-partition (latency hiding)
 constexpr int NTHREADS = (2 + NUM_EPI_WARPS) * 32;
 constexpr uint32_t TMEM_COLS = 256;         // two 128x128 FP32 accumulators
 constexpr uint32_t FULL = 0xffffffffu;
@@ -226,10 +226,11 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         }
     } else {
         // ------------------------------------------------ epilogue warps
-        const uint32_t ew = warp - 2;          // 0..7
+        // warp e reads lane quarter (warp % 4) and the 32 columns 32 * (e / 4)
+        const uint32_t ew = warp - 2;          // 0..15
         const uint32_t q = warp & 3u;          // tensor-memory lane quarter
-        const uint32_t hf = ew >> 2;           // column half
-        const uint32_t et = ew * 32 + lane;    // 0..255
+        const uint32_t cg = ew >> 2;           // column group
+        const uint32_t et = ew * 32 + lane;    // 0..511
         uint32_t it = 0;
         // the next tile's (I, J) and margins are loaded one tile ahead, so
         // their latency hides behind the current tile
@@ -247,10 +248,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             const bool diag = (w.x == w.y);
             if (!ptx::mbar_wait(&S.tfull[b], use & 1u, a.st, 30)) break;
             ptx::tc_fence_after();
-            uint32_t v[2][32];
-            const uint32_t taddr = tmem + ((q * 32u) << 16) + b * 128u + hf * 64u;
-            ptx::tmem_ld_32x32b_x32(taddr, v[0]);
-            ptx::tmem_ld_32x32b_x32(taddr + 32u, v[1]);
+            uint32_t v[32];
+            ptx::tmem_ld_32x32b_x32(tmem + ((q * 32u) << 16) + b * 128u + cg * 32u, v);
             float tnx = 0.0f, tny = 0.0f;
             if (has_next) {
                 tnx = __ldg(&a.tmax[wn.x]);
@@ -264,21 +263,25 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             int* racc = S.rowacc[b];
             int* cacc = S.colacc[b];
             const uint32_t row = w.x * 128u + q * 32u + lane;
-            int rowcnt = 0;
+            // Fast path: if max + W < 0 for the whole 32 x 32 chunk, every
+            // pair in it is certainly out (rounding of the FP32 add is
+            // monotone, so max + W >= 0 whenever any element is >= -W).
+            float mx = __uint_as_float(v[0]);
 #pragma unroll
-            for (int ch = 0; ch < 2; ++ch) {
+            for (int c = 1; c < 32; ++c) mx = fmaxf(mx, __uint_as_float(v[c]));
+            if (__any_sync(FULL, mx + W >= 0.0f)) {
                 uint32_t neg = 0, negw = 0;
 #pragma unroll
                 for (int c = 31; c >= 0; --c) {
-                    const uint32_t x = v[ch][c];
+                    const uint32_t x = v[c];
                     neg = __funnelshift_l(x, neg, 1);
                     const uint32_t y = __float_as_uint(__uint_as_float(x) + W);
                     negw = __funnelshift_l(y, negw, 1);
                 }
                 const uint32_t inm = ~neg;
-                rowcnt += __popc(inm);
+                const int rowcnt = __popc(inm);
                 const uint32_t bandm = neg & ~negw;
-                const uint32_t col0 = w.y * 128u + hf * 64u + ch * 32u;
+                const uint32_t col0 = w.y * 128u + cg * 32u;
                 if (__any_sync(FULL, bandm != 0)) {
                     unsigned long long slot = band_reserve(a.st, __popc(bandm));
                     uint32_t m = bandm;
@@ -294,13 +297,15 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                         ++slot;
                     }
                 }
-                if (!diag) {
-                    const uint32_t colbits = transpose32(inm, lane);
-                    const int cc = __popc(colbits);
-                    if (cc) atomicAdd(&cacc[hf * 64u + ch * 32u + lane], cc);
+                if (__any_sync(FULL, inm != 0)) {
+                    if (!diag) {
+                        const uint32_t colbits = transpose32(inm, lane);
+                        const int cc = __popc(colbits);
+                        if (cc) atomicAdd(&cacc[cg * 32u + lane], cc);
+                    }
+                    if (rowcnt) atomicAdd(&racc[q * 32u + lane], rowcnt);
                 }
             }
-            if (rowcnt) atomicAdd(&racc[q * 32u + lane], rowcnt);
             __syncwarp();
             if (lane == 0) ptx::mbar_arrive(&S.ebar[b]);
             if (!ptx::mbar_wait(&S.ebar[b], use & 1u, a.st, 31)) break;
@@ -308,7 +313,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 const int r = racc[et];
                 if (r) atomicAdd(&a.counts[w.x * 128u + et], r);
                 racc[et] = 0;
-            } else {
+            } else if (et < 256) {
                 const int c = cacc[et - 128];
                 if (c) atomicAdd(&a.counts[w.y * 128u + et - 128], c);
                 cacc[et - 128] = 0;
