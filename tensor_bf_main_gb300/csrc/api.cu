@@ -376,7 +376,7 @@ static int run_screen16(Join& J, Fmt fmt, bool split, Learned& L) {
     P.split = split ? 1 : 0;
     P.d = J.d;
     P.dp = (uint32_t)round_up(J.d, 64);
-    P.width = P.dp * (split ? 2 : 1) + 64;
+    P.width = P.dp * (split ? 2 : 1);
     P.scale = screen_scale(fmt, maxabs, J.d);
     double Tlo, Thi;
     oracle_band(J.T, J.d, &Tlo, &Thi);
@@ -389,19 +389,21 @@ static int run_screen16(Join& J, Fmt fmt, bool split, Learned& L) {
     P.Thi = std::min(Thi * s2, cap_t);
     P.sTlo = sqrt(P.Tlo) * (1 - 4 * kU);
     P.sThi = sqrt(P.Thi) * (1 + 4 * kU);
-    const double kprod = (split ? 3.0 : 1.0) * P.dp + 16.0;
+    const double kprod = (split ? 3.0 : 1.0) * P.dp + 16.0;  // + the aug K = 16 step
     const double scale_opt = J.opt.acc_bound_scale > 0 ? J.opt.acc_bound_scale : 1.0;
     P.cacc = scale_opt * (kprod + 16.0) * ldexp(1.0, -22);
     P.absacc = (kprod + 16.0) * ldexp(1.0, -125);
     P.clamp_lo = (fmt == Fmt::FP16) ? -16384.0 : -kTwo100;
-    DBuf<uint16_t> Q;
+    DBuf<uint16_t> Q, Aug;
     DBuf<float> beta, tmax, Xf, rad;
     EJ_TRY(Q.alloc(n_pad * P.width, J.s, "packed operands"));
+    EJ_TRY(Aug.alloc(n_pad * 32, J.s, "aug operands"));
     EJ_TRY(beta.alloc(n_pad, J.s, "out margins"));
     EJ_TRY(tmax.alloc(n_pad / 128, J.s, "tile margins"));
     EJ_TRY(Xf.alloc(n_pad * J.d, J.s, "FP32 coordinates"));
     EJ_TRY(rad.alloc(n_pad, J.s, "FP32 radii"));
-    EJ_TRY(launch_pack16(J.X, J.n, n_pad, J.perm, bad.p, mu.p, P, Q.p, beta.p, Xf.p, rad.p, J.s));
+    EJ_TRY(launch_pack16(J.X, J.n, n_pad, J.perm, bad.p, mu.p, P, Q.p, Aug.p, beta.p, Xf.p, rad.p,
+                         J.s));
     EJ_TRY(launch_tile_max(beta.p, nullptr, n_pad, tmax.p, J.s));
     tp.stop(J.s);
     J.st->ms_prep = ms_center + tp.ms();
@@ -418,8 +420,8 @@ static int run_screen16(Join& J, Fmt fmt, bool split, Learned& L) {
     J.st->gram_flops = 2.0 * kprod * 128.0 * 128.0 * (double)nwork;
     J.st->precision = fmt == Fmt::FP16 ? EJOIN_FP16 : (split ? EJOIN_BF16_SPLIT : EJOIN_BF16);
     auto screen = [&](BandPair* band, uint64_t cap, DevStatus* st) {
-        return launch_gram16(Q.p, n_pad, P, work.p, nwork, tmax.p, J.counts, band, cap, st, J.sms,
-                             J.s);
+        return launch_gram16(Q.p, Aug.p, n_pad, P, work.p, nwork, tmax.p, J.counts, band, cap, st,
+                             J.sms, J.s);
     };
     Recheck32 R;
     R.Xf = Xf.p;

@@ -190,7 +190,7 @@ struct ScreenParams {
     double absacc;     // absolute bound (FP32 underflow) of the same
     double clamp_lo;   // smallest alpha the operand format can carry
     uint32_t d, dp;    // coordinates, padded coordinates (per slab multiple)
-    uint32_t width;    // packed row width in elements
+    uint32_t width;    // packed row width in elements (dp, or 2 dp with the split)
     int split;         // 1 = hi + lo products
     Fmt fmt;
 };
@@ -230,9 +230,9 @@ int launch_dmma_join(const double* Y, uint64_t n_pad, uint32_t dp, const double*
                      DevStatus* st, cudaStream_t s);
 
 // k_umma.cu: tcgen05 Gram screen over a tile-pair work list (16-bit operands).
-int launch_gram16(const void* Q, uint64_t n_pad, const ScreenParams& P, const uint2* work,
-                  uint64_t nwork, const float* tmax, int32_t* counts, BandPair* band,
-                  uint64_t band_cap, DevStatus* st, int num_sms, cudaStream_t s);
+int launch_gram16(const void* Q, const void* aug, uint64_t n_pad, const ScreenParams& P,
+                  const uint2* work, uint64_t nwork, const float* tmax, int32_t* counts,
+                  BandPair* band, uint64_t band_cap, DevStatus* st, int num_sms, cudaStream_t s);
 
 // k_misc.cu
 // Ordered list of the upper-triangle 128-row tile pairs (I <= J), grouped by
@@ -272,11 +272,12 @@ int launch_center_stats(const double* X, uint64_t n, uint32_t d, uint8_t* bad, d
 int launch_pack_dmma(const double* X, uint64_t n, uint64_t n_pad, const uint32_t* perm,
                      const uint8_t* bad, const double* mu, const DmmaParams& P, double* Y,
                      double* h, double* g, cudaStream_t s);
-// 16-bit operand rows [hi | lo | aug], per-row out-margins beta, FP32
-// coordinates Xf ([n_pad][d], scaled, centred) and their per-row error radius.
+// 16-bit operand rows [hi | lo], aug rows [augA(16) | augB(16)], per-row
+// out-margins beta, FP32 coordinates Xf ([n_pad][d], scaled, centred) and
+// their per-row error radius.
 int launch_pack16(const double* X, uint64_t n, uint64_t n_pad, const uint32_t* perm,
                   const uint8_t* bad, const double* mu, const ScreenParams& P, void* Q,
-                  float* beta, float* Xf, float* rad, cudaStream_t s);
+                  void* Aug, float* beta, float* Xf, float* rad, cudaStream_t s);
 // FP8 operand rows and per-row (sigma, alpha, beta, 0).
 int launch_pack8(const double* X, uint64_t n, uint64_t n_pad, const uint32_t* perm,
                  const uint8_t* bad, const double* mu, const ScreenParams& P, uint8_t* Q,

@@ -6,6 +6,8 @@
 // operand rows that stay resident in L2.  The list is built by ordered
 // stream compaction over the candidate index space; the same pass drops tile
 // pairs the learned projection proves empty (see k_learn.cu for the bound).
+#include <cub/cub.cuh>
+
 #include "ejoin_internal.cuh"
 
 namespace ejoin {
@@ -136,7 +138,16 @@ int build_worklist(uint64_t nT, const LearnedBoxes* boxes, float thr, DBuf<uint2
     EJ_TRY(work.alloc(nkeep ? nkeep * SB * SB : 1, s, "work list"));
     if (nkeep) {
         if (nkeep > 0x7fffffffull) return set_error(EJOIN_EUNSUPPORTED, "work list too large");
-        expand_kernel<<<(unsigned)nkeep, SB * SB, 0, s>>>(sps.p, nT, nS, b, work.p, cnt.p + 1);
+        // back into triangular (row-major) order: consecutive work then shares row blocks
+        DBuf<uint32_t> sorted;
+        EJ_TRY(sorted.alloc(nkeep, s, "sorted super-block pairs"));
+        size_t tb = 0;
+        EJ_CUDA(cub::DeviceRadixSort::SortKeys(nullptr, tb, sps.p, sorted.p, (int)nkeep, 0, 32, s));
+        DBuf<uint8_t> tmp;
+        EJ_TRY(tmp.alloc(tb, s, "sort scratch"));
+        EJ_CUDA(cub::DeviceRadixSort::SortKeys(tmp.p, tb, sps.p, sorted.p, (int)nkeep, 0, 32, s));
+        note_launch(4);
+        expand_kernel<<<(unsigned)nkeep, SB * SB, 0, s>>>(sorted.p, nT, nS, b, work.p, cnt.p + 1);
         EJ_CUDA(cudaGetLastError());
         note_launch();
     }

@@ -206,8 +206,8 @@ __global__ void __launch_bounds__(256) pack16_kernel(const double* __restrict__ 
                                                      const uint32_t* __restrict__ perm,
                                                      const uint8_t* __restrict__ bad,
                                                      const double* __restrict__ mu, ScreenParams P,
-                                                     uint16_t* Q, float* beta, float* Xf,
-                                                     float* rad) {
+                                                     uint16_t* Q, uint16_t* Aug, float* beta,
+                                                     float* Xf, float* rad) {
     const uint64_t p0 = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / 32 * 32;
     const uint32_t lane = threadIdx.x & 31;
     if (p0 >= n_pad) return;
@@ -300,7 +300,7 @@ __global__ void __launch_bounds__(256) pack16_kernel(const double* __restrict__ 
         // never in, never band: C = q_i.q_j - alpha_i - alpha_j << -W
         ah[0] = (F == Fmt::FP16) ? 32768.0 : kTwo100;
     }
-    // aug slab: A side [a0 a1 a2 -1 -1 -1 0 ..] (16), B side [-1 -1 -1 a0 a1 a2 0 ..] (16), 0 x 32
+    // aug row: A side [a0 a1 a2 -1 -1 -1 0 ..] (16), B side [-1 -1 -1 a0 a1 a2 0 ..] (16)
     uint16_t vals[32];
 #pragma unroll
     for (int e = 0; e < 32; ++e) vals[e] = 0;
@@ -313,7 +313,7 @@ __global__ void __launch_bounds__(256) pack16_kernel(const double* __restrict__ 
     vals[19] = vals[0];
     vals[20] = vals[1];
     vals[21] = vals[2];
-    uint4* aug = reinterpret_cast<uint4*>(Q + p * (uint64_t)P.width + (P.split ? 2 * P.dp : P.dp));
+    uint4* aug = reinterpret_cast<uint4*>(Aug + p * 32);
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
         uint4 w;
@@ -323,9 +323,6 @@ __global__ void __launch_bounds__(256) pack16_kernel(const double* __restrict__ 
         w.w = vals[8 * v + 6] | ((uint32_t)vals[8 * v + 7] << 16);
         aug[v] = w;
     }
-    const uint4 zero = make_uint4(0, 0, 0, 0);
-#pragma unroll
-    for (int v = 4; v < 8; ++v) aug[v] = zero;
     beta[p] = m_good ? __double2float_ru(b) : 0.0f;
     rad[p] = radius;
 }
@@ -395,15 +392,17 @@ int launch_pack_dmma(const double* X, uint64_t n, uint64_t n_pad, const uint32_t
 
 int launch_pack16(const double* X, uint64_t n, uint64_t n_pad, const uint32_t* perm,
                   const uint8_t* bad, const double* mu, const ScreenParams& P, void* Q,
-                  float* beta, float* Xf, float* rad, cudaStream_t s) {
+                  void* Aug, float* beta, float* Xf, float* rad, cudaStream_t s) {
     if (n_pad % 32) return set_error(EJOIN_EINTERNAL, "pack16: rows not padded");
     const uint64_t blocks = (n_pad + 255) / 256;  // 8 warps x 32 rows per block
     if (P.fmt == Fmt::BF16)
         pack16_kernel<Fmt::BF16><<<(unsigned)blocks, 256, 0, s>>>(X, n, n_pad, perm, bad, mu, P,
-                                                                  (uint16_t*)Q, beta, Xf, rad);
+                                                                  (uint16_t*)Q, (uint16_t*)Aug,
+                                                                  beta, Xf, rad);
     else if (P.fmt == Fmt::FP16)
         pack16_kernel<Fmt::FP16><<<(unsigned)blocks, 256, 0, s>>>(X, n, n_pad, perm, bad, mu, P,
-                                                                  (uint16_t*)Q, beta, Xf, rad);
+                                                                  (uint16_t*)Q, (uint16_t*)Aug,
+                                                                  beta, Xf, rad);
     else
         return set_error(EJOIN_EINTERNAL, "pack16: bad format");
     EJ_CUDA(cudaGetLastError());

@@ -34,9 +34,14 @@
 namespace ejoin {
 namespace {
 
-constexpr int NST = 6;                      // smem ring stages
+constexpr int NST = 5;                      // smem ring stages
 constexpr int SLAB_BYTES = 128 * 128;       // 128 rows x 128 bytes
-constexpr int STAGE_BYTES = 2 * SLAB_BYTES; // A slab + B slab
+constexpr int AUG_BYTES = 128 * 32;         // 128 rows x 32 bytes (16 elements)
+// A slab | B slab | A aug | B aug; the aug boxes are loaded with the first
+// slab of every tile only
+constexpr int STAGE_BYTES = 2 * SLAB_BYTES + 2 * AUG_BYTES;
+constexpr uint32_t DATA_TX = 2 * SLAB_BYTES;
+constexpr uint32_t FIRST_TX = 2 * SLAB_BYTES + 2 * AUG_BYTES;
 constexpr int NUM_EPI_WARPS = 16;          // 4 per SM sub-partition (latency hiding)
 constexpr int NTHREADS = (2 + NUM_EPI_WARPS) * 32;
 constexpr uint32_t TMEM_COLS = 256;         // two 128x128 FP32 accumulators
@@ -81,17 +86,16 @@ __device__ __forceinline__ uint32_t transpose32(uint32_t x, uint32_t lane) {
     return x;
 }
 
+// Element offset of K-slab `step` of a tile: [hi0, lo0, hi1, lo1, ...] with the
+// split, [hi0, hi1, ...] without.
 __device__ __forceinline__ uint32_t slab_x(uint32_t step, uint32_t nhi, uint32_t split) {
-    const uint32_t dp = 64 * nhi;
-    if (split) {
-        if (step < 2 * nhi) return (step & 1) ? dp + 64 * (step >> 1) : 64 * (step >> 1);
-        return 2 * dp;
-    }
-    return step < nhi ? 64 * step : dp;
+    if (split) return (step & 1) ? 64 * nhi + 64 * (step >> 1) : 64 * (step >> 1);
+    return 64 * step;
 }
 
 __global__ void __launch_bounds__(NTHREADS, 1)
-    gram_kernel(const __grid_constant__ CUtensorMap tq, const GramArgs a) {
+    gram_kernel(const __grid_constant__ CUtensorMap tq, const __grid_constant__ CUtensorMap taug,
+                const GramArgs a) {
     extern __shared__ uint8_t smraw[];
     uint8_t* stages = (uint8_t*)(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
     Ctl& S = *reinterpret_cast<Ctl*>(stages + (size_t)NST * STAGE_BYTES);
@@ -114,13 +118,14 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         ptx::mbar_init(&S.fin, 1);
         ptx::fence_barrier_init();
         ptx::tma_prefetch_desc(&tq);
+        ptx::tma_prefetch_desc(&taug);
     }
     for (int i = threadIdx.x; i < 512; i += NTHREADS) (&S.rowacc[0][0])[i] = 0;
     ptx::tc_fence_before();
     __syncthreads();
     ptx::tc_fence_after();
     const uint32_t tmem = S.tmem_base;
-    const uint32_t nsteps = a.nhi * (a.split ? 2u : 1u) + 1u;
+    const uint32_t nsteps = a.nhi * (a.split ? 2u : 1u);
 
     if (warp == 0) {
         // ------------------------------------------------ TMA producer
@@ -140,9 +145,15 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                     }
                     uint8_t* sa = stages + (size_t)st * STAGE_BYTES;
                     const int32_t x = (int32_t)slab_x(step, a.nhi, a.split);
-                    ptx::mbar_arrive_expect_tx(&S.full[st], STAGE_BYTES);
+                    ptx::mbar_arrive_expect_tx(&S.full[st], step == 0 ? FIRST_TX : DATA_TX);
                     ptx::tma_load_2d(sa, &tq, x, (int32_t)(w.x * 128u), &S.full[st]);
                     ptx::tma_load_2d(sa + SLAB_BYTES, &tq, x, (int32_t)(w.y * 128u), &S.full[st]);
+                    if (step == 0) {
+                        ptx::tma_load_2d(sa + 2 * SLAB_BYTES, &taug, 0, (int32_t)(w.x * 128u),
+                                         &S.full[st]);
+                        ptx::tma_load_2d(sa + 2 * SLAB_BYTES + AUG_BYTES, &taug, 16,
+                                         (int32_t)(w.y * 128u), &S.full[st]);
+                    }
                     issued_ph[st] = ph;
                     ++issued;
                     if (++st == NST) {
@@ -184,15 +195,24 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                     if (!take(s_hi)) { ok = false; break; }
                     if (a.split && !take(s_lo)) { ok = false; break; }
                     ptx::tc_fence_after();
-                    const uint64_t ah = ptx::sdesc_sw128(ptx::smem_u32(stages + (size_t)s_hi * STAGE_BYTES));
-                    const uint64_t bh = ptx::sdesc_sw128(ptx::smem_u32(stages + (size_t)s_hi * STAGE_BYTES + SLAB_BYTES));
+                    uint8_t* st_hi = stages + (size_t)s_hi * STAGE_BYTES;
+                    const uint64_t ah = ptx::sdesc_sw128(ptx::smem_u32(st_hi));
+                    const uint64_t bh = ptx::sdesc_sw128(ptx::smem_u32(st_hi + SLAB_BYTES));
+                    if (c == 0) {
+                        // aug: A side (alpha_i, -1) x B side (-1, alpha_j), one K = 16 step
+                        const uint64_t aa = ptx::sdesc_sw32(ptx::smem_u32(st_hi + 2 * SLAB_BYTES));
+                        const uint64_t ba =
+                            ptx::sdesc_sw32(ptx::smem_u32(st_hi + 2 * SLAB_BYTES + AUG_BYTES));
+                        ptx::mma_f16(d_tmem, aa, ba, idesc, 0);
+                        acc = 1;
+                    }
                     if (a.split) {
-                        const uint64_t al = ptx::sdesc_sw128(ptx::smem_u32(stages + (size_t)s_lo * STAGE_BYTES));
-                        const uint64_t bl = ptx::sdesc_sw128(ptx::smem_u32(stages + (size_t)s_lo * STAGE_BYTES + SLAB_BYTES));
+                        uint8_t* st_lo = stages + (size_t)s_lo * STAGE_BYTES;
+                        const uint64_t al = ptx::sdesc_sw128(ptx::smem_u32(st_lo));
+                        const uint64_t bl = ptx::sdesc_sw128(ptx::smem_u32(st_lo + SLAB_BYTES));
 #pragma unroll
                         for (uint32_t kk = 0; kk < 4; ++kk) {
                             ptx::mma_f16(d_tmem, ah + 2 * kk, bh + 2 * kk, idesc, acc);
-                            acc = 1;
                             ptx::mma_f16(d_tmem, ah + 2 * kk, bl + 2 * kk, idesc, 1);
                             ptx::mma_f16(d_tmem, al + 2 * kk, bh + 2 * kk, idesc, 1);
                         }
@@ -200,24 +220,12 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                         ptx::mma_commit(&S.empty[s_lo]);
                     } else {
 #pragma unroll
-                        for (uint32_t kk = 0; kk < 4; ++kk) {
+                        for (uint32_t kk = 0; kk < 4; ++kk)
                             ptx::mma_f16(d_tmem, ah + 2 * kk, bh + 2 * kk, idesc, acc);
-                            acc = 1;
-                        }
                         ptx::mma_commit(&S.empty[s_hi]);
                     }
                 }
                 if (!ok) break;
-                uint32_t s_aug;
-                if (!take(s_aug)) break;
-                ptx::tc_fence_after();
-                {
-                    // A side: aug elements 0..15, B side: aug elements 16..31 (+32 bytes)
-                    const uint64_t aa = ptx::sdesc_sw128(ptx::smem_u32(stages + (size_t)s_aug * STAGE_BYTES));
-                    const uint64_t ba = ptx::sdesc_sw128(ptx::smem_u32(stages + (size_t)s_aug * STAGE_BYTES + SLAB_BYTES)) + 2;
-                    ptx::mma_f16(d_tmem, aa, ba, idesc, acc);
-                }
-                ptx::mma_commit(&S.empty[s_aug]);
                 ptx::mma_commit(&S.tfull[b]);
             }
             // drain: all MMAs complete before tensor memory is freed
@@ -334,17 +342,17 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 
 }  // namespace
 
-int launch_gram16(const void* Q, uint64_t n_pad, const ScreenParams& P, const uint2* work,
-                  uint64_t nwork, const float* tmax, int32_t* counts, BandPair* band,
-                  uint64_t band_cap, DevStatus* st, int num_sms, cudaStream_t s) {
+int launch_gram16(const void* Q, const void* aug, uint64_t n_pad, const ScreenParams& P,
+                  const uint2* work, uint64_t nwork, const float* tmax, int32_t* counts,
+                  BandPair* band, uint64_t band_cap, DevStatus* st, int num_sms, cudaStream_t s) {
     if (nwork == 0) return EJOIN_OK;
     if (n_pad % 128 || P.dp % 64) return set_error(EJOIN_EINTERNAL, "gram16: bad padding");
     if (n_pad > 0x7fffff80ull) return set_error(EJOIN_EUNSUPPORTED, "gram16: too many rows");
-    CUtensorMap map;
-    EJ_TRY(make_tmap_2d(&map, Q,
-                        P.fmt == Fmt::BF16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16
-                                           : CU_TENSOR_MAP_DATA_TYPE_FLOAT16,
-                        2, P.width, n_pad, 64, 128));
+    CUtensorMap map, amap;
+    const CUtensorMapDataType dt =
+        P.fmt == Fmt::BF16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16;
+    EJ_TRY(make_tmap_2d(&map, Q, dt, 2, P.width, n_pad, 64, 128));
+    EJ_TRY(make_tmap_2d(&amap, aug, dt, 2, 32, n_pad, 16, 128));
     GramArgs a;
     a.work = work;
     a.nwork = nwork;
@@ -359,7 +367,7 @@ int launch_gram16(const void* Q, uint64_t n_pad, const ScreenParams& P, const ui
     EJ_CUDA(cudaFuncSetAttribute(gram_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)SMEM_BYTES));
     const uint64_t grid = nwork < (uint64_t)num_sms ? nwork : (uint64_t)num_sms;
-    gram_kernel<<<(unsigned)grid, NTHREADS, SMEM_BYTES, s>>>(map, a);
+    gram_kernel<<<(unsigned)grid, NTHREADS, SMEM_BYTES, s>>>(map, amap, a);
     EJ_CUDA(cudaGetLastError());
     note_launch();
     return EJOIN_OK;

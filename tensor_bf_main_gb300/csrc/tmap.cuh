@@ -31,20 +31,23 @@ inline PFN_encodeTiled get_encode_tiled() {
 }
 
 // Row-major [rows][width] matrix of `esize`-byte elements; box of
-// box_w elements (box_w * esize == 128 for the 128-byte swizzle) x box_h rows.
+// box_w elements x box_h rows; the swizzle span equals the box row
+// (box_w * esize = 128 or 32 bytes).
 inline int make_tmap_2d(CUtensorMap* map, const void* base, CUtensorMapDataType dtype,
                         uint32_t esize, uint64_t width, uint64_t rows, uint32_t box_w,
                         uint32_t box_h) {
     PFN_encodeTiled enc = get_encode_tiled();
     if (!enc) return set_error(EJOIN_ECUDA, "cuTensorMapEncodeTiled entry point unavailable");
-    if (((uintptr_t)base & 15) || (width * esize) % 16 || box_w * esize != 128)
+    const uint32_t span = box_w * esize;
+    if (((uintptr_t)base & 15) || (width * esize) % 16 || (span != 128 && span != 32))
         return set_error(EJOIN_EINTERNAL, "tensor map: misaligned base/stride/box");
     cuuint64_t dims[2] = {width, rows};
     cuuint64_t strides[1] = {width * esize};
     cuuint32_t box[2] = {box_w, box_h};
     cuuint32_t estr[2] = {1, 1};
     CUresult r = enc(map, dtype, 2, const_cast<void*>(base), dims, strides, box, estr,
-                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE,
+                     span == 128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_32B,
                      CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return set_error(EJOIN_ECUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
     return EJOIN_OK;

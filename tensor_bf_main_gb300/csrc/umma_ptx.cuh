@@ -139,6 +139,18 @@ __device__ __forceinline__ uint64_t sdesc_sw128(uint32_t saddr) {
     return d;
 }
 
+// Same for a K-major operand with the 32-byte swizzle: rows of 32 bytes
+// (16 16-bit elements, one K = 16 MMA step), 8-row (256-byte) atoms.
+__device__ __forceinline__ uint64_t sdesc_sw32(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+    d |= (uint64_t)1u << 16;
+    d |= (uint64_t)(256u >> 4) << 32;
+    d |= (uint64_t)1u << 46;
+    d |= (uint64_t)6u << 61;
+    return d;
+}
+
 // Instruction descriptor, dense kind::f16 / kind::f8f6f4 with FP32 accumulate,
 // both operands K-major.  a_fmt/b_fmt: kind::f16 0 = F16, 1 = BF16;
 // kind::f8f6f4 0 = E4M3.  Bits: 4-5 D format (1 = F32), 7-9 A format,

@@ -46,18 +46,29 @@ __global__ void __launch_bounds__(128, 1) probe_kernel(const __grid_constant__ C
     const uint32_t tmem = tmem_base;
     bool ok = true;
     if (threadIdx.x == 0) {
-        ptx::mbar_arrive_expect_tx(&bar_full, 2u * nslab * kSlabBytes);
-        const int ew = (fmt == 2) ? 128 : 64;  // elements per 128-byte row
-        for (int s = 0; s < nslab; ++s) {
-            ptx::tma_load_2d(sA + s * kSlabBytes, &ta, s * ew, 0, &bar_full);
-            ptx::tma_load_2d(sB + s * kSlabBytes, &tb, s * ew, 0, &bar_full);
+        if (mode == 2) {
+            ptx::mbar_arrive_expect_tx(&bar_full, 2u * 128 * 32);
+            ptx::tma_load_2d(sA, &ta, 0, 0, &bar_full);
+            ptx::tma_load_2d(sB, &tb, 16, 0, &bar_full);
+        } else {
+            ptx::mbar_arrive_expect_tx(&bar_full, 2u * nslab * kSlabBytes);
+            const int ew = (fmt == 2) ? 128 : 64;  // elements per 128-byte row
+            for (int s = 0; s < nslab; ++s) {
+                ptx::tma_load_2d(sA + s * kSlabBytes, &ta, s * ew, 0, &bar_full);
+                ptx::tma_load_2d(sB + s * kSlabBytes, &tb, s * ew, 0, &bar_full);
+            }
         }
         ok = ptx::mbar_wait(&bar_full, 0, st, 1);
         if (ok) {
             ptx::tc_fence_after();
             const uint32_t idesc = (fmt == 2) ? ptx::idesc_f32acc(0, 0, 128, 128)
                                               : ptx::idesc_f32acc(fmt == 1 ? 1 : 0, fmt == 1 ? 1 : 0, 128, 128);
-            if (mode == 0) {
+            if (mode == 2) {
+                // 32-byte swizzled [128][16] tiles: A from box x=0 of ta, B from box x=16 of tb
+                uint64_t ad = ptx::sdesc_sw32(ptx::smem_u32(sA));
+                uint64_t bd = ptx::sdesc_sw32(ptx::smem_u32(sB));
+                ptx::mma_f16(tmem, ad, bd, idesc, 0);
+            } else if (mode == 0) {
                 for (int s = 0; s < nslab; ++s)
                     for (int kk = 0; kk < 4; ++kk) {
                         uint64_t ad = ptx::sdesc_sw128(ptx::smem_u32(sA + s * kSlabBytes)) + 2 * kk;
@@ -116,8 +127,12 @@ extern "C" int umma_probe_gram(const void* A, const void* B, int nslab, int fmt,
     cudaMemcpy(dB, B, bytes, cudaMemcpyHostToDevice);
     cudaMemset(dD, 0, 128 * 128 * 4);
     cudaMemset(dst, 0, sizeof(DevStatus));
-    if (make_tmap_2d(&ma, dA, dt, es, width, 128, 128 / es, 128) ||
-        make_tmap_2d(&mb, dB, dt, es, width, 128, 128 / es, 128)) { rc = -3; goto done; }
+    if (mode == 2) {
+        // [128][32] 16-bit matrices, boxes of 16 elements (32 bytes)
+        if (make_tmap_2d(&ma, dA, dt, es, 32, 128, 16, 128) ||
+            make_tmap_2d(&mb, dB, dt, es, 32, 128, 16, 128)) { rc = -3; goto done; }
+    } else if (make_tmap_2d(&ma, dA, dt, es, width, 128, 128 / es, 128) ||
+               make_tmap_2d(&mb, dB, dt, es, width, 128, 128 / es, 128)) { rc = -3; goto done; }
     if (cudaFuncSetAttribute(probe_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) { rc = -4; goto done; }
     probe_kernel<<<1, 128, smem>>>(ma, mb, nslab, fmt, mode, dD, dst);
     if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) { rc = -5; goto done; }

@@ -93,3 +93,28 @@ def test_probe_accumulation_error_within_bound(probe):
     bound = (K + 16) * 2.0 ** -22
     print(f"max accumulation error / sum|p| = {rel:.3e} (bound {bound:.3e})")
     assert rel * 4 <= bound
+
+
+@pytest.mark.parametrize("fmt", [0, 1])
+def test_probe_sw32_aug_tiles(probe, fmt):
+    """The aug operands: [rows][32] 16-bit arrays, A = columns 0..15 and
+    B = columns 16..31, loaded as 32-byte-swizzled boxes (one K = 16 step)."""
+    rng = np.random.default_rng(40 + fmt)
+    a = rng.standard_normal((128, 64)).astype(np.float32)
+    b = rng.standard_normal((128, 64)).astype(np.float32)
+    if fmt == 1:
+        A, B = f32_to_bf16_bits(a), f32_to_bf16_bits(b)
+        af, bf = bf16_bits_to_f64(A), bf16_bits_to_f64(B)
+    else:
+        A, B = a.astype(np.float16).view(np.uint16), b.astype(np.float16).view(np.uint16)
+        af, bf = a.astype(np.float16).astype(np.float64), b.astype(np.float16).astype(np.float64)
+    # the probe reads the first 128 x 32 elements of each buffer as [128][32]
+    A32 = np.ascontiguousarray(A[:, :32])
+    B32 = np.ascontiguousarray(B[:, :32])
+    Ap = np.zeros((128, 64), dtype=np.uint16)
+    Bp = np.zeros((128, 64), dtype=np.uint16)
+    Ap.reshape(-1)[: 128 * 32] = A32.reshape(-1)
+    Bp.reshape(-1)[: 128 * 32] = B32.reshape(-1)
+    D = probe(Ap, Bp, 1, fmt, 2)
+    ref = af[:, :16] @ bf[:, 16:32].T
+    assert np.allclose(D, ref, rtol=1e-5, atol=1e-5)
