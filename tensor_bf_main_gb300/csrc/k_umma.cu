@@ -43,7 +43,8 @@ constexpr int STAGE_BYTES = 2 * SLAB_BYTES + 2 * AUG_BYTES;
 constexpr uint32_t DATA_TX = 2 * SLAB_BYTES;
 constexpr uint32_t FIRST_TX = 2 * SLAB_BYTES + 2 * AUG_BYTES;
 constexpr int NUM_EPI_WARPS = 16;          // 4 per SM sub-partition (latency hiding)
-constexpr int NTHREADS = (2 + NUM_EPI_WARPS) * 32;
+constexpr int FLUSH_WARP = 2 + NUM_EPI_WARPS;  // adds the per-tile counts to global memory
+constexpr int NTHREADS = (3 + NUM_EPI_WARPS) * 32;
 constexpr uint32_t TMEM_COLS = 256;         // two 128x128 FP32 accumulators
 constexpr uint32_t FULL = 0xffffffffu;
 
@@ -63,7 +64,8 @@ struct GramArgs {
 struct Ctl {
     uint64_t full[NST], empty[NST];
     uint64_t tfull[2], tempty[2];
-    uint64_t ebar[2];
+    uint64_t ebar[2];   // epilogue warps done with the counts of buffer b
+    uint64_t fdone[2];  // flusher done with (and cleared) the counts of buffer b
     uint64_t fin;
     uint32_t tmem_base;
     int rowacc[2][128];
@@ -114,6 +116,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             ptx::mbar_init(&S.tfull[b], 1);
             ptx::mbar_init(&S.tempty[b], NUM_EPI_WARPS);
             ptx::mbar_init(&S.ebar[b], NUM_EPI_WARPS);
+            ptx::mbar_init(&S.fdone[b], 1);
         }
         ptx::mbar_init(&S.fin, 1);
         ptx::fence_barrier_init();
@@ -232,13 +235,12 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             ptx::mma_commit(&S.fin);
             ptx::mbar_wait(&S.fin, 0, a.st, 22);
         }
-    } else {
+    } else if (warp < FLUSH_WARP) {
         // ------------------------------------------------ epilogue warps
         // warp e reads lane quarter (warp % 4) and the 32 columns 32 * (e / 4)
         const uint32_t ew = warp - 2;          // 0..15
         const uint32_t q = warp & 3u;          // tensor-memory lane quarter
         const uint32_t cg = ew >> 2;           // column group
-        const uint32_t et = ew * 32 + lane;    // 0..511
         uint32_t it = 0;
         // the next tile's (I, J) and margins are loaded one tile ahead, so
         // their latency hides behind the current tile
@@ -268,27 +270,40 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             __syncwarp();
             if (lane == 0) ptx::mbar_arrive(&S.tempty[b]);
 
-            int* racc = S.rowacc[b];
-            int* cacc = S.colacc[b];
-            const uint32_t row = w.x * 128u + q * 32u + lane;
             // Fast path: if max + W < 0 for the whole 32 x 32 chunk, every
             // pair in it is certainly out (rounding of the FP32 add is
             // monotone, so max + W >= 0 whenever any element is >= -W).
-            float mx = __uint_as_float(v[0]);
+            float m8[8];
 #pragma unroll
-            for (int c = 1; c < 32; ++c) mx = fmaxf(mx, __uint_as_float(v[c]));
-            if (__any_sync(FULL, mx + W >= 0.0f)) {
-                uint32_t neg = 0, negw = 0;
+            for (int j = 0; j < 8; ++j)
+                m8[j] = fmaxf(fmaxf(__uint_as_float(v[j]), __uint_as_float(v[j + 8])),
+                              fmaxf(__uint_as_float(v[j + 16]), __uint_as_float(v[j + 24])));
+            const float mx = fmaxf(fmaxf(fmaxf(m8[0], m8[1]), fmaxf(m8[2], m8[3])),
+                                   fmaxf(fmaxf(m8[4], m8[5]), fmaxf(m8[6], m8[7])));
+            const bool busy = __any_sync(FULL, mx + W >= 0.0f);
+            uint32_t inm = 0, bandm = 0;
+            if (busy) {
+                // sign bits, four independent 8-column chains
+                uint32_t ng[4] = {0, 0, 0, 0}, nw[4] = {0, 0, 0, 0};
 #pragma unroll
-                for (int c = 31; c >= 0; --c) {
-                    const uint32_t x = v[c];
-                    neg = __funnelshift_l(x, neg, 1);
-                    const uint32_t y = __float_as_uint(__uint_as_float(x) + W);
-                    negw = __funnelshift_l(y, negw, 1);
-                }
-                const uint32_t inm = ~neg;
-                const int rowcnt = __popc(inm);
-                const uint32_t bandm = neg & ~negw;
+                for (int c = 7; c >= 0; --c)
+#pragma unroll
+                    for (int g = 0; g < 4; ++g) {
+                        const uint32_t x = v[8 * g + c];
+                        ng[g] = __funnelshift_l(x, ng[g], 1);
+                        nw[g] = __funnelshift_l(__float_as_uint(__uint_as_float(x) + W), nw[g], 1);
+                    }
+                const uint32_t neg = ng[0] | (ng[1] << 8) | (ng[2] << 16) | (ng[3] << 24);
+                const uint32_t negw = nw[0] | (nw[1] << 8) | (nw[2] << 16) | (nw[3] << 24);
+                inm = ~neg;
+                bandm = neg & ~negw;
+            }
+            // the counts of buffer b were flushed and cleared for tile it - 2
+            if (!ptx::mbar_wait(&S.fdone[b], (use & 1u) ^ 1u, a.st, 32)) break;
+            if (busy) {
+                int* racc = S.rowacc[b];
+                int* cacc = S.colacc[b];
+                const uint32_t row = w.x * 128u + q * 32u + lane;
                 const uint32_t col0 = w.y * 128u + cg * 32u;
                 if (__any_sync(FULL, bandm != 0)) {
                     unsigned long long slot = band_reserve(a.st, __popc(bandm));
@@ -307,28 +322,42 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 }
                 if (__any_sync(FULL, inm != 0)) {
                     if (!diag) {
-                        const uint32_t colbits = transpose32(inm, lane);
-                        const int cc = __popc(colbits);
+                        const int cc = __popc(transpose32(inm, lane));
                         if (cc) atomicAdd(&cacc[cg * 32u + lane], cc);
                     }
+                    const int rowcnt = __popc(inm);
                     if (rowcnt) atomicAdd(&racc[q * 32u + lane], rowcnt);
                 }
             }
             __syncwarp();
             if (lane == 0) ptx::mbar_arrive(&S.ebar[b]);
-            if (!ptx::mbar_wait(&S.ebar[b], use & 1u, a.st, 31)) break;
-            if (et < 128) {
-                const int r = racc[et];
-                if (r) atomicAdd(&a.counts[w.x * 128u + et], r);
-                racc[et] = 0;
-            } else if (et < 256) {
-                const int c = cacc[et - 128];
-                if (c) atomicAdd(&a.counts[w.y * 128u + et - 128], c);
-                cacc[et - 128] = 0;
-            }
             const float sn = tnx + tny;
             W = fmaf(fabsf(sn), 9.5367431640625e-07f, sn);
             w = wn;
+        }
+    } else {
+        // ------------------------------------------------ count flusher
+        // adds the per-tile row / column counts to global memory and clears
+        // them, off the epilogue warps' critical path
+        uint32_t it = 0;
+        for (uint64_t u = blockIdx.x; u < a.nwork; u += gridDim.x, ++it) {
+            const uint32_t b = it & 1u, use = it >> 1;
+            const uint2 w = __ldg(&a.work[u]);
+            if (!ptx::mbar_wait(&S.ebar[b], use & 1u, a.st, 40)) break;
+            int* racc = S.rowacc[b];
+            int* cacc = S.colacc[b];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const uint32_t r = lane + 32 * e;
+                const int rv = racc[r];
+                if (rv) atomicAdd(&a.counts[w.x * 128u + r], rv);
+                racc[r] = 0;
+                const int cv = cacc[r];
+                if (cv) atomicAdd(&a.counts[w.y * 128u + r], cv);
+                cacc[r] = 0;
+            }
+            __syncwarp();
+            if (lane == 0) ptx::mbar_arrive(&S.fdone[b]);
         }
     }
 
