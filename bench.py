@@ -38,7 +38,7 @@ sys.path.insert(0, ROOT)
 
 import numpy as np  # noqa: E402
 
-PROFILE_SUMMARY = os.path.join(ROOT, "profiles", "roofline_traffic.json")
+PROFILE_SUMMARY = os.path.join(ROOT, "profiles", "gram_kernel_traffic.json")
 
 
 def parse():
