@@ -99,6 +99,14 @@ def build(verbose: bool = False, probe: bool = True) -> str:
         if r.returncode != 0:
             raise RuntimeError(f"probe link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
         os.replace(tmp, PROBE_LIB)
+    cli_src = os.path.join(CSRC, "cli_main.cpp")
+    if os.path.exists(cli_src) and not _newer(CLI, [cli_src, LIB, *deps]):
+        cmd = ["g++", "-O2", "-std=c++17", "-I", INCLUDE, cli_src, "-o", CLI + ".tmp", "-L", PKG,
+               "-lejoin", "-Wl,-rpath," + PKG]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"CLI link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+        os.replace(CLI + ".tmp", CLI)
     if verbose:
         print("built", LIB)
     return LIB

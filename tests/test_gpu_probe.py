@@ -118,3 +118,57 @@ def test_probe_sw32_aug_tiles(probe, fmt):
     D = probe(Ap, Bp, 1, fmt, 2)
     ref = af[:, :16] @ bf[:, 16:32].T
     assert np.allclose(D, ref, rtol=1e-5, atol=1e-5)
+
+
+def e4m3_decode(b):
+    b = b.astype(np.int64)
+    s = np.where(b & 0x80, -1.0, 1.0)
+    e = (b >> 3) & 0xF
+    m = b & 0x7
+    val = np.where(e == 0, m / 8.0 * 2.0 ** -6, (1 + m / 8.0) * 2.0 ** (e - 7))
+    return s * val
+
+
+def random_e4m3(rng, shape, lo_exp=-6, hi_exp=6):
+    """Random finite, normal E4M3 codes with exponents in [lo_exp, hi_exp]
+    (hi_exp <= 7: exponent code 15 with mantissa 7 is NaN)."""
+    assert hi_exp <= 7
+    e = rng.integers(lo_exp + 7, hi_exp + 8, shape)
+    m = rng.integers(0, 8, shape)
+    s = rng.integers(0, 2, shape)
+    return ((s << 7) | (e << 3) | m).astype(np.uint8)
+
+
+@pytest.mark.parametrize("nslab", [1, 2])
+def test_probe_fp8_gram_tile(probe, nslab):
+    rng = np.random.default_rng(70 + nslab)
+    K = 128 * nslab
+    A = random_e4m3(rng, (128, K))
+    B = random_e4m3(rng, (128, K))
+    af, bf = e4m3_decode(A), e4m3_decode(B)
+    D = probe(A, B, nslab, 2, 0)
+    ref = af @ bf.T
+    scale = np.abs(af) @ np.abs(bf).T
+    rel = (np.abs(D - ref) / scale).max()
+    bound = (K + 16) * 2.0 ** -22
+    print(f"FP8: max accumulation error / sum|p| = {rel:.3e} (bound {bound:.3e})")
+    assert rel * 4 <= bound
+
+
+def test_probe_fp8_accumulation_adversarial(probe):
+    """One large product followed by many small ones of mixed sign: the FP8
+    kind keeps FP32-class accumulation precision (the screen's bound holds)."""
+    rng = np.random.default_rng(77)
+    K = 256
+    A = random_e4m3(rng, (128, K), -6, -3)
+    B = random_e4m3(rng, (128, K), -6, -3)
+    A[:, 0] = random_e4m3(rng, (128,), 6, 7)
+    B[:, 0] = random_e4m3(rng, (128,), 6, 7)
+    af, bf = e4m3_decode(A), e4m3_decode(B)
+    D = probe(A, B, 2, 2, 0)
+    ref = af @ bf.T
+    scale = np.abs(af) @ np.abs(bf).T
+    rel = (np.abs(D - ref) / scale).max()
+    bound = (K + 16) * 2.0 ** -22
+    print(f"FP8 adversarial: max error / sum|p| = {rel:.3e} (bound {bound:.3e})")
+    assert rel * 4 <= bound
