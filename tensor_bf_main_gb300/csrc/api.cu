@@ -347,6 +347,8 @@ static int prepare_learned(Join& J, const double* mu, uint64_t n_pad, Learned& L
 
 // Global power-of-two scale of the centred data for the 16-bit operands.
 static double screen_scale(Fmt f, double maxabs, uint32_t d) {
+    // BF16 / FP8: max |z| <= 1 (FP8 rows get their own scale on top);
+    // FP16: max |z|^2 <= 2^12 so that norms and margins stay in range
     if (!(maxabs > 0.0) || !isfinite(maxabs)) return 1.0;
     double target = (f == Fmt::FP16) ? 64.0 / sqrt((double)d) : 1.0;
     int e = (int)floor(log2(target / maxabs));
@@ -372,18 +374,19 @@ static int run_screen16(Join& J, Fmt fmt, bool split, Learned& L) {
     if (J.opt.proj_k) EJ_TRY(prepare_learned(J, mu.p, n_pad, L));
     tp.start(J.s);
     ScreenParams P;
+    const bool fp8 = (fmt == Fmt::E4M3);
     P.fmt = fmt;
     P.split = split ? 1 : 0;
     P.d = J.d;
-    P.dp = (uint32_t)round_up(J.d, 64);
+    P.dp = (uint32_t)round_up(J.d, fp8 ? 128 : 64);
     P.width = P.dp * (split ? 2 : 1);
     P.scale = screen_scale(fmt, maxabs, J.d);
     double Tlo, Thi;
     oracle_band(J.T, J.d, &Tlo, &Thi);
     const double s2 = P.scale * P.scale;
     // Every finite pair has s_q = |q_i - q_j|^2 <= 4 max|q|^2 (<= 2^14 for FP16
-    // by the choice of scale, <= 4d for BF16): capping T far above that keeps
-    // both tests exact while bounding the margins in the operand range.
+    // by the choice of scale, <= 4d for BF16 / FP8): capping T far above that
+    // keeps both tests exact while bounding the margins in the operand range.
     const double cap_t = (fmt == Fmt::FP16) ? 32768.0 : 1.152921504606846976e18;
     P.Tlo = std::min(Tlo * s2, cap_t);
     P.Thi = std::min(Thi * s2, cap_t);
@@ -395,15 +398,24 @@ static int run_screen16(Join& J, Fmt fmt, bool split, Learned& L) {
     P.absacc = (kprod + 16.0) * ldexp(1.0, -125);
     P.clamp_lo = (fmt == Fmt::FP16) ? -16384.0 : -kTwo100;
     DBuf<uint16_t> Q, Aug;
-    DBuf<float> beta, tmax, Xf, rad;
-    EJ_TRY(Q.alloc(n_pad * P.width, J.s, "packed operands"));
+    DBuf<uint8_t> Q8;
+    DBuf<float> beta, tmax, Xf, rad, sig, tsig;
+    if (fp8) EJ_TRY(Q8.alloc(n_pad * P.width, J.s, "packed FP8 operands"));
+    else EJ_TRY(Q.alloc(n_pad * P.width, J.s, "packed operands"));
     EJ_TRY(Aug.alloc(n_pad * 32, J.s, "aug operands"));
     EJ_TRY(beta.alloc(n_pad, J.s, "out margins"));
     EJ_TRY(tmax.alloc(n_pad / 128, J.s, "tile margins"));
     EJ_TRY(Xf.alloc(n_pad * J.d, J.s, "FP32 coordinates"));
     EJ_TRY(rad.alloc(n_pad, J.s, "FP32 radii"));
-    EJ_TRY(launch_pack16(J.X, J.n, n_pad, J.perm, bad.p, mu.p, P, Q.p, Aug.p, beta.p, Xf.p, rad.p,
-                         J.s));
+    if (fp8) {
+        EJ_TRY(sig.alloc(n_pad, J.s, "row scales"));
+        EJ_TRY(tsig.alloc(n_pad / 128, J.s, "tile scales"));
+        EJ_TRY(launch_pack8(J.X, J.n, n_pad, J.perm, bad.p, mu.p, P, Q8.p, Aug.p, beta.p, sig.p,
+                            Xf.p, rad.p, tsig.p, J.s));
+    } else {
+        EJ_TRY(launch_pack16(J.X, J.n, n_pad, J.perm, bad.p, mu.p, P, Q.p, Aug.p, beta.p, Xf.p,
+                             rad.p, J.s));
+    }
     EJ_TRY(launch_tile_max(beta.p, nullptr, n_pad, tmax.p, J.s));
     tp.stop(J.s);
     J.st->ms_prep = ms_center + tp.ms();
@@ -418,10 +430,12 @@ static int run_screen16(Join& J, Fmt fmt, bool split, Learned& L) {
     J.st->tile_pairs_total = nT * (nT + 1) / 2;
     J.st->tile_pairs_run = nwork;
     J.st->gram_flops = 2.0 * kprod * 128.0 * 128.0 * (double)nwork;
-    J.st->precision = fmt == Fmt::FP16 ? EJOIN_FP16 : (split ? EJOIN_BF16_SPLIT : EJOIN_BF16);
+    J.st->precision = fp8 ? EJOIN_FP8_E4M3
+                          : (fmt == Fmt::FP16 ? EJOIN_FP16 : (split ? EJOIN_BF16_SPLIT : EJOIN_BF16));
+    const void* Qp = fp8 ? (const void*)Q8.p : (const void*)Q.p;
     auto screen = [&](BandPair* band, uint64_t cap, DevStatus* st) {
-        return launch_gram16(Q.p, Aug.p, n_pad, P, work.p, nwork, tmax.p, J.counts, band, cap, st,
-                             J.sms, J.s);
+        return launch_gram16(Qp, Aug.p, n_pad, P, work.p, nwork, tmax.p, tsig.p, J.counts, band,
+                             cap, st, J.sms, J.s);
     };
     Recheck32 R;
     R.Xf = Xf.p;
@@ -506,8 +520,7 @@ static int self_join_impl(const double* points, uint64_t n, uint32_t d, double e
             case EJOIN_FP16: EJ_TRY(run_screen16(J, Fmt::FP16, false, learned)); break;
             case EJOIN_BF16: EJ_TRY(run_screen16(J, Fmt::BF16, false, learned)); break;
             case EJOIN_BF16_SPLIT: EJ_TRY(run_screen16(J, Fmt::BF16, true, learned)); break;
-            case EJOIN_FP8_E4M3:
-                return set_error(EJOIN_EUNSUPPORTED, "FP8 screen not available in this build");
+            case EJOIN_FP8_E4M3: EJ_TRY(run_screen16(J, Fmt::E4M3, false, learned)); break;
             default: return set_error(EJOIN_EINVAL, "unknown precision %d", prec);
         }
     }

@@ -230,9 +230,11 @@ int launch_dmma_join(const double* Y, uint64_t n_pad, uint32_t dp, const double*
                      DevStatus* st, cudaStream_t s);
 
 // k_umma.cu: tcgen05 Gram screen over a tile-pair work list (16-bit operands).
+// (FP8 operands: also the per-tile minimum row scale tsig.)
 int launch_gram16(const void* Q, const void* aug, uint64_t n_pad, const ScreenParams& P,
-                  const uint2* work, uint64_t nwork, const float* tmax, int32_t* counts,
-                  BandPair* band, uint64_t band_cap, DevStatus* st, int num_sms, cudaStream_t s);
+                  const uint2* work, uint64_t nwork, const float* tmax, const float* tsig,
+                  int32_t* counts, BandPair* band, uint64_t band_cap, DevStatus* st, int num_sms,
+                  cudaStream_t s);
 
 // k_misc.cu
 // Ordered list of the upper-triangle 128-row tile pairs (I <= J), grouped by
@@ -278,10 +280,12 @@ int launch_pack_dmma(const double* X, uint64_t n, uint64_t n_pad, const uint32_t
 int launch_pack16(const double* X, uint64_t n, uint64_t n_pad, const uint32_t* perm,
                   const uint8_t* bad, const double* mu, const ScreenParams& P, void* Q,
                   void* Aug, float* beta, float* Xf, float* rad, cudaStream_t s);
-// FP8 operand rows and per-row (sigma, alpha, beta, 0).
+// E4M3 operand rows with per-row power-of-two scales sigma, BF16 aug rows,
+// beta, sigma, FP32 coordinates / radii, and the per-tile minimum sigma.
 int launch_pack8(const double* X, uint64_t n, uint64_t n_pad, const uint32_t* perm,
                  const uint8_t* bad, const double* mu, const ScreenParams& P, uint8_t* Q,
-                 float4* meta, cudaStream_t s);
+                 void* Aug, float* beta, float* sig, float* Xf, float* rad, float* tsig,
+                 cudaStream_t s);
 // per 128-row tile: max of beta (16-bit) or of meta.z (FP8), as float
 int launch_tile_max(const float* beta, const float4* meta, uint64_t n_pad, float* tmax,
                     cudaStream_t s);

@@ -327,6 +327,170 @@ __global__ void __launch_bounds__(256) pack16_kernel(const double* __restrict__ 
     rad[p] = radius;
 }
 
+// ----------------------------------------------------------- FP8 pack --
+
+// E4M3 operands with a per-row power-of-two scale sigma_i (|z / sigma| <= 240,
+// below the format's 448 limit).  A warp packs 32 rows; per row the lanes keep
+// their FP32 coordinates zf in registers (d <= 1024), take the row maximum,
+// then quantise f = round_e4m3(zf / sigma) (division by a power of two is
+// exact), q = sigma f, residual zf - q exact in FP32.  Phase 2 (lane = row):
+// alpha in Gram units as for the 16-bit screen, stored for the BF16 aug MMA
+// as  A = [alpha/sigma (3 BF16 terms, last rounded up), 1/sigma x3],
+//     B = [-1/sigma x3, -alpha/sigma (3 terms)],
+// so that the accumulator, in units of F = f_i . f_j, holds
+// F - (alpha_i + alpha_j) / (sigma_i sigma_j).
+constexpr int PACK8_MAXV = 32;  // coordinates per lane: d <= 1024
+__global__ void __launch_bounds__(256) pack8_kernel(const double* __restrict__ X, uint64_t n,
+                                                    uint64_t n_pad,
+                                                    const uint32_t* __restrict__ perm,
+                                                    const uint8_t* __restrict__ bad,
+                                                    const double* __restrict__ mu, ScreenParams P,
+                                                    uint8_t* Q, uint16_t* Aug, float* beta,
+                                                    float* sig, float* Xf, float* rad) {
+    const uint64_t p0 = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / 32 * 32;
+    const uint32_t lane = threadIdx.x & 31;
+    if (p0 >= n_pad) return;
+    const float mnf = 0.015625f;  // E4M3 smallest normal 2^-6
+    float m_z2 = 0, m_e2 = 0, m_sig = 1.0f;
+    double m_nq = 0;
+    bool m_good = false;
+    for (uint32_t r = 0; r < 32; ++r) {
+        const uint64_t p = p0 + r;
+        const uint64_t src = p < n ? (perm ? perm[p] : p) : 0;
+        const bool good = p < n && !bad[src];
+        float zv[PACK8_MAXV];
+        float mx = 0.0f;
+#pragma unroll
+        for (int t = 0; t < PACK8_MAXV; ++t) {
+            const uint32_t k = lane + 32u * t;
+            float zf = 0.0f;
+            if (good && k < P.d) {
+                zf = (float)__dmul_rn(__dsub_rn(X[src * P.d + k], mu[k]), P.scale);
+                if (fabsf(zf) < 1.1754944e-38f) zf = 0.0f;
+            }
+            zv[t] = zf;
+            mx = fmaxf(mx, fabsf(zf));
+        }
+        for (int o = 16; o; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        // sigma = 2^ceil(log2(mx / 240)), 1 for an all-zero row
+        float sgm = 1.0f;
+        if (mx > 0.0f) {
+            int e;
+            frexpf(mx / 240.0f, &e);  // mx/240 in [2^(e-1), 2^e)
+            sgm = ldexpf(1.0f, e);
+        }
+        const float inv = 1.0f / sgm;  // exact (power of two)
+        float z2 = 0, e2 = 0;
+        double nq = 0;
+        uint8_t* row = Q + p * (uint64_t)P.width;
+#pragma unroll
+        for (int t = 0; t < PACK8_MAXV; ++t) {
+            const uint32_t k = lane + 32u * t;
+            if (k >= P.dp) break;
+            const float zf = zv[t];
+            const float f = round_fmt_f(zf * inv, 3, mnf);
+            const float q = f * sgm;        // exact
+            const float ef = zf - q;        // exact
+            const double qd = (double)q;
+            nq = __fma_rn(qd, qd, nq);
+            z2 = __fmaf_ru(zf, zf, z2);
+            e2 = __fmaf_ru(ef, ef, e2);
+            row[k] = (uint8_t)__nv_cvt_float_to_fp8(f, __NV_SATFINITE, __NV_E4M3);
+            if (k < P.d) Xf[p * P.d + k] = zf;
+        }
+        for (int o = 16; o; o >>= 1) {
+            nq += __shfl_xor_sync(0xffffffffu, nq, o);
+            z2 = __fadd_ru(z2, __shfl_xor_sync(0xffffffffu, z2, o));
+            e2 = __fadd_ru(e2, __shfl_xor_sync(0xffffffffu, e2, o));
+        }
+        if (lane == r) {
+            m_nq = nq;
+            m_z2 = z2;
+            m_e2 = e2;
+            m_sig = sgm;
+            m_good = good;
+        }
+    }
+    // ---- phase 2: row p0 + lane
+    const uint64_t p = p0 + lane;
+    const FmtInfo bf = fmt_info(Fmt::BF16);
+    double ah[3] = {0, 0, 0};
+    double b = 0.0, rsig = 1.0;
+    float radius = INFINITY;
+    if (m_good) {
+        const double gs = (P.d + 4) * kU;
+        const double nup = m_nq * (1 + gs), ndn = m_nq * (1 - gs);
+        const double a2u = nup;  // |(|q|)|^2 = |q|^2
+        const double zn = sqrt((double)m_z2) * (1 + 1e-7);
+        const double zerr = (5.9604645e-08 + 2.0 * kU) * zn * 1.0001 + 1.18e-38 * sqrt((double)P.d);
+        const double rho = (sqrt((double)m_e2) * (1 + 1e-7) + zerr) * (1 + 8 * kU);
+        radius = __double2float_ru(zerr);
+        double R = nup + P.cacc * a2u + P.absacc - 0.5 * P.Tlo + 2.0 * P.sTlo * rho;
+        R += 8 * kU * (nup + P.cacc * a2u + P.absacc + 0.5 * P.Tlo + 2.0 * P.sTlo * rho);
+        double at = R >= 0 ? R / (2.0 * (1.0 - P.cacc)) : R / (2.0 * (1.0 + P.cacc));
+        at += fabs(at) * 4 * kU;
+        rsig = 1.0 / (double)m_sig;  // exact
+        double as = fmax(at * rsig, -kTwo100);  // alpha / sigma, clamped upwards (safe)
+        ah[0] = round_fmt(as, bf);
+        const double r1 = __dsub_rn(as, ah[0]);
+        ah[1] = round_fmt(r1, bf);
+        const double r2 = __dsub_rn(r1, ah[1]);
+        ah[2] = round_fmt_up(r2, bf);
+        const double alpha = (ah[0] + ah[1] + ah[2]) * (double)m_sig;  // >= at
+        b = 0.5 * P.Thi + 2.0 * P.sThi * rho + 2.0 * rho * rho - ndn + 2.0 * alpha +
+            P.cacc * (a2u + 2.0 * fabs(alpha)) + P.absacc;
+        b += 8 * kU * (0.5 * P.Thi + 2.0 * P.sThi * rho + 2.0 * rho * rho + ndn + 2.0 * fabs(alpha) +
+                       P.cacc * (a2u + 2.0 * fabs(alpha)) + P.absacc);
+        b *= 0.5;
+    } else {
+        ah[0] = kTwo100;  // never in, never band
+        m_sig = 1.0f;
+        rsig = 1.0;
+    }
+    uint16_t vals[32];
+#pragma unroll
+    for (int e = 0; e < 32; ++e) vals[e] = 0;
+    const uint16_t rp = to_bits16(rsig, Fmt::BF16), rm = to_bits16(-rsig, Fmt::BF16);
+    vals[0] = to_bits16(ah[0], Fmt::BF16);
+    vals[1] = to_bits16(ah[1], Fmt::BF16);
+    vals[2] = to_bits16(ah[2], Fmt::BF16);
+    vals[3] = vals[4] = vals[5] = rp;
+    vals[16] = vals[17] = vals[18] = rm;
+    vals[19] = to_bits16(-ah[0], Fmt::BF16);
+    vals[20] = to_bits16(-ah[1], Fmt::BF16);
+    vals[21] = to_bits16(-ah[2], Fmt::BF16);
+    uint4* aug = reinterpret_cast<uint4*>(Aug + p * 32);
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+        uint4 w;
+        w.x = vals[8 * v + 0] | ((uint32_t)vals[8 * v + 1] << 16);
+        w.y = vals[8 * v + 2] | ((uint32_t)vals[8 * v + 3] << 16);
+        w.z = vals[8 * v + 4] | ((uint32_t)vals[8 * v + 5] << 16);
+        w.w = vals[8 * v + 6] | ((uint32_t)vals[8 * v + 7] << 16);
+        aug[v] = w;
+    }
+    beta[p] = m_good ? __double2float_ru(b) : 0.0f;
+    sig[p] = m_good ? m_sig : INFINITY;  // padding / bad rows do not lower a tile's minimum
+    rad[p] = radius;
+}
+
+// per 128-row tile: min sigma of its rows (1 for a tile without finite rows)
+__global__ void tile_min_sigma_kernel(const float* __restrict__ sig, uint64_t ntiles, float* tmin) {
+    const uint64_t t = blockIdx.x;
+    if (t >= ntiles) return;
+    float m = INFINITY;
+    for (int r = threadIdx.x; r < 128; r += blockDim.x) m = fminf(m, sig[t * 128 + r]);
+    for (int o = 16; o; o >>= 1) m = fminf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    __shared__ float sm[4];
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x / 32] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float r = sm[0];
+        for (int w = 1; w < (int)(blockDim.x / 32); ++w) r = fminf(r, sm[w]);
+        tmin[t] = isinf(r) ? 1.0f : r;
+    }
+}
+
 __global__ void tile_max_kernel(const float* __restrict__ beta, const float4* __restrict__ meta,
                                 uint64_t ntiles, float* tmax) {
     const uint64_t t = blockIdx.x;
@@ -405,6 +569,22 @@ int launch_pack16(const double* X, uint64_t n, uint64_t n_pad, const uint32_t* p
                                                                   beta, Xf, rad);
     else
         return set_error(EJOIN_EINTERNAL, "pack16: bad format");
+    EJ_CUDA(cudaGetLastError());
+    note_launch();
+    return EJOIN_OK;
+}
+
+int launch_pack8(const double* X, uint64_t n, uint64_t n_pad, const uint32_t* perm,
+                 const uint8_t* bad, const double* mu, const ScreenParams& P, uint8_t* Q,
+                 void* Aug, float* beta, float* sig, float* Xf, float* rad, float* tsig,
+                 cudaStream_t s) {
+    if (n_pad % 128) return set_error(EJOIN_EINTERNAL, "pack8: rows not padded");
+    if (P.d > 32u * PACK8_MAXV) return set_error(EJOIN_EUNSUPPORTED, "FP8 screen supports d <= %d", 32 * PACK8_MAXV);
+    pack8_kernel<<<(unsigned)((n_pad + 255) / 256), 256, 0, s>>>(X, n, n_pad, perm, bad, mu, P, Q,
+                                                                 (uint16_t*)Aug, beta, sig, Xf, rad);
+    EJ_CUDA(cudaGetLastError());
+    note_launch();
+    tile_min_sigma_kernel<<<(unsigned)(n_pad / 128), 128, 0, s>>>(sig, n_pad / 128, tsig);
     EJ_CUDA(cudaGetLastError());
     note_launch();
     return EJOIN_OK;

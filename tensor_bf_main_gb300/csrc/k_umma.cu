@@ -52,14 +52,26 @@ struct GramArgs {
     const uint2* work;
     uint64_t nwork;
     const float* tmax;
+    const float* tsig;  // FP8: per-tile minimum row scale (null for 16-bit operands)
     int32_t* counts;
     BandPair* band;
     uint64_t band_cap;
     DevStatus* st;
     uint32_t nhi;    // 64-element data slabs per part
     uint32_t split;  // hi + lo
-    uint32_t fmt;    // 0 = FP16, 1 = BF16 (instruction-descriptor operand format)
+    uint32_t fmt;    // 16-bit operands: 0 = FP16, 1 = BF16 (instruction-descriptor format)
 };
+
+// Band width of tile pair (I, J): beta_i + beta_j <= W (Gram units; FP8
+// operands: divided by sigma_I sigma_J, the accumulator's unit).  The sum is
+// rounded up by the 2^-20 relative margin; division by the power-of-two
+// scales is exact.
+__device__ __forceinline__ float band_width(const GramArgs& a, uint2 w) {
+    const float s = __ldg(&a.tmax[w.x]) + __ldg(&a.tmax[w.y]);
+    float W = fmaf(fabsf(s), 9.5367431640625e-07f, s);
+    if (a.tsig) W = W / (__ldg(&a.tsig[w.x]) * __ldg(&a.tsig[w.y]));
+    return W;
+}
 
 struct Ctl {
     uint64_t full[NST], empty[NST];
@@ -90,11 +102,17 @@ __device__ __forceinline__ uint32_t transpose32(uint32_t x, uint32_t lane) {
 
 // Element offset of K-slab `step` of a tile: [hi0, lo0, hi1, lo1, ...] with the
 // split, [hi0, hi1, ...] without.
+template <int OPK>
 __device__ __forceinline__ uint32_t slab_x(uint32_t step, uint32_t nhi, uint32_t split) {
-    if (split) return (step & 1) ? 64 * nhi + 64 * (step >> 1) : 64 * (step >> 1);
-    return 64 * step;
+    constexpr uint32_t E = OPK ? 128u : 64u;  // elements per 128-byte slab row
+    if (split) return (step & 1) ? E * nhi + E * (step >> 1) : E * (step >> 1);
+    return E * step;
 }
 
+// OPK 0: 16-bit operands, data MMAs kind::f16; OPK 1: E4M3 operands, data
+// MMAs kind::f8f6f4 (K = 32 per instruction, same 32-byte k-steps), the aug
+// MMA stays kind::f16 in BF16 and accumulates into the same tensor memory.
+template <int OPK>
 __global__ void __launch_bounds__(NTHREADS, 1)
     gram_kernel(const __grid_constant__ CUtensorMap tq, const __grid_constant__ CUtensorMap taug,
                 const GramArgs a) {
@@ -147,7 +165,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                         break;
                     }
                     uint8_t* sa = stages + (size_t)st * STAGE_BYTES;
-                    const int32_t x = (int32_t)slab_x(step, a.nhi, a.split);
+                    const int32_t x = (int32_t)slab_x<OPK>(step, a.nhi, a.split);
                     ptx::mbar_arrive_expect_tx(&S.full[st], step == 0 ? FIRST_TX : DATA_TX);
                     ptx::tma_load_2d(sa, &tq, x, (int32_t)(w.x * 128u), &S.full[st]);
                     ptx::tma_load_2d(sa + SLAB_BYTES, &tq, x, (int32_t)(w.y * 128u), &S.full[st]);
@@ -175,7 +193,14 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     } else if (warp == 1) {
         // ------------------------------------------------ MMA issuer
         if (lane == 0) {
-            const uint32_t idesc = ptx::idesc_f32acc(a.fmt, a.fmt, 128, 128);
+            const uint32_t idesc =
+                OPK ? ptx::idesc_f32acc(0, 0, 128, 128) : ptx::idesc_f32acc(a.fmt, a.fmt, 128, 128);
+            const uint32_t idesc_aug =
+                OPK ? ptx::idesc_f32acc(1, 1, 128, 128) : idesc;
+            auto mma = [&](uint32_t d, uint64_t ad, uint64_t bd, uint32_t acc_) {
+                if (OPK) ptx::mma_f8(d, ad, bd, idesc, acc_);
+                else ptx::mma_f16(d, ad, bd, idesc, acc_);
+            };
             uint32_t st = 0, ph = 0, it = 0;
             bool ok = true;
             auto take = [&](uint32_t& s_out) -> bool {
@@ -206,7 +231,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                         const uint64_t aa = ptx::sdesc_sw32(ptx::smem_u32(st_hi + 2 * SLAB_BYTES));
                         const uint64_t ba =
                             ptx::sdesc_sw32(ptx::smem_u32(st_hi + 2 * SLAB_BYTES + AUG_BYTES));
-                        ptx::mma_f16(d_tmem, aa, ba, idesc, 0);
+                        ptx::mma_f16(d_tmem, aa, ba, idesc_aug, 0);
                         acc = 1;
                     }
                     if (a.split) {
@@ -215,16 +240,15 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                         const uint64_t bl = ptx::sdesc_sw128(ptx::smem_u32(st_lo + SLAB_BYTES));
 #pragma unroll
                         for (uint32_t kk = 0; kk < 4; ++kk) {
-                            ptx::mma_f16(d_tmem, ah + 2 * kk, bh + 2 * kk, idesc, acc);
-                            ptx::mma_f16(d_tmem, ah + 2 * kk, bl + 2 * kk, idesc, 1);
-                            ptx::mma_f16(d_tmem, al + 2 * kk, bh + 2 * kk, idesc, 1);
+                            mma(d_tmem, ah + 2 * kk, bh + 2 * kk, acc);
+                            mma(d_tmem, ah + 2 * kk, bl + 2 * kk, 1);
+                            mma(d_tmem, al + 2 * kk, bh + 2 * kk, 1);
                         }
                         ptx::mma_commit(&S.empty[s_hi]);
                         ptx::mma_commit(&S.empty[s_lo]);
                     } else {
 #pragma unroll
-                        for (uint32_t kk = 0; kk < 4; ++kk)
-                            ptx::mma_f16(d_tmem, ah + 2 * kk, bh + 2 * kk, idesc, acc);
+                        for (uint32_t kk = 0; kk < 4; ++kk) mma(d_tmem, ah + 2 * kk, bh + 2 * kk, acc);
                         ptx::mma_commit(&S.empty[s_hi]);
                     }
                 }
@@ -245,11 +269,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         // the next tile's (I, J) and margins are loaded one tile ahead, so
         // their latency hides behind the current tile
         uint2 w = blockIdx.x < a.nwork ? __ldg(&a.work[blockIdx.x]) : make_uint2(0, 0);
-        float W = 0.0f;
-        if (blockIdx.x < a.nwork) {
-            const float s0 = __ldg(&a.tmax[w.x]) + __ldg(&a.tmax[w.y]);
-            W = fmaf(fabsf(s0), 9.5367431640625e-07f, s0);  // s + |s| 2^-20 >= beta_i + beta_j
-        }
+        float W = blockIdx.x < a.nwork ? band_width(a, w) : 0.0f;
         for (uint64_t u = blockIdx.x; u < a.nwork; u += gridDim.x, ++it) {
             const uint32_t b = it & 1u, use = it >> 1;
             const bool has_next = u + gridDim.x < a.nwork;
@@ -260,11 +280,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             ptx::tc_fence_after();
             uint32_t v[32];
             ptx::tmem_ld_32x32b_x32(tmem + ((q * 32u) << 16) + b * 128u + cg * 32u, v);
-            float tnx = 0.0f, tny = 0.0f;
-            if (has_next) {
-                tnx = __ldg(&a.tmax[wn.x]);
-                tny = __ldg(&a.tmax[wn.y]);
-            }
+            const float Wn = has_next ? band_width(a, wn) : 0.0f;
             ptx::tmem_ld_wait();
             ptx::tc_fence_before();
             __syncwarp();
@@ -331,8 +347,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             }
             __syncwarp();
             if (lane == 0) ptx::mbar_arrive(&S.ebar[b]);
-            const float sn = tnx + tny;
-            W = fmaf(fabsf(sn), 9.5367431640625e-07f, sn);
+            W = Wn;
             w = wn;
         }
     } else {
@@ -372,31 +387,37 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 }  // namespace
 
 int launch_gram16(const void* Q, const void* aug, uint64_t n_pad, const ScreenParams& P,
-                  const uint2* work, uint64_t nwork, const float* tmax, int32_t* counts,
-                  BandPair* band, uint64_t band_cap, DevStatus* st, int num_sms, cudaStream_t s) {
+                  const uint2* work, uint64_t nwork, const float* tmax, const float* tsig,
+                  int32_t* counts, BandPair* band, uint64_t band_cap, DevStatus* st, int num_sms,
+                  cudaStream_t s) {
     if (nwork == 0) return EJOIN_OK;
-    if (n_pad % 128 || P.dp % 64) return set_error(EJOIN_EINTERNAL, "gram16: bad padding");
+    const bool fp8 = P.fmt == Fmt::E4M3;
+    if (n_pad % 128 || P.dp % (fp8 ? 128 : 64)) return set_error(EJOIN_EINTERNAL, "gram: bad padding");
     if (n_pad > 0x7fffff80ull) return set_error(EJOIN_EUNSUPPORTED, "gram16: too many rows");
     CUtensorMap map, amap;
-    const CUtensorMapDataType dt =
-        P.fmt == Fmt::BF16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16;
-    EJ_TRY(make_tmap_2d(&map, Q, dt, 2, P.width, n_pad, 64, 128));
-    EJ_TRY(make_tmap_2d(&amap, aug, dt, 2, 32, n_pad, 16, 128));
+    const CUtensorMapDataType adt =
+        P.fmt == Fmt::FP16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
+    if (fp8)
+        EJ_TRY(make_tmap_2d(&map, Q, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, P.width, n_pad, 128, 128));
+    else
+        EJ_TRY(make_tmap_2d(&map, Q, adt, 2, P.width, n_pad, 64, 128));
+    EJ_TRY(make_tmap_2d(&amap, aug, adt, 2, 32, n_pad, 16, 128));
     GramArgs a;
     a.work = work;
     a.nwork = nwork;
     a.tmax = tmax;
+    a.tsig = fp8 ? tsig : nullptr;
     a.counts = counts;
     a.band = band;
     a.band_cap = band_cap;
     a.st = st;
-    a.nhi = P.dp / 64;
+    a.nhi = P.dp / (fp8 ? 128 : 64);
     a.split = P.split ? 1u : 0u;
     a.fmt = P.fmt == Fmt::BF16 ? 1u : 0u;
-    EJ_CUDA(cudaFuncSetAttribute(gram_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)SMEM_BYTES));
+    auto kern = fp8 ? gram_kernel<1> : gram_kernel<0>;
+    EJ_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES));
     const uint64_t grid = nwork < (uint64_t)num_sms ? nwork : (uint64_t)num_sms;
-    gram_kernel<<<(unsigned)grid, NTHREADS, SMEM_BYTES, s>>>(map, amap, a);
+    kern<<<(unsigned)grid, NTHREADS, SMEM_BYTES, s>>>(map, amap, a);
     EJ_CUDA(cudaGetLastError());
     note_launch();
     return EJOIN_OK;

@@ -10,7 +10,7 @@ from conftest import GOLDEN
 
 pytestmark = pytest.mark.gpu
 
-MODES = ["fp64_direct", "fp64_dmma", "bf16", "bf16_split", "fp16"]
+MODES = ["fp64_direct", "fp64_dmma", "bf16", "bf16_split", "fp16", "fp8_e4m3"]
 
 
 def load_f64(name, d):
@@ -143,3 +143,22 @@ def test_query_counts(ej, oracle_mod):
     eps = eps_for_mean(x, 30, rng)
     rows = rng.choice(3000, 100, replace=False)
     assert np.array_equal(ej.query_counts(x, eps, rows), oracle_mod.query_counts(x, eps, rows))
+
+
+def test_cli_reference_argv_and_csv(ej, tmp_path):
+    """ejoin_main takes the reference's argv (file, eps, searchMode, device)
+    and appends the reference's CSV result line (main.cu:115-127)."""
+    import subprocess
+    x = load_f64("test128.f64", 18)
+    data = tmp_path / "test128.txt"
+    with open(data, "w") as f:
+        for r in x:
+            f.write(", ".join(f"{v:.6f}" for v in r) + " \n")
+    exe = os.path.join(os.path.dirname(ej.LIB_PATH), "ejoin_main")
+    for mode, eps, total in ((4, 0.1, 11100), (1, 0.05, 828), (5, 0.2, 16384)):
+        out = subprocess.run([exe, str(data), str(eps), str(mode), "0"], cwd=tmp_path,
+                             capture_output=True, text=True, check=True).stdout
+        assert f"Total result set size: {total}" in out
+    lines = open(tmp_path / "tensor_brute-force.txt").read().splitlines()
+    assert lines[0].startswith("Dataset, epsilon, searchMode, executionTime, totalNeighbors")
+    assert len(lines) == 4 and lines[1].split(", ")[4] == "11100"
