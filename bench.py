@@ -52,6 +52,7 @@ def parse():
     p.add_argument("--proj-k", type=int, default=-1, help="-1: config default")
     p.add_argument("--n", type=int, default=0, help="override N (smaller runs)")
     p.add_argument("--eps", type=float, default=0.0)
+    p.add_argument("--eps-index", type=int, default=0, help="c3: which of its three radii")
     p.add_argument("--cpu-seconds", type=float, default=12.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-fp64", action="store_true")
@@ -73,7 +74,7 @@ def workload(args):
     cfg = datagen.CONFIGS[args.config]
     n = args.n or cfg["n"]
     x = datagen.generate(args.config, n=n)
-    eps = args.eps or datagen.frozen_eps(args.config, x)
+    eps = args.eps or datagen.frozen_eps(args.config, x, args.eps_index)
     return x, float(eps), cfg
 
 

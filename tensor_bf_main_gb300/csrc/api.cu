@@ -451,9 +451,11 @@ static int run_screen16(Join& J, Fmt fmt, bool split, Learned& L) {
     return screen_and_recheck(J, cap0, screen, recheck, n_pad, tg, tr);
 }
 
+// AUTO: the hi+lo split narrows the band while the quantisation residual
+// dominates the bound (small d); for large d the FP32 accumulation term
+// (proportional to K) dominates and the split's 3x MMA work buys little.
 static int resolve_precision(int p, uint32_t d) {
-    if (p == EJOIN_AUTO) return EJOIN_BF16_SPLIT;
-    (void)d;
+    if (p == EJOIN_AUTO) return d <= 256 ? EJOIN_BF16_SPLIT : EJOIN_BF16;
     return p;
 }
 

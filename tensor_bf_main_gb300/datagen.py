@@ -42,11 +42,15 @@ CONFIGS = {
 EPS = {
     "c1": 3.9568644945066116,
     "c2": 0.6694213287635902,
-    "c3": None,
+    "c3": [0.9181160375533391, 0.9782017823444267, 1.0549718481886086],
     "c4": 0.09982793683043545,
     "c5": float(np.sqrt(0.4)),
 }
-C5_SIGMA = None
+# c5: within-cluster cosines concentrate sharply in 1024 dimensions; this
+# spread puts ~2% of a 1000-point cluster above cosine 0.8 (mean ~20
+# neighbours), found by bisection on simulated clusters (the transition from
+# ~1 to ~1000 neighbours spans sigma 0.0165 .. 0.0167).
+C5_SIGMA = 0.016573473373427988
 
 SEED = 20251203
 
@@ -154,19 +158,22 @@ def calibrate_eps(x, target: float, nq: int = 256, seed: int = SEED) -> float:
         kkeep = min(x.shape[0], kkeep * 4)
 
 
-def frozen_eps(name: str, x) -> float:
-    """The frozen radius of config `name` for the full-size workload; for a
-    reduced N the radius is recalibrated on the given points."""
+def frozen_eps(name: str, x, index: int = 0) -> float:
+    """The frozen radius of config `name` for the full-size workload (c3: the
+    index-th of its three target means); for a reduced N the radius is
+    recalibrated on the given points."""
     cfg = CONFIGS[name]
     e = EPS.get(name)
     t = cfg["target"]
     if isinstance(e, list):
-        e = e[0]
+        e = e[index]
+    if isinstance(t, tuple):
+        t = t[index]
     if e is not None and x.shape[0] == cfg["n"]:
         return float(e)
     if name == "c5":
         return float(np.sqrt(0.4))
-    return calibrate_eps(x, t[0] if isinstance(t, tuple) else t)
+    return calibrate_eps(x, t)
 
 
 def mean_count(x, eps: float, nq: int = 256, seed: int = SEED) -> float:
