@@ -261,15 +261,24 @@ __host__ inline size_t train_smem_bytes(uint32_t k, uint32_t d) {
     return (size_t)(k * d + tp * (d + 1) + tp * k) * sizeof(float);
 }
 
-// Forward + hinge loss + backward for M pairs; G += dL/dP (atomics),
-// loss += sum of hinge terms / M.  A tile of TP pairs is staged once in
+// Gradient and loss are accumulated in 64-bit fixed point (2^-40 units)
+// with integer atomics: integer addition is associative, so the result does
+// not depend on the order in which blocks finish (bit-reproducible training).
+constexpr double kFix = 1099511627776.0;  // 2^40
+__device__ __forceinline__ void fix_add(unsigned long long* dst, float v) {
+    atomicAdd(dst, (unsigned long long)__double2ll_rn((double)v * kFix));
+}
+
+// Forward + hinge loss + backward for M pairs; G += dL/dP, loss += sum of
+// hinge terms / M (fixed-point accumulators).  A tile of TP pairs is staged once in
 // shared memory (row pitch d + 1: conflict-free) and serves the forward pass
 // (thread per pair) and the backward pass (thread per element of G).
 template <int K>
 __global__ void __launch_bounds__(TRAIN_THREADS) train_step_kernel(const float* __restrict__ P,
                                                                    uint32_t k, uint32_t d,
                                                                    PairBatch pb, uint64_t M,
-                                                                   float* G, float* loss) {
+                                                                   unsigned long long* G,
+                                                                   unsigned long long* loss) {
     extern __shared__ float sm[];
     const uint32_t TP = train_tile_pairs(d);
     const uint32_t pitch = d + 1;
@@ -317,27 +326,27 @@ __global__ void __launch_bounds__(TRAIN_THREADS) train_step_kernel(const float* 
             const uint32_t a = el / d, c = el % d;
             float acc = 0.0f;
             for (uint32_t p = 0; p < np; ++p) acc = fmaf(sC[p * k + a], sV[p * pitch + c], acc);
-            if (acc != 0.0f) atomicAdd(&G[el], acc);
+            if (acc != 0.0f) fix_add(&G[el], acc);
         }
     }
     for (int o = 16; o; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
-    if ((threadIdx.x & 31) == 0 && lsum != 0.0f) atomicAdd(loss, lsum * invM);
+    if ((threadIdx.x & 31) == 0 && lsum != 0.0f) fix_add(loss, lsum * invM);
 }
 
 // One Adam step on P from G (G is cleared for the next step), then the
 // power-iteration renormalisation P <- P / max(1, 1.02 s): s is the Rayleigh
 // quotient estimate of ||P||_2 from (P P^T)^32 (five normalised squarings, so
 // it converges when the leading eigenvalues are close).  One block; k <= 16.
-__global__ void adam_renorm_kernel(float* P, float* G, float* m1, float* m2, uint32_t k,
-                                   uint32_t d, float lr, float b1, float b2, float c1, float c2,
-                                   int renorm, float* sigma_out) {
+__global__ void adam_renorm_kernel(float* P, unsigned long long* G, float* m1, float* m2,
+                                   uint32_t k, uint32_t d, float lr, float b1, float b2, float c1,
+                                   float c2, int renorm, float* sigma_out) {
     __shared__ float M[16 * 16], A[16 * 16], B[16 * 16];
     __shared__ float v[16], w[16];
     __shared__ float lam, amax;
     const uint32_t nel = k * d;
     for (uint32_t e = threadIdx.x; e < nel; e += blockDim.x) {
-        const float g = G[e];
-        G[e] = 0.0f;
+        const float g = (float)((double)(long long)G[e] / kFix);
+        G[e] = 0ull;
         const float a = b1 * m1[e] + (1.0f - b1) * g;
         const float b = b2 * m2[e] + (1.0f - b2) * g * g;
         m1[e] = a;
@@ -492,7 +501,8 @@ int train_projection_dev(const double* X, const double* mu, uint64_t n, uint32_t
     double s0 = 0;
     EJ_TRY(cert_spectral_norm(P0.data(), k, d, &s0));
     for (auto& v : P0) v = (float)(v / (s0 * 1.0001));
-    DBuf<float> P, G, m1, m2, loss;
+    DBuf<float> P, m1, m2;
+    DBuf<unsigned long long> G, loss;
     EJ_TRY(P.alloc(nel, s, "projection"));
     EJ_TRY(G.alloc(nel, s, "gradient"));
     EJ_TRY(m1.alloc(nel, s, "adam m"));
@@ -542,10 +552,13 @@ int train_projection_dev(const double* X, const double* mu, uint64_t n, uint32_t
         }
     }
     out.P.resize(nel);
-    std::vector<float> L(steps ? steps : 1);
+    std::vector<unsigned long long> Lf(steps ? steps : 1);
     EJ_CUDA(cudaMemcpyAsync(out.P.data(), P.p, nel * sizeof(float), cudaMemcpyDeviceToHost, s));
-    EJ_CUDA(cudaMemcpyAsync(L.data(), loss.p, L.size() * sizeof(float), cudaMemcpyDeviceToHost, s));
+    EJ_CUDA(cudaMemcpyAsync(Lf.data(), loss.p, Lf.size() * sizeof(unsigned long long),
+                            cudaMemcpyDeviceToHost, s));
     EJ_CUDA(cudaStreamSynchronize(s));
+    std::vector<double> L(Lf.size());
+    for (size_t i = 0; i < Lf.size(); ++i) L[i] = (double)(long long)Lf[i] / 1099511627776.0;
     // first / last loss averaged over a few steps (minibatch noise)
     const size_t w = std::min<size_t>(8, L.size());
     double a = 0, b = 0;
@@ -571,7 +584,8 @@ extern "C" int ejoin_testing_projection_grad(const float* V, const float* tgt, u
     if (!V || !tgt || !P || !G_out || !loss_out || k == 0 || k > 16 || d == 0 || M == 0)
         return set_error(EJOIN_EINVAL, "bad arguments");
     cudaStream_t s = cudaStreamPerThread;
-    DBuf<float> dV, dT, dP, dG, dL;
+    DBuf<float> dV, dT, dP;
+    DBuf<unsigned long long> dG, dL;
     EJ_TRY(dV.alloc(M * d, s, "V"));
     EJ_TRY(dT.alloc(M, s, "targets"));
     EJ_TRY(dP.alloc((size_t)k * d, s, "P"));
@@ -588,9 +602,14 @@ extern "C" int ejoin_testing_projection_grad(const float* V, const float* tgt, u
     PairBatch pb{dV.p, dT.p};
     fn<<<64, TRAIN_THREADS, shm, s>>>(dP.p, k, d, pb, M, dG.p, dL.p);
     EJ_CUDA(cudaGetLastError());
-    EJ_CUDA(cudaMemcpyAsync(G_out, dG.p, (size_t)k * d * sizeof(float), cudaMemcpyDeviceToHost, s));
-    EJ_CUDA(cudaMemcpyAsync(loss_out, dL.p, sizeof(float), cudaMemcpyDeviceToHost, s));
+    std::vector<unsigned long long> g((size_t)k * d);
+    unsigned long long l = 0;
+    EJ_CUDA(cudaMemcpyAsync(g.data(), dG.p, g.size() * sizeof(unsigned long long),
+                            cudaMemcpyDeviceToHost, s));
+    EJ_CUDA(cudaMemcpyAsync(&l, dL.p, sizeof l, cudaMemcpyDeviceToHost, s));
     EJ_CUDA(cudaStreamSynchronize(s));
+    for (size_t e = 0; e < g.size(); ++e) G_out[e] = (float)((double)(long long)g[e] / kFix);
+    *loss_out = (float)((double)(long long)l / kFix);
     return EJOIN_OK;
 }
 
@@ -600,15 +619,18 @@ extern "C" int ejoin_testing_renormalise(float* P, uint32_t k, uint32_t d, float
     if (!P || k == 0 || k > 16 || d == 0) return set_error(EJOIN_EINVAL, "bad arguments");
     cudaStream_t s = cudaStreamPerThread;
     DBuf<float> dP, dZ, dS;
+    DBuf<unsigned long long> dG;
     const size_t nel = (size_t)k * d;
     EJ_TRY(dP.alloc(nel, s, "P"));
-    EJ_TRY(dZ.alloc(3 * nel, s, "zero state"));
+    EJ_TRY(dZ.alloc(2 * nel, s, "zero state"));
+    EJ_TRY(dG.alloc(nel, s, "zero gradient"));
     EJ_TRY(dS.alloc(1, s, "sigma"));
     EJ_TRY(dZ.zero(s));
+    EJ_TRY(dG.zero(s));
     EJ_CUDA(cudaMemcpyAsync(dP.p, P, nel * sizeof(float), cudaMemcpyHostToDevice, s));
     // zero gradient and learning rate: the Adam part leaves P unchanged
-    adam_renorm_kernel<<<1, 256, 0, s>>>(dP.p, dZ.p, dZ.p + nel, dZ.p + 2 * nel, k, d, 0.0f, 0.9f,
-                                         0.999f, 1.0f, 1.0f, 1, dS.p);
+    adam_renorm_kernel<<<1, 256, 0, s>>>(dP.p, dG.p, dZ.p, dZ.p + nel, k, d, 0.0f, 0.9f, 0.999f,
+                                         1.0f, 1.0f, 1, dS.p);
     EJ_CUDA(cudaGetLastError());
     EJ_CUDA(cudaMemcpyAsync(P, dP.p, nel * sizeof(float), cudaMemcpyDeviceToHost, s));
     if (sigma_est_out)

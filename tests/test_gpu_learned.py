@@ -113,3 +113,16 @@ def test_training_gains_over_untrained_projection(ej):
           f"ms: none {s0['ms_total']:.1f} untrained {sr['ms_total']:.1f} trained {st['ms_total']:.1f} "
           f"(train {st['ms_train']:.1f})")
     assert frac(st) < frac(sr) < frac(s0) == 1.0
+
+
+def test_learned_pipeline_is_reproducible(ej):
+    """Fixed-point gradient accumulation makes training bit-reproducible: two
+    runs prune exactly the same tile pairs and queue the same band."""
+    x = latent_data(60000, 6)
+    eps = eps_for_mean(x, 30)
+    a, ta, sa = ej.self_join(x, eps, precision="bf16_split", proj_k=8, train_steps=80)
+    b, tb, sb = ej.self_join(x, eps, precision="bf16_split", proj_k=8, train_steps=80)
+    assert ta == tb and np.array_equal(a, b)
+    assert sa["tile_pairs_run"] == sb["tile_pairs_run"]
+    assert sa["band_pairs"] == sb["band_pairs"]
+    assert sa["sigma_cert"] == sb["sigma_cert"]
