@@ -447,7 +447,9 @@ static int run_screen16(Join& J, Fmt fmt, bool split, Learned& L) {
     auto recheck = [&](const BandPair* band, uint64_t nb, DevStatus* st) {
         return launch_band_recheck2(J.X, J.n, J.d, J.perm, J.T, R, band, nb, J.counts, st, J.s);
     };
-    const uint64_t cap0 = std::max<uint64_t>(1u << 22, 32 * J.n);
+    // generous first queue (8 B per entry, capped at a quarter of free memory
+    // by band_budget): an overflow re-runs the whole screen
+    const uint64_t cap0 = std::max<uint64_t>(1u << 22, 512 * J.n);
     return screen_and_recheck(J, cap0, screen, recheck, n_pad, tg, tr);
 }
 

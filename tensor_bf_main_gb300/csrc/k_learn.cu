@@ -258,7 +258,7 @@ __host__ __device__ inline uint32_t train_tile_pairs(uint32_t d) {
 }
 __host__ inline size_t train_smem_bytes(uint32_t k, uint32_t d) {
     const uint32_t tp = train_tile_pairs(d);
-    return (size_t)(k * d + tp * (d + 1) + tp * k) * sizeof(float);
+    return (size_t)(2 * k * d + tp * (d + 1) + tp * k) * sizeof(float);
 }
 
 // Gradient and loss are accumulated in 64-bit fixed point (2^-40 units)
@@ -283,9 +283,13 @@ __global__ void __launch_bounds__(TRAIN_THREADS) train_step_kernel(const float* 
     const uint32_t TP = train_tile_pairs(d);
     const uint32_t pitch = d + 1;
     float* sP = sm;                // k * d
-    float* sV = sP + k * d;        // TP * pitch
+    float* sG = sP + k * d;        // k * d: this block's gradient partial
+    float* sV = sG + k * d;        // TP * pitch
     float* sC = sV + TP * pitch;   // TP * k coefficients
-    for (uint32_t e = threadIdx.x; e < k * d; e += blockDim.x) sP[e] = P[e];
+    for (uint32_t e = threadIdx.x; e < k * d; e += blockDim.x) {
+        sP[e] = P[e];
+        sG[e] = 0.0f;
+    }
     const float invM = 1.0f / (float)M;
     float lsum = 0.0f;
     for (uint64_t base = blockIdx.x * (uint64_t)TP; base < M; base += (uint64_t)gridDim.x * TP) {
@@ -321,14 +325,17 @@ __global__ void __launch_bounds__(TRAIN_THREADS) train_step_kernel(const float* 
                 if (a < (int)k) sC[p * k + a] = coef * y[a];
         }
         __syncthreads();
-        // G[a][c] += sum_p sC[p][a] * V[p][c]
+        // G[a][c] += sum_p sC[p][a] * V[p][c]  (thread-owned elements: no atomics)
         for (uint32_t el = threadIdx.x; el < k * d; el += blockDim.x) {
             const uint32_t a = el / d, c = el % d;
             float acc = 0.0f;
             for (uint32_t p = 0; p < np; ++p) acc = fmaf(sC[p * k + a], sV[p * pitch + c], acc);
-            if (acc != 0.0f) fix_add(&G[el], acc);
+            sG[el] += acc;
         }
     }
+    __syncthreads();
+    for (uint32_t el = threadIdx.x; el < k * d; el += blockDim.x)
+        if (sG[el] != 0.0f) fix_add(&G[el], sG[el]);
     for (int o = 16; o; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
     if ((threadIdx.x & 31) == 0 && lsum != 0.0f) fix_add(loss, lsum * invM);
 }
@@ -526,7 +533,8 @@ int train_projection_dev(const double* X, const double* mu, uint64_t n, uint32_t
     auto step_fn = k <= 8 ? train_step_kernel<8> : train_step_kernel<16>;
     EJ_CUDA(cudaFuncSetAttribute(step_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
     const uint32_t tp = train_tile_pairs(d);
-    const unsigned grid = (unsigned)std::min<uint64_t>((B + tp - 1) / tp, 1024);
+    // a few blocks per SM, each accumulating its partial gradient in shared memory
+    const unsigned grid = (unsigned)std::min<uint64_t>((B + tp - 1) / tp, 304);
     uint32_t t_step = 0;
     uint64_t cursor = 0;
     for (uint32_t r = 0; r < rounds; ++r) {
