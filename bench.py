@@ -48,7 +48,7 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--config", default="c4")
-    p.add_argument("--precision", default="auto")
+    p.add_argument("--precision", default="config", help="'config': the config's own arithmetic")
     p.add_argument("--proj-k", type=int, default=-1, help="-1: config default")
     p.add_argument("--n", type=int, default=0, help="override N (smaller runs)")
     p.add_argument("--eps", type=float, default=0.0)
@@ -209,6 +209,8 @@ def run_ours(args):
     x, eps, cfg = workload(args)
     n, d = x.shape
     proj_k = args.proj_k if args.proj_k >= 0 else cfg.get("proj_k", 0)
+    if args.precision == "config":
+        args.precision = cfg.get("precision", "auto")
     stream = torch.cuda.current_stream(dev)
     xd = torch.from_numpy(x).to(dev)
     cd = torch.empty(n, dtype=torch.int32, device=dev)

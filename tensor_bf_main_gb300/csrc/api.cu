@@ -453,11 +453,12 @@ static int run_screen16(Join& J, Fmt fmt, bool split, Learned& L) {
     return screen_and_recheck(J, cap0, screen, recheck, n_pad, tg, tr);
 }
 
-// AUTO: the hi+lo split narrows the band while the quantisation residual
-// dominates the bound (small d); for large d the FP32 accumulation term
-// (proportional to K) dominates and the split's 3x MMA work buys little.
+// AUTO (measured on GB300 over the benchmark shapes): FP16's 11-bit
+// significand keeps the band narrow at a third of the split's MMA work for
+// d <= 128; beyond that the FP32 accumulation term (proportional to K)
+// dominates the bound and BF16 (wider range, no scaling limits) is as fast.
 static int resolve_precision(int p, uint32_t d) {
-    if (p == EJOIN_AUTO) return d <= 256 ? EJOIN_BF16_SPLIT : EJOIN_BF16;
+    if (p == EJOIN_AUTO) return d <= 128 ? EJOIN_FP16 : EJOIN_BF16;
     return p;
 }
 

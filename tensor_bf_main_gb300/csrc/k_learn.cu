@@ -298,31 +298,71 @@ __global__ void __launch_bounds__(TRAIN_THREADS) train_step_kernel(const float* 
         for (uint32_t e = threadIdx.x; e < np * d; e += blockDim.x)
             sV[(e / d) * pitch + e % d] = pb.V[base * d + e];
         __syncthreads();
-        for (uint32_t p = threadIdx.x; p < TP; p += blockDim.x) {
-            float y[K];
+        if (d <= 256) {
+            // thread per pair
+            for (uint32_t p = threadIdx.x; p < TP; p += blockDim.x) {
+                float y[K];
 #pragma unroll
-            for (int a = 0; a < K; ++a) y[a] = 0.0f;
-            float coef = 0.0f;
-            if (p < np && pb.tgt[base + p] > 0.0f) {
-                const float* v = sV + p * pitch;
-                for (uint32_t c = 0; c < d; ++c) {
-                    const float vc = v[c];
+                for (int a = 0; a < K; ++a) y[a] = 0.0f;
+                float coef = 0.0f;
+                if (p < np && pb.tgt[base + p] > 0.0f) {
+                    const float* v = sV + p * pitch;
+                    for (uint32_t c = 0; c < d; ++c) {
+                        const float vc = v[c];
+#pragma unroll
+                        for (int a = 0; a < K; ++a)
+                            if (a < (int)k) y[a] = fmaf(sP[a * d + c], vc, y[a]);
+                    }
+                    float r2 = 0.0f;
+#pragma unroll
+                    for (int a = 0; a < K; ++a) r2 = fmaf(y[a], y[a], r2);
+                    const float r = sqrtf(r2), t = pb.tgt[base + p];
+                    if (r < t) {
+                        lsum += 1.0f - r / t;
+                        coef = r > 0.0f ? -invM / (t * r) : 0.0f;
+                    }
+                }
+#pragma unroll
+                for (int a = 0; a < K; ++a)
+                    if (a < (int)k) sC[p * k + a] = coef * y[a];
+            }
+        } else {
+            // warp per pair, lanes over coordinates (large d, few pairs per tile)
+            const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x / 32, nw = blockDim.x / 32;
+            for (uint32_t p = wid; p < TP; p += nw) {
+                const bool act = p < np && pb.tgt[base + p] > 0.0f;  // warp-uniform
+                float y[K];
+#pragma unroll
+                for (int a = 0; a < K; ++a) y[a] = 0.0f;
+                if (act) {
+                    const float* v = sV + p * pitch;
+                    for (uint32_t c = lane; c < d; c += 32) {
+                        const float vc = v[c];
+#pragma unroll
+                        for (int a = 0; a < K; ++a)
+                            if (a < (int)k) y[a] = fmaf(sP[a * d + c], vc, y[a]);
+                    }
 #pragma unroll
                     for (int a = 0; a < K; ++a)
-                        if (a < (int)k) y[a] = fmaf(sP[a * d + c], vc, y[a]);
+                        for (int o = 16; o; o >>= 1) y[a] += __shfl_xor_sync(0xffffffffu, y[a], o);
                 }
-                float r2 = 0.0f;
+                float coef = 0.0f;
+                if (act) {
+                    float r2 = 0.0f;
 #pragma unroll
-                for (int a = 0; a < K; ++a) r2 = fmaf(y[a], y[a], r2);
-                const float r = sqrtf(r2), t = pb.tgt[base + p];
-                if (r < t) {
-                    lsum += 1.0f - r / t;
-                    coef = r > 0.0f ? -invM / (t * r) : 0.0f;
+                    for (int a = 0; a < K; ++a) r2 = fmaf(y[a], y[a], r2);
+                    const float r = sqrtf(r2), t = pb.tgt[base + p];
+                    if (r < t) {
+                        if (lane == 0) lsum += 1.0f - r / t;
+                        coef = r > 0.0f ? -invM / (t * r) : 0.0f;
+                    }
+                }
+                if (lane == 0) {
+#pragma unroll
+                    for (int a = 0; a < K; ++a)
+                        if (a < (int)k) sC[p * k + a] = coef * y[a];
                 }
             }
-#pragma unroll
-            for (int a = 0; a < K; ++a)
-                if (a < (int)k) sC[p * k + a] = coef * y[a];
         }
         __syncthreads();
         // G[a][c] += sum_p sC[p][a] * V[p][c]  (thread-owned elements: no atomics)

@@ -29,13 +29,18 @@ import numpy as np
 
 CHUNK = 1 << 16
 
+# `precision` / `proj_k`: the arithmetic each configuration specifies (c1 the
+# plain FP64 join, c2 the FP16 path, c3 BF16 hi+lo, c4 BF16 hi+lo with a k = 8
+# projection, c5 FP8 E4M3 with a k = 16 projection).
 CONFIGS = {
-    "c1": dict(n=10_000, d=128, kind="uniform", target=32),
-    "c2": dict(n=1_000_000, d=128, kind="gmm", k=64, sigma=0.05, target=64),
-    "c3": dict(n=2_000_000, d=256, kind="powerlaw", target=(16, 128, 1024)),
+    "c1": dict(n=10_000, d=128, kind="uniform", target=32, precision="fp64_dmma"),
+    "c2": dict(n=1_000_000, d=128, kind="gmm", k=64, sigma=0.05, target=64, precision="fp16"),
+    "c3": dict(n=2_000_000, d=256, kind="powerlaw", target=(16, 128, 1024),
+               precision="bf16_split"),
     "c4": dict(n=4_000_000, d=64, kind="latent", k=256, latent=8, sigma=0.02, noise=0.01,
-               target=50, proj_k=8),
-    "c5": dict(n=1_000_000, d=1024, kind="sphere", k=1000, target=20, proj_k=16),
+               target=50, proj_k=8, precision="bf16_split"),
+    "c5": dict(n=1_000_000, d=1024, kind="sphere", k=1000, target=20, proj_k=16,
+               precision="fp8_e4m3"),
 }
 
 # Frozen radii (see calibrate()); c3 holds one radius per target mean.
