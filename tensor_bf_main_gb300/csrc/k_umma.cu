@@ -73,6 +73,9 @@ __device__ __forceinline__ float band_width(const GramArgs& a, uint2 w) {
     return W;
 }
 
+constexpr uint32_t BAND_SMEM = 1024;  // staged band entries per accumulator buffer
+constexpr uint32_t BAND_SKIP = 0xffffffffu;  // staged slot not used (recheck skips i >= n)
+
 struct Ctl {
     uint64_t full[NST], empty[NST];
     uint64_t tfull[2], tempty[2];
@@ -82,6 +85,8 @@ struct Ctl {
     uint32_t tmem_base;
     int rowacc[2][128];
     int colacc[2][128];
+    uint32_t band_n[2];                  // band entries staged for buffer b
+    BandPair band_buf[2][BAND_SMEM];     // staged band entries (flushed by the flusher warp)
 };
 
 constexpr size_t SMEM_BYTES = 1024 + (size_t)NST * STAGE_BYTES + sizeof(Ctl);
@@ -142,6 +147,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         ptx::tma_prefetch_desc(&taug);
     }
     for (int i = threadIdx.x; i < 512; i += NTHREADS) (&S.rowacc[0][0])[i] = 0;
+    if (threadIdx.x < 2) S.band_n[threadIdx.x] = 0;
     ptx::tc_fence_before();
     __syncthreads();
     ptx::tc_fence_after();
@@ -322,18 +328,39 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 const uint32_t row = w.x * 128u + q * 32u + lane;
                 const uint32_t col0 = w.y * 128u + cg * 32u;
                 if (__any_sync(FULL, bandm != 0)) {
-                    unsigned long long slot = band_reserve(a.st, __popc(bandm));
+                    // stage in shared memory (the flusher reserves global slots)
+                    const uint32_t nb = __popc(bandm);
+                    uint32_t incl = nb;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const uint32_t t = __shfl_up_sync(FULL, incl, o);
+                        if (lane >= (uint32_t)o) incl += t;
+                    }
+                    const uint32_t total = __shfl_sync(FULL, incl, 31);
+                    uint32_t base = 0;
+                    if (lane == 31) base = atomicAdd(&S.band_n[b], total);
+                    base = __shfl_sync(FULL, base, 31);
+                    const bool fits = base + total <= BAND_SMEM;  // warp-uniform
+                    uint32_t slot = base + incl - nb;
+                    unsigned long long gslot = fits ? 0ull : band_reserve(a.st, nb);
                     uint32_t m = bandm;
                     while (m) {
                         const uint32_t c = __ffs(m) - 1;
                         m &= m - 1;
-                        if (slot < a.band_cap) {
-                            BandPair bp;
-                            bp.i = row;
-                            bp.j = (col0 + c) | (diag ? 0u : kBandBoth);
-                            a.band[slot] = bp;
+                        BandPair bp;
+                        bp.i = row;
+                        bp.j = (col0 + c) | (diag ? 0u : kBandBoth);
+                        if (fits) {
+                            S.band_buf[b][slot++] = bp;
+                        } else {
+                            if (gslot < a.band_cap) a.band[gslot] = bp;
+                            ++gslot;
                         }
-                        ++slot;
+                    }
+                    if (!fits) {
+                        // mark this warp's staged slots unused
+                        for (uint32_t q2 = base + incl - nb; q2 < base + incl && q2 < BAND_SMEM; ++q2)
+                            S.band_buf[b][q2] = BandPair{BAND_SKIP, BAND_SKIP};
                     }
                 }
                 if (__any_sync(FULL, inm != 0)) {
@@ -371,6 +398,17 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 if (cv) atomicAdd(&a.counts[w.y * 128u + r], cv);
                 cacc[r] = 0;
             }
+            // staged band entries of this tile: one global reservation, coalesced copy
+            const uint32_t nst = min(S.band_n[b], BAND_SMEM);
+            if (nst) {
+                unsigned long long gbase = 0;
+                if (lane == 0) gbase = atomicAdd(&a.st->band_count, (unsigned long long)nst);
+                gbase = __shfl_sync(FULL, gbase, 0);
+                for (uint32_t e = lane; e < nst; e += 32)
+                    if (gbase + e < a.band_cap) a.band[gbase + e] = S.band_buf[b][e];
+            }
+            __syncwarp();
+            if (lane == 0) S.band_n[b] = 0;
             __syncwarp();
             if (lane == 0) ptx::mbar_arrive(&S.fdone[b]);
         }
