@@ -576,7 +576,7 @@ int ejoin_default_options(ejoin_options* opt) {
     opt->precision = EJOIN_AUTO;
     opt->proj_k = 0;
     opt->train_pairs = 1u << 20;
-    opt->train_steps = 200;
+    opt->train_steps = 50;
     opt->order = EJOIN_ORDER_MORTON;
     opt->seed = 0x5eed5eedull;
     opt->acc_bound_scale = 1.0;
