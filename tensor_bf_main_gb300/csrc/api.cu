@@ -261,7 +261,7 @@ static int run_dmma(Join& J) {
     EJ_TRY(mu.alloc(J.d, J.s, "mean"));
     double maxabs = 0;
     uint64_t ngood = 0;
-    EJ_TRY(launch_center_stats(J.X, J.n, J.d, bad.p, mu.p, &maxabs, &ngood, J.s));
+    EJ_TRY(launch_center_stats(J.X, J.n, J.d, bad.p, mu.p, &maxabs, &ngood, nullptr, J.s));
     DmmaParams P;
     P.d = J.d;
     P.dp = (uint32_t)round_up(J.d, 32);
@@ -303,7 +303,8 @@ struct Learned {
     uint32_t k = 0;
 };
 
-static int prepare_learned(Join& J, const double* mu, uint64_t n_pad, Learned& L) {
+static int prepare_learned(Join& J, const float* Y32, const uint8_t* bad, uint64_t n_pad,
+                           Learned& L) {
     const uint32_t k = J.opt.proj_k;
     if (k == 0 || k > 16) return set_error(EJOIN_EINVAL, "proj_k must be in 0..16 (got %u)", k);
     EventTimer tt, to;
@@ -315,7 +316,7 @@ static int prepare_learned(Join& J, const double* mu, uint64_t n_pad, Learned& L
         EJ_TRY(cert_spectral_norm(P.data(), k, J.d, &sigma));
     } else {
         TrainResult tr;
-        EJ_TRY(train_projection_dev(J.X, mu, J.n, J.d, J.eps, k, J.opt.train_pairs,
+        EJ_TRY(train_projection_dev(Y32, bad, J.n, J.d, J.eps, k, J.opt.train_pairs,
                                     J.opt.train_steps, J.opt.seed, J.opt.order == EJOIN_ORDER_LEAD,
                                     J.s, tr));
         P.swap(tr.P);
@@ -326,7 +327,7 @@ static int prepare_learned(Join& J, const double* mu, uint64_t n_pad, Learned& L
     DBuf<float> Pd;
     EJ_TRY(Pd.alloc(P.size(), J.s, "projection"));
     EJ_CUDA(cudaMemcpyAsync(Pd.p, P.data(), P.size() * sizeof(float), cudaMemcpyHostToDevice, J.s));
-    EJ_TRY(learned_order(J.X, mu, J.n, n_pad, J.d, Pd.p, k, J.opt.order == EJOIN_ORDER_LEAD,
+    EJ_TRY(learned_order(Y32, bad, J.n, n_pad, J.d, Pd.p, k, J.opt.order == EJOIN_ORDER_LEAD,
                          L.perm, &L.boxes, J.s));
     to.stop(J.s);
     double Tlo, Thi;
@@ -367,11 +368,16 @@ static int run_screen16(Join& J, Fmt fmt, bool split, Learned& L) {
     EJ_TRY(mu.alloc(J.d, J.s, "mean"));
     double maxabs = 0;
     uint64_t ngood = 0;
-    EJ_TRY(launch_center_stats(J.X, J.n, J.d, bad.p, mu.p, &maxabs, &ngood, J.s));
+    DBuf<float> Y32;
+    EJ_TRY(Y32.alloc(J.n * J.d, J.s, "FP32 centred points"));
+    EJ_TRY(launch_center_stats(J.X, J.n, J.d, bad.p, mu.p, &maxabs, &ngood, Y32.p, J.s));
     tp.stop(J.s);
     const double ms_center = tp.ms();
+    // centred coordinates beyond the FP32 range: the FP32 copies would
+    // overflow, so such data takes the (equally exact) FP64 DMMA screen
+    if (!(maxabs < 1e36)) return run_dmma(J);
     const uint64_t n_pad = round_up(J.n, 128);
-    if (J.opt.proj_k) EJ_TRY(prepare_learned(J, mu.p, n_pad, L));
+    if (J.opt.proj_k) EJ_TRY(prepare_learned(J, Y32.p, bad.p, n_pad, L));
     tp.start(J.s);
     ScreenParams P;
     const bool fp8 = (fmt == Fmt::E4M3);
@@ -410,11 +416,11 @@ static int run_screen16(Join& J, Fmt fmt, bool split, Learned& L) {
     if (fp8) {
         EJ_TRY(sig.alloc(n_pad, J.s, "row scales"));
         EJ_TRY(tsig.alloc(n_pad / 128, J.s, "tile scales"));
-        EJ_TRY(launch_pack8(J.X, J.n, n_pad, J.perm, bad.p, mu.p, P, Q8.p, Aug.p, beta.p, sig.p,
+        EJ_TRY(launch_pack8(Y32.p, J.n, n_pad, J.perm, bad.p, P, Q8.p, Aug.p, beta.p, sig.p,
                             Xf.p, rad.p, tsig.p, J.s));
     } else {
-        EJ_TRY(launch_pack16(J.X, J.n, n_pad, J.perm, bad.p, mu.p, P, Q.p, Aug.p, beta.p, Xf.p,
-                             rad.p, J.s));
+        EJ_TRY(launch_pack16(Y32.p, J.n, n_pad, J.perm, bad.p, P, Q.p, Aug.p, beta.p, Xf.p, rad.p,
+                             J.s));
     }
     EJ_TRY(launch_tile_max(beta.p, nullptr, n_pad, tmax.p, J.s));
     tp.stop(J.s);
@@ -665,10 +671,12 @@ int ejoin_train_projection(const double* points, uint64_t n, uint32_t d, double 
     EJ_TRY(mu.alloc(d, s, "mean"));
     double maxabs = 0;
     uint64_t ngood = 0;
-    EJ_TRY(launch_center_stats(X, n, d, bad.p, mu.p, &maxabs, &ngood, s));
+    DBuf<float> Y32;
+    EJ_TRY(Y32.alloc(n * d, s, "FP32 centred points"));
+    EJ_TRY(launch_center_stats(X, n, d, bad.p, mu.p, &maxabs, &ngood, Y32.p, s));
     TrainResult tr;
-    EJ_TRY(train_projection_dev(X, mu.p, n, d, eps, opt.proj_k, opt.train_pairs, opt.train_steps,
-                                opt.seed, opt.order == EJOIN_ORDER_LEAD, s, tr));
+    EJ_TRY(train_projection_dev(Y32.p, bad.p, n, d, eps, opt.proj_k, opt.train_pairs,
+                                opt.train_steps, opt.seed, opt.order == EJOIN_ORDER_LEAD, s, tr));
     t.stop(s);
     memcpy(P_out, tr.P.data(), tr.P.size() * sizeof(float));
     if (sigma_cert_out) *sigma_cert_out = tr.sigma_cert;

@@ -252,10 +252,11 @@ struct TrainResult {
     double loss_first = 0, loss_last = 0;
     double sigma_cert = 0;
 };
-int train_projection_dev(const double* X, const double* mu, uint64_t n, uint32_t d, double eps,
+// Y32: FP32 centred copy of the points (launch_center_stats); bad: row flags.
+int train_projection_dev(const float* Y32, const uint8_t* bad, uint64_t n, uint32_t d, double eps,
                          uint32_t k, uint64_t pairs, uint32_t steps, uint64_t seed, int lead_only,
                          cudaStream_t s, TrainResult& out);
-int learned_order(const double* X, const double* mu, uint64_t n, uint64_t n_pad, uint32_t d,
+int learned_order(const float* Y32, const uint8_t* bad, uint64_t n, uint64_t n_pad, uint32_t d,
                   const float* P_dev, uint32_t k, int lead_only, DBuf<uint32_t>& perm,
                   LearnedBoxes* boxes, cudaStream_t s);
 // host.cpp: certified upper bound of ||P||_2
@@ -268,8 +269,9 @@ int launch_band_recheck2(const double* X, uint64_t n, uint32_t d, const uint32_t
 // k_prep.cu
 // bad[i] = 1 for rows with a non-finite coordinate; mean over the good rows
 // (deterministic two-pass sums); max |fl(x - mu)| over good rows.
+// Also writes the FP32 centred copy Y32 [n][d] when Y32 is non-null.
 int launch_center_stats(const double* X, uint64_t n, uint32_t d, uint8_t* bad, double* mu,
-                        double* maxabs, uint64_t* ngood, cudaStream_t s);
+                        double* maxabs, uint64_t* ngood, float* Y32, cudaStream_t s);
 // FP64 centred copy Y[n_pad][dp] and per-row thresholds h, g for the DMMA screen.
 int launch_pack_dmma(const double* X, uint64_t n, uint64_t n_pad, const uint32_t* perm,
                      const uint8_t* bad, const double* mu, const DmmaParams& P, double* Y,
@@ -277,13 +279,13 @@ int launch_pack_dmma(const double* X, uint64_t n, uint64_t n_pad, const uint32_t
 // 16-bit operand rows [hi | lo], aug rows [augA(16) | augB(16)], per-row
 // out-margins beta, FP32 coordinates Xf ([n_pad][d], scaled, centred) and
 // their per-row error radius.
-int launch_pack16(const double* X, uint64_t n, uint64_t n_pad, const uint32_t* perm,
-                  const uint8_t* bad, const double* mu, const ScreenParams& P, void* Q,
-                  void* Aug, float* beta, float* Xf, float* rad, cudaStream_t s);
+int launch_pack16(const float* Y32, uint64_t n, uint64_t n_pad, const uint32_t* perm,
+                  const uint8_t* bad, const ScreenParams& P, void* Q, void* Aug, float* beta,
+                  float* Xf, float* rad, cudaStream_t s);
 // E4M3 operand rows with per-row power-of-two scales sigma, BF16 aug rows,
 // beta, sigma, FP32 coordinates / radii, and the per-tile minimum sigma.
-int launch_pack8(const double* X, uint64_t n, uint64_t n_pad, const uint32_t* perm,
-                 const uint8_t* bad, const double* mu, const ScreenParams& P, uint8_t* Q,
+int launch_pack8(const float* Y32, uint64_t n, uint64_t n_pad, const uint32_t* perm,
+                 const uint8_t* bad, const ScreenParams& P, uint8_t* Q,
                  void* Aug, float* beta, float* sig, float* Xf, float* rad, float* tsig,
                  cudaStream_t s);
 // per 128-row tile: max of beta (16-bit) or of meta.z (FP8), as float

@@ -47,15 +47,15 @@ __host__ __device__ __forceinline__ uint64_t splitmix64(uint64_t x) {
 
 // ------------------------------------------------------------ projection --
 
-// proj[i][a] = fl32(sum_c P[a][c] * yf[i][c]) with yf = fl32(fl64(x - mu)),
-// thread per point, P in shared memory.  err[i] bounds the distance from the
+// proj[i][a] = fl32(sum_c P[a][c] * yf[i][c]) with yf = fl32(fl64(x - mu))
+// (the FP32 centred copy), thread per point, P in shared memory.  err[i] bounds the distance from the
 // exact P (x_i - mu) in every coordinate:
 //   |yf_c - (x_c - mu_c)| <= 1.0001 * 2^-24 |yf_c| (+ 2^-149 if subnormal),
 //   FP32 fma accumulation of d terms <= (d + 2) 2^-24 sum |P yf|,
 // so err = (d + 4) 2^-24 S (1 + 2^-16) + d 2^-148, S = sum_c |P_ac| |yf_c|
 // (itself computed with upward rounding).  Projections of x - mu give the
 // same differences P(x_i - x_j) as projections of x.  Non-finite rows get NaN.
-__global__ void project_kernel(const double* __restrict__ X, const double* __restrict__ mu,
+__global__ void project_kernel(const float* __restrict__ Y32, const uint8_t* __restrict__ bad,
                                uint64_t n, uint32_t d, const float* __restrict__ P, uint32_t k,
                                float* proj, float* err) {
     extern __shared__ float sP[];
@@ -63,15 +63,18 @@ __global__ void project_kernel(const double* __restrict__ X, const double* __res
     __syncthreads();
     const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const double* x = X + i * d;
+    const float NaNf = __int_as_float(0x7fc00000);
+    if (bad[i]) {
+        for (uint32_t a = 0; a < k; ++a) proj[i * k + a] = NaNf;
+        err[i] = NaNf;
+        return;
+    }
+    const float* y = Y32 + i * d;
     float acc[16], sabs[16];
 #pragma unroll
     for (int a = 0; a < 16; ++a) acc[a] = sabs[a] = 0.0f;
-    bool finite = true;
     for (uint32_t c = 0; c < d; ++c) {
-        const double y = __dsub_rn(x[c], mu[c]);
-        finite &= isfinite(y) != 0;
-        const float yf = (float)y;
+        const float yf = y[c];
         const float ay = fabsf(yf);
 #pragma unroll
         for (int a = 0; a < 16; ++a)
@@ -85,11 +88,11 @@ __global__ void project_kernel(const double* __restrict__ X, const double* __res
 #pragma unroll
     for (int a = 0; a < 16; ++a)
         if (a < (int)k) {
-            proj[i * k + a] = finite ? acc[a] : __int_as_float(0x7fc00000);
+            proj[i * k + a] = acc[a];
             smax = fmaxf(smax, sabs[a]);
         }
     const float c1 = (float)(d + 4) * 5.9604644775390625e-08f * 1.0000153f;  // (d+4) 2^-24 (1+2^-16)
-    err[i] = finite ? __fmaf_ru(c1, smax, (float)d * 3.5873240686715317e-43f) : __int_as_float(0x7fc00000);
+    err[i] = __fmaf_ru(c1, smax, (float)d * 3.5873240686715317e-43f);
 }
 
 __device__ __forceinline__ uint32_t ordered_bits32(float v) {
@@ -213,10 +216,13 @@ struct PairBatch {
     float* tgt;      // [M] hinge target t (0 = pair not far: inactive)
 };
 
-// Half uniform random pairs, half pairs close in the current order (perm).
-__global__ void sample_pairs_kernel(const double* __restrict__ X, uint64_t n, uint32_t d,
-                                    const uint32_t* __restrict__ perm, uint64_t M, uint64_t seed,
-                                    double eps, uint32_t window, PairBatch pb) {
+// Half uniform random pairs, half pairs close in the current order (perm);
+// differences and distances from the FP32 centred copy (training needs no
+// exactness).  Pairs with a non-finite row are inactive.
+__global__ void sample_pairs_kernel(const float* __restrict__ Y32, const uint8_t* __restrict__ bad,
+                                    uint64_t n, uint32_t d, const uint32_t* __restrict__ perm,
+                                    uint64_t M, uint64_t seed, double eps, uint32_t window,
+                                    PairBatch pb) {
     const uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
     if (e >= M) return;
     const uint64_t h1 = splitmix64(seed ^ (e * 0x9E3779B97F4A7C15ull));
@@ -232,19 +238,17 @@ __global__ void sample_pairs_kernel(const double* __restrict__ X, uint64_t n, ui
         i = perm ? perm[t] : t;
         j = perm ? perm[u] : u;
     }
-    const double* a = X + i * d;
-    const double* b = X + j * d;
-    double s = 0.0;
-    bool fin = true;
+    const float* a = Y32 + i * d;
+    const float* b = Y32 + j * d;
+    float s = 0.0f;
     for (uint32_t c = 0; c < d; ++c) {
-        const double v = a[c] - b[c];
-        fin &= isfinite(v) != 0;
-        s = __fma_rn(v, v, s);
-        pb.V[e * d + c] = (float)v;
+        const float v = a[c] - b[c];
+        s = fmaf(v, v, s);
+        pb.V[e * d + c] = v;
     }
-    const double delta = sqrt(s);
+    const float delta = sqrtf(s);
     float t = 0.0f;
-    if (fin && delta > eps * 1.02) t = (float)fmin(delta, 2.0 * eps);
+    if (!bad[i] && !bad[j] && delta > (float)(eps * 1.02)) t = fminf(delta, (float)(2.0 * eps));
     pb.tgt[e] = t;
 }
 
@@ -475,7 +479,7 @@ __global__ void adam_renorm_kernel(float* P, unsigned long long* G, float* m1, f
 // given, computes the boxes of the 128-row tiles and of super-blocks of
 // kSuperTiles tiles (FP32, outward rounded).  perm: sorted position ->
 // original row.
-int learned_order(const double* X, const double* mu, uint64_t n, uint64_t n_pad, uint32_t d,
+int learned_order(const float* Y32, const uint8_t* bad, uint64_t n, uint64_t n_pad, uint32_t d,
                   const float* P_dev, uint32_t k, int lead_only, DBuf<uint32_t>& perm,
                   LearnedBoxes* boxes, cudaStream_t s) {
     DBuf<float> proj, err;
@@ -483,7 +487,8 @@ int learned_order(const double* X, const double* mu, uint64_t n, uint64_t n_pad,
     EJ_TRY(err.alloc(n, s, "projection error bounds"));
     const size_t shm = (size_t)k * d * sizeof(float);
     EJ_CUDA(cudaFuncSetAttribute(project_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
-    project_kernel<<<(unsigned)((n + 127) / 128), 128, shm, s>>>(X, mu, n, d, P_dev, k, proj.p, err.p);
+    project_kernel<<<(unsigned)((n + 127) / 128), 128, shm, s>>>(Y32, bad, n, d, P_dev, k, proj.p,
+                                                                 err.p);
     EJ_CUDA(cudaGetLastError());
     note_launch();
     DBuf<unsigned int> rng;
@@ -530,7 +535,7 @@ int learned_order(const double* X, const double* mu, uint64_t n, uint64_t n_pad,
     return EJOIN_OK;
 }
 
-int train_projection_dev(const double* X, const double* mu, uint64_t n, uint32_t d, double eps,
+int train_projection_dev(const float* Y32, const uint8_t* bad, uint64_t n, uint32_t d, double eps,
                          uint32_t k, uint64_t pairs, uint32_t steps, uint64_t seed, int lead_only,
                          cudaStream_t s, TrainResult& out) {
     if (k == 0 || k > 16) return set_error(EJOIN_EINVAL, "proj_k must be in 1..16");
@@ -579,9 +584,9 @@ int train_projection_dev(const double* X, const double* mu, uint64_t n, uint32_t
     uint64_t cursor = 0;
     for (uint32_t r = 0; r < rounds; ++r) {
         DBuf<uint32_t> perm;
-        EJ_TRY(learned_order(X, mu, n, n_pad, d, P.p, k, lead_only, perm, nullptr, s));
+        EJ_TRY(learned_order(Y32, bad, n, n_pad, d, P.p, k, lead_only, perm, nullptr, s));
         sample_pairs_kernel<<<(unsigned)((M + 255) / 256), 256, 0, s>>>(
-            X, n, d, perm.p, M, seed + 7919ull * (r + 1), eps, 256, PairBatch{V.p, tgt.p});
+            Y32, bad, n, d, perm.p, M, seed + 7919ull * (r + 1), eps, 256, PairBatch{V.p, tgt.p});
         EJ_CUDA(cudaGetLastError());
         note_launch();
         const uint32_t nsteps = steps / rounds + (r < steps % rounds ? 1 : 0);

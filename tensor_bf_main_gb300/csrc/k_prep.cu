@@ -68,14 +68,25 @@ __global__ void colsum_final_kernel(const double* __restrict__ partial, uint32_t
     mu[k] = g ? s / (double)g : 0.0;
 }
 
+// max |fl(x - mu)| over the finite rows and, when Y32 is given, the FP32
+// centred copy Y32[i][k] = fl32(fl64(x_ik - mu_k)) (0 for non-finite rows).
+// Later passes (projection, training pairs, operand packing) read Y32 instead
+// of re-centring the FP64 rows: on this GPU FP64 arithmetic is the scarce
+// resource, and every bound downstream needs only |Y32 - y| <= 2^-24 |y|
+// (+ 2^-149 for subnormal results).
 __global__ void maxabs_kernel(const double* __restrict__ X, uint64_t n, uint32_t d,
                               const uint8_t* __restrict__ bad, const double* __restrict__ mu,
-                              unsigned long long* maxbits) {
+                              unsigned long long* maxbits, float* Y32) {
     const uint64_t row = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / 32;
     const int lane = threadIdx.x & 31;
     double m = 0.0;
-    if (row < n && !bad[row]) {
-        for (uint32_t k = lane; k < d; k += 32) m = fmax(m, fabs(__dsub_rn(X[row * d + k], mu[k])));
+    if (row < n) {
+        const bool good = !bad[row];
+        for (uint32_t k = lane; k < d; k += 32) {
+            const double y = good ? __dsub_rn(X[row * d + k], mu[k]) : 0.0;
+            m = fmax(m, fabs(y));
+            if (Y32) Y32[row * d + k] = (float)y;
+        }
     }
     for (int o = 16; o; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
     // one atomic per block (non-negative doubles order like their bit patterns)
@@ -201,11 +212,10 @@ __device__ __forceinline__ float round_fmt_f(float v, int fbits, float min_norma
 // a per-row radius go to Xf / rad for the FP32 band pre-check.  Phase 2 (lane
 // = row): the FP64 threshold arithmetic (alpha, beta), the aug slab.
 template <Fmt F>
-__global__ void __launch_bounds__(256) pack16_kernel(const double* __restrict__ X, uint64_t n,
+__global__ void __launch_bounds__(256) pack16_kernel(const float* __restrict__ Y32, uint64_t n,
                                                      uint64_t n_pad,
                                                      const uint32_t* __restrict__ perm,
-                                                     const uint8_t* __restrict__ bad,
-                                                     const double* __restrict__ mu, ScreenParams P,
+                                                     const uint8_t* __restrict__ bad, ScreenParams P,
                                                      uint16_t* Q, uint16_t* Aug, float* beta,
                                                      float* Xf, float* rad) {
     const uint64_t p0 = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / 32 * 32;
@@ -227,8 +237,7 @@ __global__ void __launch_bounds__(256) pack16_kernel(const double* __restrict__ 
         for (uint32_t k = lane; k < P.dp; k += 32) {
             float hi = 0.0f, lo = 0.0f, zf = 0.0f;
             if (good && k < P.d) {
-                const double z = __dmul_rn(__dsub_rn(X[src * P.d + k], mu[k]), P.scale);
-                zf = (float)z;
+                zf = Y32[src * P.d + k] * sf;  // exact power-of-two scaling
                 if (fabsf(zf) < 1.1754944e-38f) zf = 0.0f;  // keep Xf free of FP32 subnormals
                 hi = round_fmt_f(zf, fi.fbits, mnf);
                 float ef = zf - hi;  // exact
@@ -264,7 +273,6 @@ __global__ void __launch_bounds__(256) pack16_kernel(const double* __restrict__ 
             m_good = good;
         }
     }
-    (void)sf;
     // ---- phase 2: row p0 + lane
     const uint64_t p = p0 + lane;
     double ah[3] = {0, 0, 0};
@@ -276,8 +284,10 @@ __global__ void __launch_bounds__(256) pack16_kernel(const double* __restrict__ 
         const double a2u = (double)m_a2, lu = (double)m_l2;
         const double zn = sqrt((double)m_z2) * (1 + 1e-7);  // >= |zf|; |z| <= |zf| (1 + 2^-24)
         // |z - q| <= |z - zf| + |ef|, plus the centring error u |z|
-        // FP32 rounding of z (relative 2^-24) or flush of values below 2^-126
-        const double zerr = (5.9604645e-08 + 2.0 * kU) * zn * 1.0001 + 1.18e-38 * sqrt((double)P.d);
+        // FP32 rounding of z (relative 2^-24, subnormal 2^-149 before scaling) or
+        // flush of values below 2^-126, plus the FP64 centring error u |z|
+        const double zerr = (5.9604645e-08 + 2.0 * kU) * zn * 1.0001 +
+                            (1.18e-38 + 1.41e-45 * P.scale) * sqrt((double)P.d);
         const double rho = (sqrt((double)m_e2) * (1 + 1e-7) + zerr) * (1 + 8 * kU);
         radius = __double2float_ru(zerr);
         double R = nup + P.cacc * a2u + lu + P.absacc - 0.5 * P.Tlo + 2.0 * P.sTlo * rho;
@@ -340,11 +350,10 @@ __global__ void __launch_bounds__(256) pack16_kernel(const double* __restrict__ 
 // so that the accumulator, in units of F = f_i . f_j, holds
 // F - (alpha_i + alpha_j) / (sigma_i sigma_j).
 constexpr int PACK8_MAXV = 32;  // coordinates per lane: d <= 1024
-__global__ void __launch_bounds__(256) pack8_kernel(const double* __restrict__ X, uint64_t n,
+__global__ void __launch_bounds__(256) pack8_kernel(const float* __restrict__ Y32, uint64_t n,
                                                     uint64_t n_pad,
                                                     const uint32_t* __restrict__ perm,
-                                                    const uint8_t* __restrict__ bad,
-                                                    const double* __restrict__ mu, ScreenParams P,
+                                                    const uint8_t* __restrict__ bad, ScreenParams P,
                                                     uint8_t* Q, uint16_t* Aug, float* beta,
                                                     float* sig, float* Xf, float* rad) {
     const uint64_t p0 = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / 32 * 32;
@@ -365,7 +374,7 @@ __global__ void __launch_bounds__(256) pack8_kernel(const double* __restrict__ X
             const uint32_t k = lane + 32u * t;
             float zf = 0.0f;
             if (good && k < P.d) {
-                zf = (float)__dmul_rn(__dsub_rn(X[src * P.d + k], mu[k]), P.scale);
+                zf = Y32[src * P.d + k] * (float)P.scale;  // exact power-of-two scaling
                 if (fabsf(zf) < 1.1754944e-38f) zf = 0.0f;
             }
             zv[t] = zf;
@@ -422,7 +431,8 @@ __global__ void __launch_bounds__(256) pack8_kernel(const double* __restrict__ X
         const double nup = m_nq * (1 + gs), ndn = m_nq * (1 - gs);
         const double a2u = nup;  // |(|q|)|^2 = |q|^2
         const double zn = sqrt((double)m_z2) * (1 + 1e-7);
-        const double zerr = (5.9604645e-08 + 2.0 * kU) * zn * 1.0001 + 1.18e-38 * sqrt((double)P.d);
+        const double zerr = (5.9604645e-08 + 2.0 * kU) * zn * 1.0001 +
+                            (1.18e-38 + 1.41e-45 * P.scale) * sqrt((double)P.d);
         const double rho = (sqrt((double)m_e2) * (1 + 1e-7) + zerr) * (1 + 8 * kU);
         radius = __double2float_ru(zerr);
         double R = nup + P.cacc * a2u + P.absacc - 0.5 * P.Tlo + 2.0 * P.sTlo * rho;
@@ -514,7 +524,7 @@ __global__ void tile_max_kernel(const float* __restrict__ beta, const float4* __
 }  // namespace
 
 int launch_center_stats(const double* X, uint64_t n, uint32_t d, uint8_t* bad, double* mu,
-                        double* maxabs, uint64_t* ngood_host, cudaStream_t s) {
+                        double* maxabs, uint64_t* ngood_host, float* Y32, cudaStream_t s) {
     DBuf<unsigned long long> cnt;
     EJ_TRY(cnt.alloc(2, s, "center stats"));
     EJ_TRY(cnt.zero(s));
@@ -531,7 +541,7 @@ int launch_center_stats(const double* X, uint64_t n, uint32_t d, uint8_t* bad, d
     colsum_final_kernel<<<(d + 127) / 128, 128, 0, s>>>(part.p, nb, d, cnt.p, mu);
     EJ_CUDA(cudaGetLastError());
     note_launch();
-    maxabs_kernel<<<(unsigned)warps_blocks, 256, 0, s>>>(X, n, d, bad, mu, cnt.p + 1);
+    maxabs_kernel<<<(unsigned)warps_blocks, 256, 0, s>>>(X, n, d, bad, mu, cnt.p + 1, Y32);
     EJ_CUDA(cudaGetLastError());
     note_launch();
     unsigned long long h[2];
@@ -554,17 +564,17 @@ int launch_pack_dmma(const double* X, uint64_t n, uint64_t n_pad, const uint32_t
     return EJOIN_OK;
 }
 
-int launch_pack16(const double* X, uint64_t n, uint64_t n_pad, const uint32_t* perm,
-                  const uint8_t* bad, const double* mu, const ScreenParams& P, void* Q,
-                  void* Aug, float* beta, float* Xf, float* rad, cudaStream_t s) {
+int launch_pack16(const float* Y32, uint64_t n, uint64_t n_pad, const uint32_t* perm,
+                  const uint8_t* bad, const ScreenParams& P, void* Q, void* Aug, float* beta,
+                  float* Xf, float* rad, cudaStream_t s) {
     if (n_pad % 32) return set_error(EJOIN_EINTERNAL, "pack16: rows not padded");
     const uint64_t blocks = (n_pad + 255) / 256;  // 8 warps x 32 rows per block
     if (P.fmt == Fmt::BF16)
-        pack16_kernel<Fmt::BF16><<<(unsigned)blocks, 256, 0, s>>>(X, n, n_pad, perm, bad, mu, P,
+        pack16_kernel<Fmt::BF16><<<(unsigned)blocks, 256, 0, s>>>(Y32, n, n_pad, perm, bad, P,
                                                                   (uint16_t*)Q, (uint16_t*)Aug,
                                                                   beta, Xf, rad);
     else if (P.fmt == Fmt::FP16)
-        pack16_kernel<Fmt::FP16><<<(unsigned)blocks, 256, 0, s>>>(X, n, n_pad, perm, bad, mu, P,
+        pack16_kernel<Fmt::FP16><<<(unsigned)blocks, 256, 0, s>>>(Y32, n, n_pad, perm, bad, P,
                                                                   (uint16_t*)Q, (uint16_t*)Aug,
                                                                   beta, Xf, rad);
     else
@@ -574,13 +584,13 @@ int launch_pack16(const double* X, uint64_t n, uint64_t n_pad, const uint32_t* p
     return EJOIN_OK;
 }
 
-int launch_pack8(const double* X, uint64_t n, uint64_t n_pad, const uint32_t* perm,
-                 const uint8_t* bad, const double* mu, const ScreenParams& P, uint8_t* Q,
+int launch_pack8(const float* Y32, uint64_t n, uint64_t n_pad, const uint32_t* perm,
+                 const uint8_t* bad, const ScreenParams& P, uint8_t* Q,
                  void* Aug, float* beta, float* sig, float* Xf, float* rad, float* tsig,
                  cudaStream_t s) {
     if (n_pad % 128) return set_error(EJOIN_EINTERNAL, "pack8: rows not padded");
     if (P.d > 32u * PACK8_MAXV) return set_error(EJOIN_EUNSUPPORTED, "FP8 screen supports d <= %d", 32 * PACK8_MAXV);
-    pack8_kernel<<<(unsigned)((n_pad + 255) / 256), 256, 0, s>>>(X, n, n_pad, perm, bad, mu, P, Q,
+    pack8_kernel<<<(unsigned)((n_pad + 255) / 256), 256, 0, s>>>(Y32, n, n_pad, perm, bad, P, Q,
                                                                  (uint16_t*)Aug, beta, sig, Xf, rad);
     EJ_CUDA(cudaGetLastError());
     note_launch();

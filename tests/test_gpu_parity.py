@@ -162,3 +162,17 @@ def test_cli_reference_argv_and_csv(ej, tmp_path):
     lines = open(tmp_path / "tensor_brute-force.txt").read().splitlines()
     assert lines[0].startswith("Dataset, epsilon, searchMode, executionTime, totalNeighbors")
     assert len(lines) == 4 and lines[1].split(", ")[4] == "11100"
+
+
+@pytest.mark.parametrize("mode", ["bf16_split", "fp16", "fp8_e4m3"])
+def test_extreme_magnitudes(ej, oracle_mod, mode):
+    """Coordinates near the FP64 range limits: tiny (1e-200) and huge (1e200,
+    beyond FP32) data stay exact (huge data takes the FP64 screen)."""
+    rng = np.random.default_rng(31)
+    base = clustered(1500, 16, rng)
+    for scale in (1e-200, 1e-30, 1e30, 1e200):
+        x = base * scale
+        eps = eps_for_mean(x, 15, rng)
+        exp, tot = oracle_mod.self_join(x, eps)
+        counts, total, st = ej.self_join(x, eps, precision=mode)
+        assert np.array_equal(counts, exp), (scale, st)
