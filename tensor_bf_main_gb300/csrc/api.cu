@@ -373,9 +373,11 @@ static int run_screen16(Join& J, Fmt fmt, bool split, Learned& L) {
     EJ_TRY(launch_center_stats(J.X, J.n, J.d, bad.p, mu.p, &maxabs, &ngood, Y32.p, J.s));
     tp.stop(J.s);
     const double ms_center = tp.ms();
-    // centred coordinates beyond the FP32 range: the FP32 copies would
-    // overflow, so such data takes the (equally exact) FP64 DMMA screen
-    if (!(maxabs < 1e36)) return run_dmma(J);
+    // The FP32 copies and the power-of-two operand scale need the centred
+    // coordinates well inside the FP32 range (the scale 1 / max|y| must be an
+    // FP32 number and max|y| must not under- or overflow in FP32).  Other data
+    // takes the (equally exact) FP64 DMMA screen.
+    if (!(maxabs == 0.0 || (maxabs > 1e-30 && maxabs < 1e30))) return run_dmma(J);
     const uint64_t n_pad = round_up(J.n, 128);
     if (J.opt.proj_k) EJ_TRY(prepare_learned(J, Y32.p, bad.p, n_pad, L));
     tp.start(J.s);

@@ -176,13 +176,17 @@ __global__ void pack_dmma_kernel(const double* __restrict__ X, uint64_t n, uint6
         return;
     }
     const double gs = (P.d + 4) * kU;
-    const double nup = nrm * (1 + gs), ndn = nrm * (1 - gs);
-    const double rho = 1.0001 * kU * sqrt(nup) * (1 + 8 * kU);
+    // FP64 underflow: every square, product and rounded sum may lose up to
+    // 2^-1074 in absolute terms (relevant for data near the bottom of the
+    // double range); these absolute terms join the relative bounds below
+    const double tiny = (2.0 * P.dp + P.d + 16) * 4.9406564584124654e-324;
+    const double nup = nrm * (1 + gs) + tiny, ndn = nrm * (1 - gs) - tiny;
+    const double rho = 1.0001 * kU * sqrt(nup) * (1 + 8 * kU) + tiny;
     // in:  G >= h_i + h_j   (h rounded up, incl. epilogue subtraction rounding)
-    double hv = 0.5 * (nup * (1 + P.crel) + 2.0 * P.sTlo * rho - 0.5 * P.Tlo);
+    double hv = 0.5 * (nup * (1 + P.crel) + 2.0 * P.sTlo * rho - 0.5 * P.Tlo) + tiny;
     hv += 8 * kU * (nup + fabs(hv) + P.Tlo + P.sTlo * rho);
     // out: G <  g_i + g_j   (g rounded down)
-    double gv = 0.5 * (ndn - P.crel * nup - 0.5 * P.Thi - 2.0 * P.sThi * rho - 2.0 * rho * rho);
+    double gv = 0.5 * (ndn - P.crel * nup - 0.5 * P.Thi - 2.0 * P.sThi * rho - 2.0 * rho * rho) - tiny;
     gv -= 8 * kU * (nup + fabs(gv) + P.Thi + P.sThi * rho);
     h[p] = hv;
     g[p] = gv;

@@ -164,7 +164,7 @@ def test_cli_reference_argv_and_csv(ej, tmp_path):
     assert len(lines) == 4 and lines[1].split(", ")[4] == "11100"
 
 
-@pytest.mark.parametrize("mode", ["bf16_split", "fp16", "fp8_e4m3"])
+@pytest.mark.parametrize("mode", ["bf16_split", "fp16", "fp8_e4m3", "fp64_dmma"])
 def test_extreme_magnitudes(ej, oracle_mod, mode):
     """Coordinates near the FP64 range limits: tiny (1e-200) and huge (1e200,
     beyond FP32) data stay exact (huge data takes the FP64 screen)."""
