@@ -259,9 +259,8 @@ static int run_dmma(Join& J) {
     DBuf<double> mu;
     EJ_TRY(bad.alloc(J.n, J.s, "row flags"));
     EJ_TRY(mu.alloc(J.d, J.s, "mean"));
-    double maxabs = 0;
-    uint64_t ngood = 0;
-    EJ_TRY(launch_center_stats(J.X, J.n, J.d, bad.p, mu.p, &maxabs, &ngood, nullptr, J.s));
+    CenterStats cs;
+    EJ_TRY(launch_center_stats(J.X, J.n, J.d, bad.p, mu.p, nullptr, nullptr, &cs, J.s));
     DmmaParams P;
     P.d = J.d;
     P.dp = (uint32_t)round_up(J.d, 32);
@@ -303,8 +302,8 @@ struct Learned {
     uint32_t k = 0;
 };
 
-static int prepare_learned(Join& J, const float* Y32, const uint8_t* bad, uint64_t n_pad,
-                           Learned& L) {
+static int prepare_learned(Join& J, const float* Y32, const float* Yerr, const uint8_t* bad,
+                           uint64_t n_pad, Learned& L) {
     const uint32_t k = J.opt.proj_k;
     if (k == 0 || k > 16) return set_error(EJOIN_EINVAL, "proj_k must be in 0..16 (got %u)", k);
     EventTimer tt, to;
@@ -327,8 +326,19 @@ static int prepare_learned(Join& J, const float* Y32, const uint8_t* bad, uint64
     DBuf<float> Pd;
     EJ_TRY(Pd.alloc(P.size(), J.s, "projection"));
     EJ_CUDA(cudaMemcpyAsync(Pd.p, P.data(), P.size() * sizeof(float), cudaMemcpyHostToDevice, J.s));
-    EJ_TRY(learned_order(Y32, bad, J.n, n_pad, J.d, Pd.p, k, J.opt.order == EJOIN_ORDER_LEAD,
-                         L.perm, &L.boxes, J.s));
+    // pmax >= max_a |P_a| (products of FP32 values are exact in FP64; the
+    // relative margin covers the summation and square-root roundings)
+    double pm = 0.0;
+    for (uint32_t a = 0; a < k; ++a) {
+        double s2 = 0.0;
+        for (uint32_t c = 0; c < J.d; ++c) s2 += (double)P[(size_t)a * J.d + c] * P[(size_t)a * J.d + c];
+        pm = std::max(pm, sqrt(s2) * (1.0 + (J.d + 4) * kU));
+    }
+    float pmax = (float)pm;
+    if ((double)pmax < pm) pmax = nextafterf(pmax, INFINITY);
+    if (!std::isfinite(pmax)) return set_error(EJOIN_EINVAL, "projection has non-finite entries");
+    EJ_TRY(learned_order(Y32, Yerr, bad, J.n, n_pad, J.d, Pd.p, k, pmax,
+                         J.opt.order == EJOIN_ORDER_LEAD, L.perm, &L.boxes, J.s));
     to.stop(J.s);
     double Tlo, Thi;
     oracle_band(J.T, J.d, &Tlo, &Thi);
@@ -366,20 +376,24 @@ static int run_screen16(Join& J, Fmt fmt, bool split, Learned& L) {
     DBuf<double> mu;
     EJ_TRY(bad.alloc(J.n, J.s, "row flags"));
     EJ_TRY(mu.alloc(J.d, J.s, "mean"));
-    double maxabs = 0;
-    uint64_t ngood = 0;
-    DBuf<float> Y32;
+    DBuf<float> Y32, Yerr;
     EJ_TRY(Y32.alloc(J.n * J.d, J.s, "FP32 centred points"));
-    EJ_TRY(launch_center_stats(J.X, J.n, J.d, bad.p, mu.p, &maxabs, &ngood, Y32.p, J.s));
+    EJ_TRY(Yerr.alloc(J.n, J.s, "centring error bounds"));
+    CenterStats cs;
+    EJ_TRY(launch_center_stats(J.X, J.n, J.d, bad.p, mu.p, Y32.p, Yerr.p, &cs, J.s));
     tp.stop(J.s);
     const double ms_center = tp.ms();
-    // The FP32 copies and the power-of-two operand scale need the centred
-    // coordinates well inside the FP32 range (the scale 1 / max|y| must be an
-    // FP32 number and max|y| must not under- or overflow in FP32).  Other data
-    // takes the (equally exact) FP64 DMMA screen.
-    if (!(maxabs == 0.0 || (maxabs > 1e-30 && maxabs < 1e30))) return run_dmma(J);
+    // The FP32 copies need the centred coordinates well inside the FP32 range:
+    // squared norms of up to 2^27 coordinates must not overflow, and the
+    // absolute error terms (2^-126 per flushed coordinate, underflow of FP32
+    // norms) must stay negligible.  Other data takes the (equally exact) FP64
+    // DMMA screen.
+    const double maxabs = cs.maxy;
+    const bool fp32_ok = !cs.range && (maxabs == 0.0 ? !cs.flushed
+                                                     : (maxabs >= 0x1p-50 && maxabs <= 0x1p50));
+    if (!fp32_ok) return run_dmma(J);
     const uint64_t n_pad = round_up(J.n, 128);
-    if (J.opt.proj_k) EJ_TRY(prepare_learned(J, Y32.p, bad.p, n_pad, L));
+    if (J.opt.proj_k) EJ_TRY(prepare_learned(J, Y32.p, Yerr.p, bad.p, n_pad, L));
     tp.start(J.s);
     ScreenParams P;
     const bool fp8 = (fmt == Fmt::E4M3);
@@ -418,11 +432,11 @@ static int run_screen16(Join& J, Fmt fmt, bool split, Learned& L) {
     if (fp8) {
         EJ_TRY(sig.alloc(n_pad, J.s, "row scales"));
         EJ_TRY(tsig.alloc(n_pad / 128, J.s, "tile scales"));
-        EJ_TRY(launch_pack8(Y32.p, J.n, n_pad, J.perm, bad.p, P, Q8.p, Aug.p, beta.p, sig.p,
-                            Xf.p, rad.p, tsig.p, J.s));
+        EJ_TRY(launch_pack8(Y32.p, Yerr.p, J.n, n_pad, J.perm, bad.p, P, Q8.p, Aug.p, beta.p,
+                            sig.p, Xf.p, rad.p, tsig.p, J.s));
     } else {
-        EJ_TRY(launch_pack16(Y32.p, J.n, n_pad, J.perm, bad.p, P, Q.p, Aug.p, beta.p, Xf.p, rad.p,
-                             J.s));
+        EJ_TRY(launch_pack16(Y32.p, Yerr.p, J.n, n_pad, J.perm, bad.p, P, Q.p, Aug.p, beta.p,
+                             Xf.p, rad.p, J.s));
     }
     EJ_TRY(launch_tile_max(beta.p, nullptr, n_pad, tmax.p, J.s));
     tp.stop(J.s);
@@ -671,11 +685,10 @@ int ejoin_train_projection(const double* points, uint64_t n, uint32_t d, double 
     DBuf<double> mu;
     EJ_TRY(bad.alloc(n, s, "row flags"));
     EJ_TRY(mu.alloc(d, s, "mean"));
-    double maxabs = 0;
-    uint64_t ngood = 0;
     DBuf<float> Y32;
     EJ_TRY(Y32.alloc(n * d, s, "FP32 centred points"));
-    EJ_TRY(launch_center_stats(X, n, d, bad.p, mu.p, &maxabs, &ngood, Y32.p, s));
+    CenterStats cs;
+    EJ_TRY(launch_center_stats(X, n, d, bad.p, mu.p, Y32.p, nullptr, &cs, s));
     TrainResult tr;
     EJ_TRY(train_projection_dev(Y32.p, bad.p, n, d, eps, opt.proj_k, opt.train_pairs,
                                 opt.train_steps, opt.seed, opt.order == EJOIN_ORDER_LEAD, s, tr));

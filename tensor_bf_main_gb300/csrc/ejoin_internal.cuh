@@ -256,9 +256,11 @@ struct TrainResult {
 int train_projection_dev(const float* Y32, const uint8_t* bad, uint64_t n, uint32_t d, double eps,
                          uint32_t k, uint64_t pairs, uint32_t steps, uint64_t seed, int lead_only,
                          cudaStream_t s, TrainResult& out);
-int learned_order(const float* Y32, const uint8_t* bad, uint64_t n, uint64_t n_pad, uint32_t d,
-                  const float* P_dev, uint32_t k, int lead_only, DBuf<uint32_t>& perm,
-                  LearnedBoxes* boxes, cudaStream_t s);
+// Yerr (centring error bounds) is required with boxes: the boxes are rigorous.
+// pmax >= max_a ||P_a||_2 (rounded up).
+int learned_order(const float* Y32, const float* Yerr, const uint8_t* bad, uint64_t n,
+                  uint64_t n_pad, uint32_t d, const float* P_dev, uint32_t k, float pmax,
+                  int lead_only, DBuf<uint32_t>& perm, LearnedBoxes* boxes, cudaStream_t s);
 // host.cpp: certified upper bound of ||P||_2
 int cert_spectral_norm(const float* P, uint32_t k, uint32_t d, double* out);
 
@@ -267,11 +269,17 @@ int launch_band_recheck2(const double* X, uint64_t n, uint32_t d, const uint32_t
                          DevStatus* st, cudaStream_t s);
 
 // k_prep.cu
-// bad[i] = 1 for rows with a non-finite coordinate; mean over the good rows
-// (deterministic two-pass sums); max |fl(x - mu)| over good rows.
-// Also writes the FP32 centred copy Y32 [n][d] when Y32 is non-null.
+// Centring statistics.  bad[i] = 1 for rows with a non-finite coordinate;
+// mu = an FP32-representable mean (of a fixed sample of rows); with Y32 the
+// FP32 centred copy [n][d] and Yerr[i] >= ||Y32_i - (x_i - mu)||_2.
+struct CenterStats {
+    double maxy = 0;       // max |Y32| over the finite rows
+    uint64_t ngood = 0;    // finite rows
+    bool range = false;    // a coordinate beyond 2^120: the FP32 copy is unusable
+    bool flushed = false;  // a nonzero coordinate below 2^-126 was replaced by 0
+};
 int launch_center_stats(const double* X, uint64_t n, uint32_t d, uint8_t* bad, double* mu,
-                        double* maxabs, uint64_t* ngood, float* Y32, cudaStream_t s);
+                        float* Y32, float* Yerr, CenterStats* out, cudaStream_t s);
 // FP64 centred copy Y[n_pad][dp] and per-row thresholds h, g for the DMMA screen.
 int launch_pack_dmma(const double* X, uint64_t n, uint64_t n_pad, const uint32_t* perm,
                      const uint8_t* bad, const double* mu, const DmmaParams& P, double* Y,
@@ -279,13 +287,13 @@ int launch_pack_dmma(const double* X, uint64_t n, uint64_t n_pad, const uint32_t
 // 16-bit operand rows [hi | lo], aug rows [augA(16) | augB(16)], per-row
 // out-margins beta, FP32 coordinates Xf ([n_pad][d], scaled, centred) and
 // their per-row error radius.
-int launch_pack16(const float* Y32, uint64_t n, uint64_t n_pad, const uint32_t* perm,
-                  const uint8_t* bad, const ScreenParams& P, void* Q, void* Aug, float* beta,
-                  float* Xf, float* rad, cudaStream_t s);
+int launch_pack16(const float* Y32, const float* Yerr, uint64_t n, uint64_t n_pad,
+                  const uint32_t* perm, const uint8_t* bad, const ScreenParams& P, void* Q,
+                  void* Aug, float* beta, float* Xf, float* rad, cudaStream_t s);
 // E4M3 operand rows with per-row power-of-two scales sigma, BF16 aug rows,
 // beta, sigma, FP32 coordinates / radii, and the per-tile minimum sigma.
-int launch_pack8(const float* Y32, uint64_t n, uint64_t n_pad, const uint32_t* perm,
-                 const uint8_t* bad, const ScreenParams& P, uint8_t* Q,
+int launch_pack8(const float* Y32, const float* Yerr, uint64_t n, uint64_t n_pad,
+                 const uint32_t* perm, const uint8_t* bad, const ScreenParams& P, uint8_t* Q,
                  void* Aug, float* beta, float* sig, float* Xf, float* rad, float* tsig,
                  cudaStream_t s);
 // per 128-row tile: max of beta (16-bit) or of meta.z (FP8), as float

@@ -47,54 +47,6 @@ __host__ __device__ __forceinline__ uint64_t splitmix64(uint64_t x) {
 
 // ------------------------------------------------------------ projection --
 
-// proj[i][a] = fl32(sum_c P[a][c] * yf[i][c]) with yf = fl32(fl64(x - mu))
-// (the FP32 centred copy), thread per point, P in shared memory.  err[i] bounds the distance from the
-// exact P (x_i - mu) in every coordinate:
-//   |yf_c - (x_c - mu_c)| <= 1.0001 * 2^-24 |yf_c| (+ 2^-149 if subnormal),
-//   FP32 fma accumulation of d terms <= (d + 2) 2^-24 sum |P yf|,
-// so err = (d + 4) 2^-24 S (1 + 2^-16) + d 2^-148, S = sum_c |P_ac| |yf_c|
-// (itself computed with upward rounding).  Projections of x - mu give the
-// same differences P(x_i - x_j) as projections of x.  Non-finite rows get NaN.
-__global__ void project_kernel(const float* __restrict__ Y32, const uint8_t* __restrict__ bad,
-                               uint64_t n, uint32_t d, const float* __restrict__ P, uint32_t k,
-                               float* proj, float* err) {
-    extern __shared__ float sP[];
-    for (uint32_t e = threadIdx.x; e < k * d; e += blockDim.x) sP[e] = P[e];
-    __syncthreads();
-    const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const float NaNf = __int_as_float(0x7fc00000);
-    if (bad[i]) {
-        for (uint32_t a = 0; a < k; ++a) proj[i * k + a] = NaNf;
-        err[i] = NaNf;
-        return;
-    }
-    const float* y = Y32 + i * d;
-    float acc[16], sabs[16];
-#pragma unroll
-    for (int a = 0; a < 16; ++a) acc[a] = sabs[a] = 0.0f;
-    for (uint32_t c = 0; c < d; ++c) {
-        const float yf = y[c];
-        const float ay = fabsf(yf);
-#pragma unroll
-        for (int a = 0; a < 16; ++a)
-            if (a < (int)k) {
-                const float pc = sP[a * d + c];
-                acc[a] = fmaf(pc, yf, acc[a]);
-                sabs[a] = __fmaf_ru(fabsf(pc), ay, sabs[a]);
-            }
-    }
-    float smax = 0.0f;
-#pragma unroll
-    for (int a = 0; a < 16; ++a)
-        if (a < (int)k) {
-            proj[i * k + a] = acc[a];
-            smax = fmaxf(smax, sabs[a]);
-        }
-    const float c1 = (float)(d + 4) * 5.9604644775390625e-08f * 1.0000153f;  // (d+4) 2^-24 (1+2^-16)
-    err[i] = __fmaf_ru(c1, smax, (float)d * 3.5873240686715317e-43f);
-}
-
 __device__ __forceinline__ uint32_t ordered_bits32(float v) {
     const uint32_t b = __float_as_uint(v);
     return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
@@ -104,35 +56,128 @@ __device__ __forceinline__ float from_ordered_bits32(uint32_t b) {
     return __uint_as_float(b);
 }
 
-__global__ void range_kernel(const float* __restrict__ proj, uint64_t n, uint32_t k,
-                             unsigned int* mn, unsigned int* mx) {
-    const uint32_t a = blockIdx.y;
-    uint32_t lo = 0xffffffffu, hi = 0u;
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
-         i += (uint64_t)gridDim.x * blockDim.x) {
-        const float v = proj[i * k + a];
-        if (!isnan(v)) {
-            const uint32_t b = ordered_bits32(v);
-            lo = min(lo, b);
-            hi = max(hi, b);
+// proj[i][a] = fl32(sum_c P[a][c] Y32[i][c]) (FP32 FMA chain, c in order);
+// with Yerr, err[i] bounds |proj[i][a] - P_a (x_i - mu)| for every a:
+//   FP32 accumulation of d terms <= (d + 2) 2^-24 sum_c |P_ac| |Y_c|
+//                                <= (d + 2) 2^-24 |P_a| |Y|   (Cauchy-Schwarz)
+//   centring error               <= |P_a| Yerr_i
+// so err = pmax ((d + 4) 2^-24 (1 + 2^-16) |Y| + Yerr_i) + d 2^-148 (rounded
+// up), pmax >= max_a |P_a| (host, rounded up).  Projections of x - mu give
+// the same differences P(x_i - x_j) as projections of x.  Non-finite rows
+// get NaN.  A persistent block stages 128 rows x 64 coordinates at a time in
+// shared memory (coalesced loads; row pitch 65: conflict-free), a thread then
+// projects one row; the block also folds the per-coordinate range of the
+// finite projections into mn / mx (order-preserving bits, one atomic each).
+constexpr uint32_t PJ_ROWS = 128, PJ_CH = 64;
+template <int K>
+__global__ void __launch_bounds__(PJ_ROWS) project_kernel(
+    const float* __restrict__ Y32, const float* __restrict__ Yerr, const uint8_t* __restrict__ bad,
+    uint64_t n, uint32_t d, const float* __restrict__ P, uint32_t k, float pmax, float* proj,
+    float* err, unsigned int* mn, unsigned int* mx) {
+    __shared__ float sY[PJ_ROWS * (PJ_CH + 1)];
+    __shared__ float sP[K * PJ_CH];
+    __shared__ unsigned int smn[4][K], smx[4][K];
+    const uint32_t t = threadIdx.x, lane = t & 31, w = t >> 5;
+    const float NaNf = __int_as_float(0x7fc00000);
+    const float c1 = (float)(d + 4) * 5.9604644775390625e-08f * 1.0000153f;  // (d+4) 2^-24 (1+2^-16)
+    uint32_t lo[K], hi[K];
+#pragma unroll
+    for (int a = 0; a < K; ++a) {
+        lo[a] = 0xffffffffu;
+        hi[a] = 0u;
+    }
+    for (uint64_t i0 = blockIdx.x * (uint64_t)PJ_ROWS; i0 < n; i0 += (uint64_t)gridDim.x * PJ_ROWS) {
+        const uint64_t i = i0 + t;
+        float acc[K];
+#pragma unroll
+        for (int a = 0; a < K; ++a) acc[a] = 0.0f;
+        float s2 = 0.0f;
+        for (uint32_t c0 = 0; c0 < d; c0 += PJ_CH) {
+            const uint32_t cw = min(PJ_CH, d - c0);
+            __syncthreads();
+            for (uint32_t e = t; e < PJ_ROWS * PJ_CH; e += PJ_ROWS) {
+                const uint32_t r = e / PJ_CH, c = e % PJ_CH;
+                sY[r * (PJ_CH + 1) + c] =
+                    (i0 + r < n && c < cw) ? Y32[(i0 + r) * d + c0 + c] : 0.0f;
+            }
+            for (uint32_t e = t; e < K * PJ_CH; e += PJ_ROWS) {
+                const uint32_t a = e / PJ_CH, c = e % PJ_CH;
+                sP[e] = (a < k && c < cw) ? P[a * d + c0 + c] : 0.0f;
+            }
+            __syncthreads();
+            const float* y = sY + t * (PJ_CH + 1);
+#pragma unroll 4
+            for (uint32_t c = 0; c < cw; ++c) {
+                const float yc = y[c];
+                s2 = __fmaf_ru(yc, yc, s2);
+#pragma unroll
+                for (int a = 0; a < K; ++a) acc[a] = fmaf(sP[a * PJ_CH + c], yc, acc[a]);
+            }
+        }
+        if (i < n) {
+            if (bad[i]) {
+                for (uint32_t a = 0; a < k; ++a) proj[i * k + a] = NaNf;
+                if (err) err[i] = NaNf;
+            } else {
+#pragma unroll
+                for (int a = 0; a < K; ++a)
+                    if (a < (int)k) {
+                        proj[i * k + a] = acc[a];
+                        const uint32_t b = ordered_bits32(acc[a]);
+                        lo[a] = min(lo[a], b);
+                        hi[a] = max(hi[a], b);
+                    }
+                if (err) {
+                    const float inner = __fmaf_ru(c1, __fsqrt_ru(s2), Yerr[i]);
+                    err[i] = __fmaf_ru(pmax, inner, (float)d * 3.5873240686715317e-43f);
+                }
+            }
         }
     }
-    for (int o = 16; o; o >>= 1) {
-        lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
-        hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
-    }
-    if ((threadIdx.x & 31) == 0) {
-        atomicMin(&mn[a], lo);
-        atomicMax(&mx[a], hi);
+#pragma unroll
+    for (int a = 0; a < K; ++a)
+        for (int o = 16; o; o >>= 1) {
+            lo[a] = min(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], o));
+            hi[a] = max(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], o));
+        }
+    if (lane == 0)
+#pragma unroll
+        for (int a = 0; a < K; ++a) {
+            smn[w][a] = lo[a];
+            smx[w][a] = hi[a];
+        }
+    __syncthreads();
+    if (t < k) {
+        uint32_t l = smn[0][t], h = smx[0][t];
+        for (int q = 1; q < (int)(PJ_ROWS / 32); ++q) {
+            l = min(l, smn[q][t]);
+            h = max(h, smx[q][t]);
+        }
+        if (l != 0xffffffffu) atomicMin(&mn[t], l);
+        if (h != 0u) atomicMax(&mx[t], h);
     }
 }
 
 // Sort keys: Morton interleave of the leading min(k, 8) coordinates quantised
 // to 64 / m bits each, or the order-preserving bits of coordinate 0.  NaN
-// rows sort last.
+// rows sort last.  The quantisation (v - lo) * (levels / span) in FP32 is
+// monotone in v, which is all the ordering needs.
 __global__ void key_kernel(const float* __restrict__ proj, uint64_t n, uint32_t k, int lead_only,
                            const unsigned int* mn, const unsigned int* mx,
                            unsigned long long* keys, uint32_t* idx) {
+    const uint32_t m = k < 8 ? k : 8;
+    const uint32_t bits = 64 / m;
+    const uint32_t qb = bits > 31 ? 31 : bits;
+    const uint32_t qmax = (1u << qb) - 1u;
+    __shared__ float slo[8], sinv[8];
+    if (threadIdx.x < m) {
+        const float lo = from_ordered_bits32(mn[threadIdx.x]);
+        const float hi = from_ordered_bits32(mx[threadIdx.x]);
+        const float span = hi - lo;
+        slo[threadIdx.x] = lo;
+        sinv[threadIdx.x] = span > 0.0f ? (float)qmax / span : 0.0f;
+    }
+    __syncthreads();
     const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
     idx[i] = (uint32_t)i;
@@ -145,19 +190,16 @@ __global__ void key_kernel(const float* __restrict__ proj, uint64_t n, uint32_t 
         keys[i] = ordered_bits32(p0);
         return;
     }
-    const uint32_t m = k < 8 ? k : 8;
-    const uint32_t bits = 64 / m;
-    const double levels = ldexp(1.0, (int)(bits > 31 ? 31 : bits)) - 1.0;
     uint32_t q[8];
-    for (uint32_t a = 0; a < m; ++a) {
-        const float lo = from_ordered_bits32(mn[a]), hi = from_ordered_bits32(mx[a]);
-        const float span = hi - lo;
-        float t = span > 0.0f ? (proj[i * k + a] - lo) / span : 0.0f;
-        t = fminf(fmaxf(t, 0.0f), 1.0f);
-        q[a] = (uint32_t)((double)t * levels);
+#pragma unroll
+    for (uint32_t a = 0; a < 8; ++a) {
+        q[a] = 0;
+        if (a < m) {
+            const float t = fmaxf((proj[i * k + a] - slo[a]) * sinv[a], 0.0f);  // NaN -> 0
+            q[a] = min(__float2uint_rz(t), qmax);
+        }
     }
     unsigned long long key = 0;
-    const uint32_t qb = bits > 31 ? 31 : bits;
     for (int b = (int)qb - 1; b >= 0; --b)
         for (uint32_t a = 0; a < m; ++a) key = (key << 1) | ((q[a] >> b) & 1u);
     keys[i] = key;
@@ -218,38 +260,48 @@ struct PairBatch {
 
 // Half uniform random pairs, half pairs close in the current order (perm);
 // differences and distances from the FP32 centred copy (training needs no
-// exactness).  Pairs with a non-finite row are inactive.
+// exactness).  Pairs with a non-finite row are inactive.  A warp builds one
+// pair at a time: lanes over coordinates (coalesced row reads and writes).
 __global__ void sample_pairs_kernel(const float* __restrict__ Y32, const uint8_t* __restrict__ bad,
                                     uint64_t n, uint32_t d, const uint32_t* __restrict__ perm,
                                     uint64_t M, uint64_t seed, double eps, uint32_t window,
                                     PairBatch pb) {
-    const uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-    if (e >= M) return;
-    const uint64_t h1 = splitmix64(seed ^ (e * 0x9E3779B97F4A7C15ull));
-    const uint64_t h2 = splitmix64(h1);
-    uint64_t i, j;
-    if (e & 1) {
-        i = h1 % n;
-        j = h2 % n;
-    } else {
-        const uint64_t t = h1 % n;
-        uint64_t u = t + 1 + (h2 % window);
-        if (u >= n) u = t >= 1 + (h2 % window) ? t - 1 - (h2 % window) : 0;
-        i = perm ? perm[t] : t;
-        j = perm ? perm[u] : u;
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t gw = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / 32;
+    const uint64_t nw = (uint64_t)gridDim.x * blockDim.x / 32;
+    const float lo = (float)(eps * 1.02), cap = (float)(2.0 * eps);
+    for (uint64_t e = gw; e < M; e += nw) {
+        const uint64_t h1 = splitmix64(seed ^ (e * 0x9E3779B97F4A7C15ull));
+        const uint64_t h2 = splitmix64(h1);
+        uint64_t i, j;
+        if (e & 1) {
+            i = h1 % n;
+            j = h2 % n;
+        } else {
+            const uint64_t t = h1 % n;
+            uint64_t u = t + 1 + (h2 % window);
+            if (u >= n) u = t >= 1 + (h2 % window) ? t - 1 - (h2 % window) : 0;
+            i = perm ? perm[t] : t;
+            j = perm ? perm[u] : u;
+        }
+        const float* a = Y32 + i * d;
+        const float* b = Y32 + j * d;
+        float* v = pb.V + e * d;
+        float s = 0.0f;
+#pragma unroll 4
+        for (uint32_t c = lane; c < d; c += 32) {
+            const float t = a[c] - b[c];
+            s = fmaf(t, t, s);
+            v[c] = t;
+        }
+        for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) {
+            const float delta = sqrtf(s);
+            float t = 0.0f;
+            if (!bad[i] && !bad[j] && delta > lo) t = fminf(delta, cap);
+            pb.tgt[e] = t;
+        }
     }
-    const float* a = Y32 + i * d;
-    const float* b = Y32 + j * d;
-    float s = 0.0f;
-    for (uint32_t c = 0; c < d; ++c) {
-        const float v = a[c] - b[c];
-        s = fmaf(v, v, s);
-        pb.V[e * d + c] = v;
-    }
-    const float delta = sqrtf(s);
-    float t = 0.0f;
-    if (!bad[i] && !bad[j] && delta > (float)(eps * 1.02)) t = fminf(delta, (float)(2.0 * eps));
-    pb.tgt[e] = t;
 }
 
 constexpr int TRAIN_THREADS = 256;
@@ -479,25 +531,32 @@ __global__ void adam_renorm_kernel(float* P, unsigned long long* G, float* m1, f
 // given, computes the boxes of the 128-row tiles and of super-blocks of
 // kSuperTiles tiles (FP32, outward rounded).  perm: sorted position ->
 // original row.
-int learned_order(const float* Y32, const uint8_t* bad, uint64_t n, uint64_t n_pad, uint32_t d,
-                  const float* P_dev, uint32_t k, int lead_only, DBuf<uint32_t>& perm,
-                  LearnedBoxes* boxes, cudaStream_t s) {
+int learned_order(const float* Y32, const float* Yerr, const uint8_t* bad, uint64_t n,
+                  uint64_t n_pad, uint32_t d, const float* P_dev, uint32_t k, float pmax,
+                  int lead_only, DBuf<uint32_t>& perm, LearnedBoxes* boxes, cudaStream_t s) {
+    if (boxes && !Yerr) return set_error(EJOIN_EINTERNAL, "learned_order: boxes need Yerr");
     DBuf<float> proj, err;
     EJ_TRY(proj.alloc(n * k, s, "projections"));
-    EJ_TRY(err.alloc(n, s, "projection error bounds"));
-    const size_t shm = (size_t)k * d * sizeof(float);
-    EJ_CUDA(cudaFuncSetAttribute(project_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
-    project_kernel<<<(unsigned)((n + 127) / 128), 128, shm, s>>>(Y32, bad, n, d, P_dev, k, proj.p,
-                                                                 err.p);
-    EJ_CUDA(cudaGetLastError());
-    note_launch();
+    if (boxes) EJ_TRY(err.alloc(n, s, "projection error bounds"));
     DBuf<unsigned int> rng;
     EJ_TRY(rng.alloc(2 * k, s, "projection ranges"));
     EJ_CUDA(cudaMemsetAsync(rng.p, 0xff, k * sizeof(unsigned int), s));
     EJ_CUDA(cudaMemsetAsync(rng.p + k, 0, k * sizeof(unsigned int), s));
-    range_kernel<<<dim3(128, k), 256, 0, s>>>(proj.p, n, k, rng.p, rng.p + k);
-    EJ_CUDA(cudaGetLastError());
-    note_launch();
+    {
+        int sms = 0, dev = 0;
+        EJ_CUDA(cudaGetDevice(&dev));
+        EJ_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        auto fn = k <= 8 ? project_kernel<8> : project_kernel<16>;
+        int per_sm = 0;
+        EJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, PJ_ROWS, 0));
+        const uint64_t tiles = (n + PJ_ROWS - 1) / PJ_ROWS;
+        const unsigned grid = (unsigned)std::max<uint64_t>(
+            1, std::min<uint64_t>(tiles, (uint64_t)sms * std::max(per_sm, 1)));
+        fn<<<grid, PJ_ROWS, 0, s>>>(Y32, boxes ? Yerr : nullptr, bad, n, d, P_dev, k, pmax, proj.p,
+                                    boxes ? err.p : nullptr, rng.p, rng.p + k);
+        EJ_CUDA(cudaGetLastError());
+        note_launch();
+    }
     DBuf<unsigned long long> keys, keys2;
     DBuf<uint32_t> idx;
     EJ_TRY(keys.alloc(n, s, "sort keys"));
@@ -578,14 +637,22 @@ int train_projection_dev(const float* Y32, const uint8_t* bad, uint64_t n, uint3
     auto step_fn = k <= 8 ? train_step_kernel<8> : train_step_kernel<16>;
     EJ_CUDA(cudaFuncSetAttribute(step_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
     const uint32_t tp = train_tile_pairs(d);
+    unsigned sample_grid = 1;
+    {
+        int sms = 0, dev = 0;
+        EJ_CUDA(cudaGetDevice(&dev));
+        EJ_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        sample_grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((M + 7) / 8, (uint64_t)sms * 8));
+    }
     // a few blocks per SM, each accumulating its partial gradient in shared memory
     const unsigned grid = (unsigned)std::min<uint64_t>((B + tp - 1) / tp, 304);
     uint32_t t_step = 0;
     uint64_t cursor = 0;
     for (uint32_t r = 0; r < rounds; ++r) {
         DBuf<uint32_t> perm;
-        EJ_TRY(learned_order(Y32, bad, n, n_pad, d, P.p, k, lead_only, perm, nullptr, s));
-        sample_pairs_kernel<<<(unsigned)((M + 255) / 256), 256, 0, s>>>(
+        EJ_TRY(learned_order(Y32, nullptr, bad, n, n_pad, d, P.p, k, 0.0f, lead_only, perm,
+                             nullptr, s));
+        sample_pairs_kernel<<<sample_grid, 256, 0, s>>>(
             Y32, bad, n, d, perm.p, M, seed + 7919ull * (r + 1), eps, 256, PairBatch{V.p, tgt.p});
         EJ_CUDA(cudaGetLastError());
         note_launch();

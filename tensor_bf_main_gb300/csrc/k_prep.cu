@@ -19,83 +19,226 @@
 #include <cuda_fp8.h>
 #include <string.h>
 
+#include <algorithm>
+
 #include "ejoin_internal.cuh"
 
 namespace ejoin {
 namespace {
 
-constexpr int ROWS_PER_BLOCK_MEAN = 1024;
+// ------------------------------------------------------------- centring --
+//
+// mu is the FP32-representable mean of up to kMeanSample rows spread evenly
+// over the data (finite values only).  Any fixed mu keeps every bound below
+// rigorous; the mean only keeps the centred magnitudes small.
+constexpr uint64_t kMeanSample = 65536;
+constexpr uint32_t kMeanRowsPerBlock = 256;
 
-__global__ void rowcheck_kernel(const double* __restrict__ X, uint64_t n, uint32_t d,
-                                uint8_t* bad, unsigned long long* ngood) {
-    const uint64_t row = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / 32;
-    const int lane = threadIdx.x & 31;
-    bool ok = true;
-    if (row < n) {
-        for (uint32_t k = lane; k < d; k += 32) ok &= isfinite(X[row * d + k]) != 0;
-    }
-    ok = __all_sync(0xffffffffu, ok);
-    if (row < n && lane == 0) bad[row] = ok ? 0 : 1;
-    // one atomic per block
-    __shared__ unsigned cnt;
-    if (threadIdx.x == 0) cnt = 0;
-    __syncthreads();
-    if (row < n && lane == 0 && ok) atomicAdd(&cnt, 1u);
-    __syncthreads();
-    if (threadIdx.x == 0 && cnt) atomicAdd(ngood, (unsigned long long)cnt);
-}
-
-// partial[b][k] = sum over good rows of block b (fixed order: deterministic)
-__global__ void colsum_partial_kernel(const double* __restrict__ X, uint64_t n, uint32_t d,
-                                      const uint8_t* __restrict__ bad, double* partial) {
-    const uint64_t r0 = blockIdx.x * (uint64_t)ROWS_PER_BLOCK_MEAN;
-    const uint64_t r1 = min(n, r0 + ROWS_PER_BLOCK_MEAN);
+__global__ void sample_colsum_kernel(const double* __restrict__ X, uint64_t n, uint32_t d,
+                                     uint64_t S, double* psum, uint32_t* pcnt) {
+    const uint64_t j0 = blockIdx.x * (uint64_t)kMeanRowsPerBlock;
+    const uint64_t j1 = min(S, j0 + kMeanRowsPerBlock);
     for (uint32_t k = threadIdx.x; k < d; k += blockDim.x) {
         double s = 0.0;
-        for (uint64_t r = r0; r < r1; ++r)
-            if (!bad[r]) s += X[r * d + k];
-        partial[blockIdx.x * (uint64_t)d + k] = s;
+        uint32_t c = 0;
+#pragma unroll 8
+        for (uint64_t j = j0; j < j1; ++j) {
+            const uint64_t row = j * n / S;  // evenly spread, increasing
+            const double v = X[row * d + k];
+            if (isfinite(v)) {
+                s += v;
+                ++c;
+            }
+        }
+        psum[blockIdx.x * (uint64_t)d + k] = s;
+        pcnt[blockIdx.x * (uint64_t)d + k] = c;
     }
 }
 
-__global__ void colsum_final_kernel(const double* __restrict__ partial, uint32_t nb, uint32_t d,
-                                    const unsigned long long* ngood, double* mu) {
-    uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+// mu_k = fl32(sum / count) in a fixed order (deterministic); 0 without data
+// or beyond 1e30 (such data leaves the FP32 path anyway).
+__global__ void sample_mean_kernel(const double* __restrict__ psum, const uint32_t* __restrict__ pcnt,
+                                   uint32_t nb, uint32_t d, double* mu, float* muf) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= d) return;
     double s = 0.0;
-    for (uint32_t b = 0; b < nb; ++b) s += partial[(uint64_t)b * d + k];
-    unsigned long long g = *ngood;
-    mu[k] = g ? s / (double)g : 0.0;
+    uint64_t c = 0;
+    for (uint32_t b = 0; b < nb; ++b) {
+        s += psum[(uint64_t)b * d + k];
+        c += pcnt[(uint64_t)b * d + k];
+    }
+    const double m = c ? s / (double)c : 0.0;
+    const float f = fabs(m) < 1e30 ? (float)m : 0.0f;
+    muf[k] = f;
+    mu[k] = (double)f;
 }
 
-// max |fl(x - mu)| over the finite rows and, when Y32 is given, the FP32
-// centred copy Y32[i][k] = fl32(fl64(x_ik - mu_k)) (0 for non-finite rows).
-// Later passes (projection, training pairs, operand packing) read Y32 instead
-// of re-centring the FP64 rows: on this GPU FP64 arithmetic is the scarce
-// resource, and every bound downstream needs only |Y32 - y| <= 2^-24 |y|
-// (+ 2^-149 for subnormal results).
-__global__ void maxabs_kernel(const double* __restrict__ X, uint64_t n, uint32_t d,
-                              const uint8_t* __restrict__ bad, const double* __restrict__ mu,
-                              unsigned long long* maxbits, float* Y32) {
-    const uint64_t row = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / 32;
-    const int lane = threadIdx.x & 31;
-    double m = 0.0;
-    if (row < n) {
-        const bool good = !bad[row];
-        for (uint32_t k = lane; k < d; k += 32) {
-            const double y = good ? __dsub_rn(X[row * d + k], mu[k]) : 0.0;
-            m = fmax(m, fabs(y));
-            if (Y32) Y32[row * d + k] = (float)y;
+constexpr uint32_t kCenterRange = 1u;  // a finite |x| >= 2^120: FP32 path unusable
+constexpr uint32_t kCenterFlush = 2u;  // a nonzero |x| < 2^-126 was replaced by 0
+
+struct CenterAcc {
+    unsigned long long ngood;
+    uint32_t maxy;  // bits of max |Y| (non-negative floats order like their bits)
+    uint32_t flags;
+};
+
+// Y = fl32(x - mu) to within  |Y - (x - mu)| <= c_rel |Y| + e  (exact real
+// x - mu, c_rel = 2^-23 (1 + 2^-23)), using integer and FP32 operations only
+// (FP64 arithmetic is scarce on this GPU).  With E the biased exponent of x:
+//  * 2^-126 <= |x| < 2^120: xf1 = x truncated to 24 significant bits (an FP32
+//    normal, built from the bit fields), rem = x - xf1 = (low 29 mantissa
+//    bits) * 2^(E-1075), |rem| < 2^-23 |x|.  If 2^(E-1075) is an FP32 normal
+//    (E >= 949), xf2 = fl32(rem) (one rounding, the power-of-two product is
+//    exact); otherwise xf2 = 0.  a = fl32(xf1 - mu), Y = fl32(a + xf2).
+//    Round-to-nearest gives |Y - (a + xf2)| <= u|Y| + 2^-150,
+//    |a - (xf1 - mu)| <= u|a|, |a| <= (1 + u)|Y| + 2^-150 + |xf2|, hence
+//      xf2 kept:    e = 2^-46 (1 + 2^-20) |xf1| + 2^-148
+//      xf2 dropped: e = |rem| <= 2^-23 (1 + 2^-22) |xf1|  (a = Y exactly)
+//  * |x| < 2^-126: x is replaced by 0, Y = -mu exactly, e = 2^-126.
+//  * |x| >= 2^120 (finite): flagged; the caller leaves the FP32 path.
+__device__ __forceinline__ float center_coord(double x, float mu, float& e, uint32_t& flags,
+                                              bool& finite) {
+    const uint32_t hi = (uint32_t)__double2hiint(x), lo = (uint32_t)__double2loint(x);
+    const uint32_t E = (hi >> 20) & 0x7ffu;
+    const uint32_t sgn = hi & 0x80000000u;
+    finite = E != 0x7ffu;
+    float xf1 = 0.0f, xf2 = 0.0f;
+    e = 0.0f;
+    if (E >= 897u && E <= 1142u) {
+        xf1 = __uint_as_float(sgn | ((E - 896u) << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29));
+        if (E >= 949u) {
+            xf2 = __fmul_rn(__uint2float_rn(lo & 0x1fffffffu), __uint_as_float((E - 948u) << 23));
+            xf2 = __uint_as_float(__float_as_uint(xf2) | sgn);
+            e = __fmaf_ru(fabsf(xf1), 1.4210854715202004e-14f * 1.00000095367431640625f,
+                          3.5873240686715317e-43f);  // 2^-46 (1 + 2^-20), 2^-148
+        } else {
+            e = __fmul_ru(fabsf(xf1), 1.1920928955078125e-07f * 1.0000002384185791f);  // 2^-23 (1 + 2^-22)
+        }
+    } else if (E <= 896u) {
+        if ((hi & 0x7fffffffu) | lo) {
+            e = 1.1754943508222875e-38f;  // 2^-126
+            flags |= kCenterFlush;
+        }
+    } else if (finite) {
+        flags |= kCenterRange;
+    }
+    return __fadd_rn(__fsub_rn(xf1, mu), xf2);
+}
+
+// One pass over X: bad[i] (a non-finite coordinate), Y32 = the FP32 centred
+// copy (0 for bad rows), Yerr[i] >= ||Y32_i - (x_i - mu)||_2 (rounded up:
+// c_rel ||Y32_i|| + sum of the per-coordinate e), and the global maximum of
+// |Y32| over good rows, their count and the range flags.  A warp handles
+// ROWS rows per step with all loads issued first (VEC = 2: 16-byte loads of
+// coordinate pairs, d even); without Y32 only bad and the count are written.
+template <int VEC, int ROWS>
+__global__ void __launch_bounds__(256) center_kernel(const double* __restrict__ X, uint64_t n,
+                                                     uint32_t d, const float* __restrict__ muf,
+                                                     uint8_t* __restrict__ bad,
+                                                     float* __restrict__ Y32,
+                                                     float* __restrict__ Yerr, CenterAcc* acc) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t gw = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / 32;
+    const uint64_t nw = (uint64_t)gridDim.x * blockDim.x / 32;
+    const uint32_t nv = d / VEC;  // vectors per row
+    float my = 0.0f;
+    uint32_t fl = 0, ng = 0;
+    for (uint64_t r0 = gw * ROWS; r0 < n; r0 += nw * ROWS) {
+        bool fin[ROWS];
+        float s2[ROWS], se[ROWS], rmax[ROWS];
+        uint32_t rfl[ROWS];
+#pragma unroll
+        for (int r = 0; r < ROWS; ++r) {
+            fin[r] = true;
+            s2[r] = se[r] = rmax[r] = 0.0f;
+            rfl[r] = 0;
+        }
+        for (uint32_t v0 = 0; v0 < nv; v0 += 32) {
+            const uint32_t v = v0 + lane;
+            double xv[ROWS][VEC];
+#pragma unroll
+            for (int r = 0; r < ROWS; ++r) {
+                const bool ok = r0 + r < n && v < nv;
+                if (VEC == 2) {
+                    const double2 t = ok ? reinterpret_cast<const double2*>(X + (r0 + r) * d)[v]
+                                         : make_double2(0.0, 0.0);
+                    xv[r][0] = t.x;
+                    xv[r][VEC - 1] = t.y;
+                } else {
+                    xv[r][0] = ok ? X[(r0 + r) * d + v] : 0.0;
+                }
+            }
+            if (v >= nv) continue;
+#pragma unroll
+            for (int r = 0; r < ROWS; ++r) {
+                if (r0 + r >= n) continue;
+                float y[VEC];
+#pragma unroll
+                for (int c = 0; c < VEC; ++c) {
+                    float e;
+                    bool f;
+                    y[c] = center_coord(xv[r][c], muf[v * VEC + c], e, rfl[r], f);
+                    fin[r] &= f;
+                    s2[r] = __fmaf_ru(y[c], y[c], s2[r]);
+                    se[r] = __fadd_ru(se[r], e);
+                    rmax[r] = fmaxf(rmax[r], fabsf(y[c]));
+                }
+                if (Y32) {
+                    float* yr = Y32 + (r0 + r) * d;
+                    if (VEC == 2) reinterpret_cast<float2*>(yr)[v] = make_float2(y[0], y[VEC - 1]);
+                    else yr[v] = y[0];
+                }
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < ROWS; ++r) {
+            const uint64_t row = r0 + r;
+            if (row >= n) continue;  // warp-uniform
+            const bool good = __all_sync(0xffffffffu, fin[r]);
+            float a = s2[r], b = se[r];
+            for (int o = 16; o; o >>= 1) {
+                a = __fadd_ru(a, __shfl_xor_sync(0xffffffffu, a, o));
+                b = __fadd_ru(b, __shfl_xor_sync(0xffffffffu, b, o));
+            }
+            if (good) {
+                my = fmaxf(my, rmax[r]);
+                fl |= rfl[r];
+                ng += lane == 0;
+            } else if (Y32) {
+                for (uint32_t k = lane; k < d; k += 32) Y32[row * d + k] = 0.0f;
+            }
+            if (lane == 0) {
+                bad[row] = good ? 0 : 1;
+                if (Yerr)
+                    Yerr[row] = good ? __fmaf_ru(1.1920930376163766e-07f, __fsqrt_ru(a), b) : 0.0f;
+            }
         }
     }
-    for (int o = 16; o; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-    // one atomic per block (non-negative doubles order like their bit patterns)
-    __shared__ unsigned long long bm;
-    if (threadIdx.x == 0) bm = 0;
+    // block-level merge, one set of atomics per block
+    for (int o = 16; o; o >>= 1) {
+        my = fmaxf(my, __shfl_xor_sync(0xffffffffu, my, o));
+        fl |= __shfl_xor_sync(0xffffffffu, fl, o);
+        ng += __shfl_xor_sync(0xffffffffu, ng, o);
+    }
+    __shared__ float smy[8];
+    __shared__ uint32_t sfl[8], sng[8];
+    const uint32_t w = threadIdx.x / 32;
+    if (lane == 0) {
+        smy[w] = my;
+        sfl[w] = fl;
+        sng[w] = ng;
+    }
     __syncthreads();
-    if (lane == 0 && m > 0.0) atomicMax(&bm, (unsigned long long)__double_as_longlong(m));
-    __syncthreads();
-    if (threadIdx.x == 0 && bm) atomicMax(maxbits, bm);
+    if (threadIdx.x == 0) {
+        for (uint32_t i = 1; i < blockDim.x / 32; ++i) {
+            my = fmaxf(my, smy[i]);
+            fl |= sfl[i];
+            ng += sng[i];
+        }
+        if (ng) atomicAdd(&acc->ngood, (unsigned long long)ng);
+        if (my > 0.0f) atomicMax(&acc->maxy, __float_as_uint(my));
+        if (fl) atomicOr(&acc->flags, fl);
+    }
 }
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -207,19 +350,32 @@ __device__ __forceinline__ float round_fmt_f(float v, int fbits, float min_norma
     return fabsf(r) < min_normal ? 0.0f : r;
 }
 
+// Squared norm of q accumulated in FP32 (round to nearest): each term passes
+// through at most ceil(dp / 32) lane-chain FMAs and 5 shuffle-tree additions,
+// so |computed - exact| <= gamma * exact + (dp + 160) 2^-149 (underflow), with
+// gamma = (ceil(dp / 32) + 6) 2^-24 (1.01 covers gamma_m's denominator).
+struct NormBound {
+    double rel, abs;
+};
+__device__ __forceinline__ NormBound fp32_norm_bound(uint32_t dp) {
+    return {((dp + 31) / 32 + 6) * 5.9604644775390625e-08 * 1.01, (dp + 160) * 1.4012984643248171e-45};
+}
+
 // A warp packs 32 consecutive rows.  Phase 1 (lanes over coordinates, one row
-// at a time): z = s * fl64(x - mu) (exact scaling), zf = fl32(z),
-// hi = round(zf), lo = round(zf - hi) (split), ef = zf - hi - lo; every
-// FP32 subtraction here is exact, and the residual z - q = (z - zf) + ef with
-// |z - zf| <= 2^-24 |z|.  Per row: nq = |q|^2 in FP64, and in FP32 rounded
-// up: |zf|^2, |ef|^2, |(|hi| + |lo|)|^2, |lo|^2.  The FP32 coordinates zf and
-// a per-row radius go to Xf / rad for the FP32 band pre-check.  Phase 2 (lane
-// = row): the FP64 threshold arithmetic (alpha, beta), the aug slab.
+// at a time): z = s * Y32 (exact power-of-two scaling of the FP32 centred
+// copy), hi = round(z), lo = round(z - hi) (split), ef = z - hi - lo; every
+// FP32 subtraction here is exact.  The residual to the exact centred point is
+// (Yerr_i s, from the centring pass) + |ef| (+ 2^-126 per flushed coordinate).
+// Per row: nq = |q|^2 (FP32, bounded by fp32_norm_bound) and in FP32 rounded
+// up: |ef|^2, |(|hi| + |lo|)|^2, |lo|^2.  The FP32 coordinates z and a per-row
+// radius go to Xf / rad for the FP32 band pre-check.  Phase 2 (lane = row):
+// the FP64 threshold arithmetic (alpha, beta), the aug slab.
 template <Fmt F>
 __global__ void __launch_bounds__(256) pack16_kernel(const float* __restrict__ Y32, uint64_t n,
                                                      uint64_t n_pad,
                                                      const uint32_t* __restrict__ perm,
-                                                     const uint8_t* __restrict__ bad, ScreenParams P,
+                                                     const uint8_t* __restrict__ bad,
+                                                     const float* __restrict__ Yerr, ScreenParams P,
                                                      uint16_t* Q, uint16_t* Aug, float* beta,
                                                      float* Xf, float* rad) {
     const uint64_t p0 = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / 32 * 32;
@@ -228,16 +384,15 @@ __global__ void __launch_bounds__(256) pack16_kernel(const float* __restrict__ Y
     const FmtInfo fi = fmt_info(F);
     const float mnf = (float)fi.min_normal;
     const float sf = (float)P.scale;
-    float m_z2 = 0, m_e2 = 0, m_a2 = 0, m_l2 = 0;
-    double m_nq = 0;
+    float m_nq = 0, m_e2 = 0, m_a2 = 0, m_l2 = 0;
+    uint64_t m_src = 0;
     bool m_good = false;
     for (uint32_t r = 0; r < 32; ++r) {
         const uint64_t p = p0 + r;
         const uint64_t src = p < n ? (perm ? perm[p] : p) : 0;
         const bool good = p < n && !bad[src];
         uint16_t* row = Q + p * (uint64_t)P.width;
-        float z2 = 0, e2 = 0, a2 = 0, l2 = 0;
-        double nq = 0;
+        float nq = 0, e2 = 0, a2 = 0, l2 = 0;
         for (uint32_t k = lane; k < P.dp; k += 32) {
             float hi = 0.0f, lo = 0.0f, zf = 0.0f;
             if (good && k < P.d) {
@@ -249,10 +404,9 @@ __global__ void __launch_bounds__(256) pack16_kernel(const float* __restrict__ Y
                     lo = round_fmt_f(ef, fi.fbits, mnf);
                     ef = ef - lo;  // exact
                 }
-                const double q = (double)(hi + lo);  // hi + lo exact in FP32
-                nq = __fma_rn(q, q, nq);
+                const float q = hi + lo;  // exact
+                nq = __fmaf_rn(q, q, nq);
                 const float aq = fabsf(hi) + fabsf(lo);  // exact
-                z2 = __fmaf_ru(zf, zf, z2);
                 e2 = __fmaf_ru(ef, ef, e2);
                 a2 = __fmaf_ru(aq, aq, a2);
                 l2 = __fmaf_ru(lo, lo, l2);
@@ -262,18 +416,17 @@ __global__ void __launch_bounds__(256) pack16_kernel(const float* __restrict__ Y
             if (k < P.d) Xf[p * P.d + k] = zf;
         }
         for (int o = 16; o; o >>= 1) {
-            nq += __shfl_xor_sync(0xffffffffu, nq, o);
-            z2 = __fadd_ru(z2, __shfl_xor_sync(0xffffffffu, z2, o));
+            nq = __fadd_rn(nq, __shfl_xor_sync(0xffffffffu, nq, o));
             e2 = __fadd_ru(e2, __shfl_xor_sync(0xffffffffu, e2, o));
             a2 = __fadd_ru(a2, __shfl_xor_sync(0xffffffffu, a2, o));
             l2 = __fadd_ru(l2, __shfl_xor_sync(0xffffffffu, l2, o));
         }
         if (lane == r) {
             m_nq = nq;
-            m_z2 = z2;
             m_e2 = e2;
             m_a2 = a2;
             m_l2 = l2;
+            m_src = src;
             m_good = good;
         }
     }
@@ -283,15 +436,14 @@ __global__ void __launch_bounds__(256) pack16_kernel(const float* __restrict__ Y
     double b = 0.0;
     float radius = INFINITY;  // bad and padding rows: the FP32 pre-check never decides
     if (m_good) {
-        const double gs = (P.d + 4) * kU;
-        const double nup = m_nq * (1 + gs), ndn = m_nq * (1 - gs);
+        const NormBound nb = fp32_norm_bound(P.dp);
+        const double nup = (double)m_nq * (1 + nb.rel) + nb.abs;
+        const double ndn = (double)m_nq * (1 - nb.rel) - nb.abs;
         const double a2u = (double)m_a2, lu = (double)m_l2;
-        const double zn = sqrt((double)m_z2) * (1 + 1e-7);  // >= |zf|; |z| <= |zf| (1 + 2^-24)
-        // |z - q| <= |z - zf| + |ef|, plus the centring error u |z|
-        // FP32 rounding of z (relative 2^-24, subnormal 2^-149 before scaling) or
-        // flush of values below 2^-126, plus the FP64 centring error u |z|
-        const double zerr = (5.9604645e-08 + 2.0 * kU) * zn * 1.0001 +
-                            (1.18e-38 + 1.41e-45 * P.scale) * sqrt((double)P.d);
+        // distance of the FP32 coordinates from the exact scaled centred point:
+        // the centring bound (exact scaling) plus values flushed below 2^-126
+        const double zerr = ((double)__ldg(&Yerr[m_src]) * P.scale +
+                             1.1754943508222875e-38 * sqrt((double)P.d)) * (1 + 4 * kU);
         const double rho = (sqrt((double)m_e2) * (1 + 1e-7) + zerr) * (1 + 8 * kU);
         radius = __double2float_ru(zerr);
         double R = nup + P.cacc * a2u + lu + P.absacc - 0.5 * P.Tlo + 2.0 * P.sTlo * rho;
@@ -357,15 +509,16 @@ constexpr int PACK8_MAXV = 32;  // coordinates per lane: d <= 1024
 __global__ void __launch_bounds__(256) pack8_kernel(const float* __restrict__ Y32, uint64_t n,
                                                     uint64_t n_pad,
                                                     const uint32_t* __restrict__ perm,
-                                                    const uint8_t* __restrict__ bad, ScreenParams P,
+                                                    const uint8_t* __restrict__ bad,
+                                                    const float* __restrict__ Yerr, ScreenParams P,
                                                     uint8_t* Q, uint16_t* Aug, float* beta,
                                                     float* sig, float* Xf, float* rad) {
     const uint64_t p0 = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / 32 * 32;
     const uint32_t lane = threadIdx.x & 31;
     if (p0 >= n_pad) return;
     const float mnf = 0.015625f;  // E4M3 smallest normal 2^-6
-    float m_z2 = 0, m_e2 = 0, m_sig = 1.0f;
-    double m_nq = 0;
+    float m_nq = 0, m_e2 = 0, m_sig = 1.0f;
+    uint64_t m_src = 0;
     bool m_good = false;
     for (uint32_t r = 0; r < 32; ++r) {
         const uint64_t p = p0 + r;
@@ -393,8 +546,7 @@ __global__ void __launch_bounds__(256) pack8_kernel(const float* __restrict__ Y3
             sgm = ldexpf(1.0f, e);
         }
         const float inv = 1.0f / sgm;  // exact (power of two)
-        float z2 = 0, e2 = 0;
-        double nq = 0;
+        float nq = 0, e2 = 0;
         uint8_t* row = Q + p * (uint64_t)P.width;
 #pragma unroll
         for (int t = 0; t < PACK8_MAXV; ++t) {
@@ -404,22 +556,19 @@ __global__ void __launch_bounds__(256) pack8_kernel(const float* __restrict__ Y3
             const float f = round_fmt_f(zf * inv, 3, mnf);
             const float q = f * sgm;        // exact
             const float ef = zf - q;        // exact
-            const double qd = (double)q;
-            nq = __fma_rn(qd, qd, nq);
-            z2 = __fmaf_ru(zf, zf, z2);
+            nq = __fmaf_rn(q, q, nq);
             e2 = __fmaf_ru(ef, ef, e2);
             row[k] = (uint8_t)__nv_cvt_float_to_fp8(f, __NV_SATFINITE, __NV_E4M3);
             if (k < P.d) Xf[p * P.d + k] = zf;
         }
         for (int o = 16; o; o >>= 1) {
-            nq += __shfl_xor_sync(0xffffffffu, nq, o);
-            z2 = __fadd_ru(z2, __shfl_xor_sync(0xffffffffu, z2, o));
+            nq = __fadd_rn(nq, __shfl_xor_sync(0xffffffffu, nq, o));
             e2 = __fadd_ru(e2, __shfl_xor_sync(0xffffffffu, e2, o));
         }
         if (lane == r) {
             m_nq = nq;
-            m_z2 = z2;
             m_e2 = e2;
+            m_src = src;
             m_sig = sgm;
             m_good = good;
         }
@@ -431,12 +580,12 @@ __global__ void __launch_bounds__(256) pack8_kernel(const float* __restrict__ Y3
     double b = 0.0, rsig = 1.0;
     float radius = INFINITY;
     if (m_good) {
-        const double gs = (P.d + 4) * kU;
-        const double nup = m_nq * (1 + gs), ndn = m_nq * (1 - gs);
+        const NormBound nb = fp32_norm_bound(P.dp);
+        const double nup = (double)m_nq * (1 + nb.rel) + nb.abs;
+        const double ndn = (double)m_nq * (1 - nb.rel) - nb.abs;
         const double a2u = nup;  // |(|q|)|^2 = |q|^2
-        const double zn = sqrt((double)m_z2) * (1 + 1e-7);
-        const double zerr = (5.9604645e-08 + 2.0 * kU) * zn * 1.0001 +
-                            (1.18e-38 + 1.41e-45 * P.scale) * sqrt((double)P.d);
+        const double zerr = ((double)__ldg(&Yerr[m_src]) * P.scale +
+                             1.1754943508222875e-38 * sqrt((double)P.d)) * (1 + 4 * kU);
         const double rho = (sqrt((double)m_e2) * (1 + 1e-7) + zerr) * (1 + 8 * kU);
         radius = __double2float_ru(zerr);
         double R = nup + P.cacc * a2u + P.absacc - 0.5 * P.Tlo + 2.0 * P.sTlo * rho;
@@ -528,33 +677,54 @@ __global__ void tile_max_kernel(const float* __restrict__ beta, const float4* __
 }  // namespace
 
 int launch_center_stats(const double* X, uint64_t n, uint32_t d, uint8_t* bad, double* mu,
-                        double* maxabs, uint64_t* ngood_host, float* Y32, cudaStream_t s) {
-    DBuf<unsigned long long> cnt;
-    EJ_TRY(cnt.alloc(2, s, "center stats"));
-    EJ_TRY(cnt.zero(s));
-    const uint64_t warps_blocks = (n * 32 + 255) / 256;
-    rowcheck_kernel<<<(unsigned)warps_blocks, 256, 0, s>>>(X, n, d, bad, cnt.p);
-    EJ_CUDA(cudaGetLastError());
-    note_launch();
-    const uint32_t nb = (uint32_t)((n + ROWS_PER_BLOCK_MEAN - 1) / ROWS_PER_BLOCK_MEAN);
-    DBuf<double> part;
-    EJ_TRY(part.alloc((size_t)nb * d, s, "column partial sums"));
-    colsum_partial_kernel<<<nb, 128, 0, s>>>(X, n, d, bad, part.p);
-    EJ_CUDA(cudaGetLastError());
-    note_launch();
-    colsum_final_kernel<<<(d + 127) / 128, 128, 0, s>>>(part.p, nb, d, cnt.p, mu);
-    EJ_CUDA(cudaGetLastError());
-    note_launch();
-    maxabs_kernel<<<(unsigned)warps_blocks, 256, 0, s>>>(X, n, d, bad, mu, cnt.p + 1, Y32);
-    EJ_CUDA(cudaGetLastError());
-    note_launch();
-    unsigned long long h[2];
-    EJ_CUDA(cudaMemcpyAsync(h, cnt.p, sizeof h, cudaMemcpyDeviceToHost, s));
+                        float* Y32, float* Yerr, CenterStats* out, cudaStream_t s) {
+    *out = CenterStats{};
+    DBuf<float> muf;
+    EJ_TRY(muf.alloc(d, s, "FP32 mean"));
+    const uint64_t S = std::min<uint64_t>(n, kMeanSample);
+    const uint32_t nb = (uint32_t)((S + kMeanRowsPerBlock - 1) / kMeanRowsPerBlock);
+    if (nb) {
+        DBuf<double> psum;
+        DBuf<uint32_t> pcnt;
+        EJ_TRY(psum.alloc((size_t)nb * d, s, "sample column sums"));
+        EJ_TRY(pcnt.alloc((size_t)nb * d, s, "sample column counts"));
+        sample_colsum_kernel<<<nb, 128, 0, s>>>(X, n, d, S, psum.p, pcnt.p);
+        EJ_CUDA(cudaGetLastError());
+        sample_mean_kernel<<<(d + 127) / 128, 128, 0, s>>>(psum.p, pcnt.p, nb, d, mu, muf.p);
+        EJ_CUDA(cudaGetLastError());
+        note_launch(2);
+    } else {
+        EJ_TRY(muf.zero(s));
+        EJ_CUDA(cudaMemsetAsync(mu, 0, d * sizeof(double), s));
+    }
+    DBuf<CenterAcc> acc;
+    EJ_TRY(acc.alloc(1, s, "centring totals"));
+    EJ_TRY(acc.zero(s));
+    if (n) {
+        int sms = 0, dev = 0;
+        EJ_CUDA(cudaGetDevice(&dev));
+        EJ_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        // one wave of resident blocks (8 warps, 4 rows per warp step)
+        const bool vec = (d % 2 == 0) && (((uintptr_t)X & 15) == 0);
+        auto fn = vec ? center_kernel<2, 4> : center_kernel<1, 4>;
+        int per_sm = 0;
+        EJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 256, 0));
+        const uint64_t want = (n + 31) / 32;
+        const unsigned grid = (unsigned)std::max<uint64_t>(
+            1, std::min<uint64_t>(want, (uint64_t)sms * std::max(per_sm, 1)));
+        fn<<<grid, 256, 0, s>>>(X, n, d, muf.p, bad, Y32, Yerr, acc.p);
+        EJ_CUDA(cudaGetLastError());
+        note_launch();
+    }
+    CenterAcc h;
+    EJ_CUDA(cudaMemcpyAsync(&h, acc.p, sizeof h, cudaMemcpyDeviceToHost, s));
     EJ_CUDA(cudaStreamSynchronize(s));
-    *ngood_host = h[0];
-    double m;
-    memcpy(&m, &h[1], sizeof m);
-    *maxabs = m;
+    float my;
+    memcpy(&my, &h.maxy, sizeof my);
+    out->maxy = (double)my;
+    out->ngood = h.ngood;
+    out->range = (h.flags & kCenterRange) != 0;
+    out->flushed = (h.flags & kCenterFlush) != 0;
     return EJOIN_OK;
 }
 
@@ -568,18 +738,18 @@ int launch_pack_dmma(const double* X, uint64_t n, uint64_t n_pad, const uint32_t
     return EJOIN_OK;
 }
 
-int launch_pack16(const float* Y32, uint64_t n, uint64_t n_pad, const uint32_t* perm,
-                  const uint8_t* bad, const ScreenParams& P, void* Q, void* Aug, float* beta,
-                  float* Xf, float* rad, cudaStream_t s) {
+int launch_pack16(const float* Y32, const float* Yerr, uint64_t n, uint64_t n_pad,
+                  const uint32_t* perm, const uint8_t* bad, const ScreenParams& P, void* Q,
+                  void* Aug, float* beta, float* Xf, float* rad, cudaStream_t s) {
     if (n_pad % 32) return set_error(EJOIN_EINTERNAL, "pack16: rows not padded");
     const uint64_t blocks = (n_pad + 255) / 256;  // 8 warps x 32 rows per block
     if (P.fmt == Fmt::BF16)
-        pack16_kernel<Fmt::BF16><<<(unsigned)blocks, 256, 0, s>>>(Y32, n, n_pad, perm, bad, P,
-                                                                  (uint16_t*)Q, (uint16_t*)Aug,
+        pack16_kernel<Fmt::BF16><<<(unsigned)blocks, 256, 0, s>>>(Y32, n, n_pad, perm, bad, Yerr,
+                                                                  P, (uint16_t*)Q, (uint16_t*)Aug,
                                                                   beta, Xf, rad);
     else if (P.fmt == Fmt::FP16)
-        pack16_kernel<Fmt::FP16><<<(unsigned)blocks, 256, 0, s>>>(Y32, n, n_pad, perm, bad, P,
-                                                                  (uint16_t*)Q, (uint16_t*)Aug,
+        pack16_kernel<Fmt::FP16><<<(unsigned)blocks, 256, 0, s>>>(Y32, n, n_pad, perm, bad, Yerr,
+                                                                  P, (uint16_t*)Q, (uint16_t*)Aug,
                                                                   beta, Xf, rad);
     else
         return set_error(EJOIN_EINTERNAL, "pack16: bad format");
@@ -588,14 +758,14 @@ int launch_pack16(const float* Y32, uint64_t n, uint64_t n_pad, const uint32_t* 
     return EJOIN_OK;
 }
 
-int launch_pack8(const float* Y32, uint64_t n, uint64_t n_pad, const uint32_t* perm,
-                 const uint8_t* bad, const ScreenParams& P, uint8_t* Q,
+int launch_pack8(const float* Y32, const float* Yerr, uint64_t n, uint64_t n_pad,
+                 const uint32_t* perm, const uint8_t* bad, const ScreenParams& P, uint8_t* Q,
                  void* Aug, float* beta, float* sig, float* Xf, float* rad, float* tsig,
                  cudaStream_t s) {
     if (n_pad % 128) return set_error(EJOIN_EINTERNAL, "pack8: rows not padded");
     if (P.d > 32u * PACK8_MAXV) return set_error(EJOIN_EUNSUPPORTED, "FP8 screen supports d <= %d", 32 * PACK8_MAXV);
-    pack8_kernel<<<(unsigned)((n_pad + 255) / 256), 256, 0, s>>>(Y32, n, n_pad, perm, bad, P, Q,
-                                                                 (uint16_t*)Aug, beta, sig, Xf, rad);
+    pack8_kernel<<<(unsigned)((n_pad + 255) / 256), 256, 0, s>>>(Y32, n, n_pad, perm, bad, Yerr, P,
+                                                                 Q, (uint16_t*)Aug, beta, sig, Xf, rad);
     EJ_CUDA(cudaGetLastError());
     note_launch();
     tile_min_sigma_kernel<<<(unsigned)(n_pad / 128), 128, 0, s>>>(sig, n_pad / 128, tsig);
