@@ -105,6 +105,10 @@ typedef struct ejoin_stats {
     double ms_recheck;          /* FP64 band recheck */
     double gram_flops;          /* MMA (or FP64) flops executed by the Gram kernel */
     uint64_t kernel_launches;   /* CUDA kernels this call launched */
+    /* reserved[0]: band pairs the FP32 pre-check left to the exact FP64 chain;
+       reserved[1]: 128 x 256 blocks the tensor-core Gram kernel computed
+       (each covers up to two of the tile_pairs_run 128 x 128 tile pairs);
+       ejoin_train_projection: reserved[0] / [1] = first / last hinge loss. */
     double reserved[5];
 } ejoin_stats;
 

@@ -94,6 +94,8 @@ class Stats(ctypes.Structure):
     def as_dict(self) -> dict:
         d = {name: getattr(self, name) for name, _ in self._fields_ if name != "reserved"}
         d["precision"] = Precision.NAMES.get(d["precision"], d["precision"])
+        d["exact_rechecks"] = int(self.reserved[0])
+        d["gram_blocks"] = int(self.reserved[1])
         return d
 
 

@@ -196,10 +196,13 @@ static uint64_t band_budget(uint64_t want) {
 }
 
 // Runs `screen` (which fills counts and the band queue), re-running it with a
-// larger queue on overflow, then `recheck` resolves the band exactly.
+// larger queue on overflow, then `recheck` resolves the band exactly.  The
+// queue holds `unit` BandPair-sized words per entry: pairs (unit 1) or band
+// records (unit 2, with the pair count in DevStatus::band_pairs); capacities
+// are in pairs.
 template <typename Screen, typename Recheck>
 static int screen_and_recheck(Join& J, uint64_t cap0, Screen&& screen, Recheck&& recheck,
-                              uint64_t n_pad, EventTimer& tg, EventTimer& tr) {
+                              uint64_t n_pad, EventTimer& tg, EventTimer& tr, uint32_t unit = 1) {
     DBuf<BandPair> band;
     DBuf<DevStatus> dst;
     EJ_TRY(dst.alloc(1, J.s, "status"));
@@ -209,20 +212,21 @@ static int screen_and_recheck(Join& J, uint64_t cap0, Screen&& screen, Recheck&&
         EJ_TRY(dst.zero(J.s));
         EJ_CUDA(cudaMemsetAsync(J.counts, 0, n_pad * sizeof(int32_t), J.s));
         tg.start(J.s);
-        EJ_TRY(screen(band.p, cap, dst.p));
+        EJ_TRY(screen(band.p, cap / unit, dst.p));
         tg.stop(J.s);
         DevStatus h;
         EJ_CUDA(cudaMemcpyAsync(&h, dst.p, sizeof h, cudaMemcpyDeviceToHost, J.s));
         EJ_CUDA(cudaStreamSynchronize(J.s));
         if (h.timeout)
             return set_error(EJOIN_ETIMEOUT, "Gram kernel: a bounded device wait expired (site %u)", h.where);
-        if (h.band_count <= cap) {
+        if (h.band_count <= cap / unit) {
+            const uint64_t pairs = unit == 1 ? h.band_count : h.band_pairs;
             tr.start(J.s);
-            EJ_TRY(recheck(band.p, h.band_count, dst.p));
+            EJ_TRY(recheck(band.p, h.band_count, pairs, dst.p));
             tr.stop(J.s);
             EJ_CUDA(cudaMemcpyAsync(&h, dst.p, sizeof h, cudaMemcpyDeviceToHost, J.s));
             EJ_CUDA(cudaStreamSynchronize(J.s));
-            J.st->band_pairs = h.band_count;
+            J.st->band_pairs = pairs;
             J.st->band_hits = h.band_hits;
             J.st->reserved[0] = (double)h.exact_rechecks;
             J.st->ms_gram = tg.ms();
@@ -230,7 +234,7 @@ static int screen_and_recheck(Join& J, uint64_t cap0, Screen&& screen, Recheck&&
             return EJOIN_OK;
         }
         J.st->band_overflows++;
-        const uint64_t want = h.band_count + h.band_count / 16 + 1024;
+        const uint64_t want = (h.band_count + h.band_count / 16 + 1024) * unit;
         const uint64_t got = band_budget(want);
         if (got < want || attempt >= 3)
             return set_error(EJOIN_ENOMEM, "band queue needs %llu entries; device memory allows %llu",
@@ -284,7 +288,7 @@ static int run_dmma(Join& J) {
     auto screen = [&](BandPair* band, uint64_t cap, DevStatus* st) {
         return launch_dmma_join(Y.p, n_pad, P.dp, h.p, g.p, J.counts, band, cap, st, J.s);
     };
-    auto recheck = [&](const BandPair* band, uint64_t nb, DevStatus* st) {
+    auto recheck = [&](const BandPair* band, uint64_t nb, uint64_t, DevStatus* st) {
         return launch_band_recheck(J.X, J.n, J.d, J.perm, J.T, band, nb, J.counts, st, J.s);
     };
     return screen_and_recheck(J, std::max<uint64_t>(1u << 20, J.n), screen, recheck, n_pad, tg, tr);
@@ -392,7 +396,8 @@ static int run_screen16(Join& J, Fmt fmt, bool split, Learned& L) {
     const bool fp32_ok = !cs.range && (maxabs == 0.0 ? !cs.flushed
                                                      : (maxabs >= 0x1p-50 && maxabs <= 0x1p50));
     if (!fp32_ok) return run_dmma(J);
-    const uint64_t n_pad = round_up(J.n, 128);
+    // rows padded to whole 128 x 256 blocks of the Gram kernel
+    const uint64_t n_pad = round_up(J.n, 256);
     if (J.opt.proj_k) EJ_TRY(prepare_learned(J, Y32.p, Yerr.p, bad.p, n_pad, L));
     tp.start(J.s);
     ScreenParams P;
@@ -446,18 +451,21 @@ static int run_screen16(Join& J, Fmt fmt, bool split, Learned& L) {
     uint64_t nwork = 0;
     EventTimer tw;
     tw.start(J.s);
-    EJ_TRY(build_worklist(nT, L.k ? &L.boxes : nullptr, L.thr, work, &nwork, J.s));
+    uint64_t ntiles = 0;
+    const uint64_t nTa = (J.n + 127) / 128;
+    EJ_TRY(build_worklist(nT, nTa, L.k ? &L.boxes : nullptr, L.thr, work, &nwork, &ntiles, J.s));
     tw.stop(J.s);
     J.st->ms_order += tw.ms();
-    J.st->tile_pairs_total = nT * (nT + 1) / 2;
-    J.st->tile_pairs_run = nwork;
-    J.st->gram_flops = 2.0 * kprod * 128.0 * 128.0 * (double)nwork;
+    J.st->tile_pairs_total = nTa * (nTa + 1) / 2;
+    J.st->tile_pairs_run = ntiles;
+    J.st->reserved[1] = (double)nwork;
+    J.st->gram_flops = 2.0 * kprod * 128.0 * 256.0 * (double)nwork;
     J.st->precision = fp8 ? EJOIN_FP8_E4M3
                           : (fmt == Fmt::FP16 ? EJOIN_FP16 : (split ? EJOIN_BF16_SPLIT : EJOIN_BF16));
     const void* Qp = fp8 ? (const void*)Q8.p : (const void*)Q.p;
     auto screen = [&](BandPair* band, uint64_t cap, DevStatus* st) {
-        return launch_gram16(Qp, Aug.p, n_pad, P, work.p, nwork, tmax.p, tsig.p, J.counts, band,
-                             cap, st, J.sms, J.s);
+        return launch_gram16(Qp, Aug.p, n_pad, P, work.p, nwork, tmax.p, tsig.p, J.counts,
+                             reinterpret_cast<BandRec*>(band), cap, st, J.sms, J.s);
     };
     Recheck32 R;
     R.Xf = Xf.p;
@@ -466,13 +474,20 @@ static int run_screen16(Join& J, Fmt fmt, bool split, Learned& L) {
     R.sThi = P.sThi;
     R.c32 = (J.d + 8) * ldexp(1.0, -24) * 1.01;
     R.abs32 = (J.d + 8) * ldexp(1.0, -148);
-    auto recheck = [&](const BandPair* band, uint64_t nb, DevStatus* st) {
-        return launch_band_recheck2(J.X, J.n, J.d, J.perm, J.T, R, band, nb, J.counts, st, J.s);
+    // band records -> pairs, then the FP32 pre-check / exact FP64 recheck
+    auto recheck = [&](const BandPair* band, uint64_t nrec, uint64_t npairs, DevStatus* st) {
+        if (npairs == 0) return EJOIN_OK;
+        DBuf<BandPair> pairs;
+        EJ_TRY(pairs.alloc(npairs, J.s, "band pairs"));
+        EJ_TRY(launch_band_expand(reinterpret_cast<const BandRec*>(band), nrec, pairs.p, npairs,
+                                  J.s));
+        return launch_band_recheck2(J.X, J.n, J.d, J.perm, J.T, R, pairs.p, npairs, J.counts, st,
+                                    J.s);
     };
-    // generous first queue (8 B per entry, capped at a quarter of free memory
-    // by band_budget): an overflow re-runs the whole screen
+    // generous first queue (capped at a quarter of free memory by
+    // band_budget): an overflow re-runs the whole screen
     const uint64_t cap0 = std::max<uint64_t>(1u << 22, 512 * J.n);
-    return screen_and_recheck(J, cap0, screen, recheck, n_pad, tg, tr);
+    return screen_and_recheck(J, cap0, screen, recheck, n_pad, tg, tr, 2);
 }
 
 // AUTO (measured on GB300 over the benchmark shapes): FP16's 11-bit
@@ -532,7 +547,7 @@ static int self_join_impl(const double* points, uint64_t n, uint32_t d, double e
     DBuf<double> xbuf;
     DBuf<int32_t> cbuf;
     Learned learned;  // owns J.perm when the learned ordering is used
-    const uint64_t n_pad = round_up(std::max<uint64_t>(n, 1), 128);
+    const uint64_t n_pad = round_up(std::max<uint64_t>(n, 1), 256);  // padded rows of every screen
     EJ_TRY(cbuf.alloc(n_pad, s, "counts"));
     EJ_TRY(cbuf.zero(s));
     J.counts = cbuf.p;

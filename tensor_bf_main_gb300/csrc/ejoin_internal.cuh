@@ -110,11 +110,23 @@ struct BandPair {
 };
 constexpr uint32_t kBandBoth = 0x80000000u;
 
+// Band record of the tensor-core screen: the pairs (i, j0 + c) for every set
+// bit c of mask (j0 carries kBandBoth like BandPair::j).  One record per row
+// of a 32 x 32 chunk with band pairs: the screen's epilogue writes a row's
+// bit mask instead of expanding it (launch_band_expand does that later).
+struct BandRec {
+    uint32_t i;
+    uint32_t j0;
+    uint32_t mask;
+    uint32_t pad;
+};
+
 // Status word written by kernels whose waits are bounded.
 struct DevStatus {
     unsigned int timeout;    // a bounded wait expired (where: code below)
     unsigned int where;
-    unsigned long long band_count;  // band pairs produced (may exceed capacity)
+    unsigned long long band_count;  // band queue entries produced (may exceed capacity)
+    unsigned long long band_pairs;  // pairs in those entries (record queues)
     unsigned long long band_hits;
     unsigned long long exact_rechecks;  // band pairs the FP32 pre-check left to FP64
 };
@@ -233,15 +245,17 @@ int launch_dmma_join(const double* Y, uint64_t n_pad, uint32_t dp, const double*
 // (FP8 operands: also the per-tile minimum row scale tsig.)
 int launch_gram16(const void* Q, const void* aug, uint64_t n_pad, const ScreenParams& P,
                   const uint2* work, uint64_t nwork, const float* tmax, const float* tsig,
-                  int32_t* counts, BandPair* band, uint64_t band_cap, DevStatus* st, int num_sms,
+                  int32_t* counts, BandRec* band, uint64_t band_cap, DevStatus* st, int num_sms,
                   cudaStream_t s);
 
 // k_misc.cu
-// Ordered list of the upper-triangle 128-row tile pairs (I <= J), grouped by
-// super-block pairs; with `boxes`, pairs whose squared box gap exceeds thr
-// are dropped (super-block pairs first).
-int build_worklist(uint64_t nT, const LearnedBoxes* boxes, float thr, DBuf<uint2>& work,
-                   uint64_t* nwork_out, cudaStream_t s);
+// Ordered list of 128 x 256 blocks (row tile I, column tiles 2p, 2p+1)
+// covering the upper-triangle tile pairs (I <= J < nTa), grouped by
+// super-block pairs; entry = (I, p | active-half mask << 30).  With `boxes`,
+// tile pairs whose squared box gap exceeds thr are inactive (super-block
+// pairs are dropped first).  ntiles_out: active 128 x 128 tile pairs.
+int build_worklist(uint64_t nT, uint64_t nTa, const LearnedBoxes* boxes, float thr,
+                   DBuf<uint2>& work, uint64_t* nwork_out, uint64_t* ntiles_out, cudaStream_t s);
 int sum_counts(const int32_t* counts, uint64_t n, unsigned long long* dev_total, cudaStream_t s);
 int scatter_counts(const int32_t* src, const uint32_t* perm, uint64_t n, int32_t* dst,
                    cudaStream_t s);
@@ -264,6 +278,9 @@ int learned_order(const float* Y32, const float* Yerr, const uint8_t* bad, uint6
 // host.cpp: certified upper bound of ||P||_2
 int cert_spectral_norm(const float* P, uint32_t k, uint32_t d, double* out);
 
+// Expands band records into pairs (any order); out holds Sum popc(mask).
+int launch_band_expand(const BandRec* rec, uint64_t nrec, BandPair* out, uint64_t cap,
+                       cudaStream_t s);
 int launch_band_recheck2(const double* X, uint64_t n, uint32_t d, const uint32_t* perm, double T,
                          const Recheck32& R, const BandPair* band, uint64_t nband, int32_t* counts,
                          DevStatus* st, cudaStream_t s);

@@ -1,11 +1,12 @@
 // k_misc.cu -- tile-pair work lists, totals and count scatter.
 //
-// Work list: the upper-triangle 128x128 tile pairs (I <= J) in a blocked
-// order -- super-blocks of SB x SB tile pairs, super-blocks in row-major
-// triangular order -- so that the CTAs running concurrently touch a few MB of
-// operand rows that stay resident in L2.  The list is built by ordered
-// stream compaction over the candidate index space; the same pass drops tile
-// pairs the learned projection proves empty (see k_learn.cu for the bound).
+// Work list: blocks of one 128-row tile I x two 128-column tiles (2p, 2p+1)
+// covering the upper-triangle tile pairs (I <= J), in a blocked order --
+// super-blocks of SB x SB tiles, super-blocks in row-major triangular order
+// -- so that the CTAs running concurrently touch a few MB of operand rows
+// that stay resident in L2.  Each entry carries a 2-bit mask of its active
+// halves (J = 2p + h in the upper triangle, below the last data tile, and not
+// proven empty by the learned projection; see k_learn.cu for the bound).
 #include <cub/cub.cuh>
 
 #include "ejoin_internal.cuh"
@@ -59,41 +60,84 @@ __global__ void superpairs_kernel(uint64_t nS, BoxArgs b, uint32_t* out, unsigne
     if (keep) out[base + __popc(m & ((1u << lane) - 1u))] = (uint32_t)sp;
 }
 
-// One block of SB*SB threads per surviving super-block pair: its tile pairs
-// (I <= J, in range, not proven empty) in row-major order.
-__global__ void __launch_bounds__(SB * SB) expand_kernel(const uint32_t* __restrict__ sps,
-                                                         uint64_t nT, uint64_t nS, BoxArgs b,
-                                                         uint2* out, unsigned long long* count) {
+// One block of SB * SB / 2 threads per surviving super-block pair: its
+// (I, column pair) blocks with at least one active half, in row-major order.
+// count[0] += blocks, count[1] += active halves (128x128 tile pairs).
+constexpr uint32_t EXPAND_THREADS = SB * SB / 2;
+__global__ void __launch_bounds__(EXPAND_THREADS) expand_kernel(const uint32_t* __restrict__ sps,
+                                                                uint64_t nTa, uint64_t nS, BoxArgs b,
+                                                                uint2* out,
+                                                                unsigned long long* count) {
     __shared__ uint64_t sSI, sSJ;
-    __shared__ unsigned wsum[SB * SB / 32];
+    __shared__ unsigned wsum[EXPAND_THREADS / 32];
+    __shared__ unsigned hsum;
     __shared__ unsigned long long sbase;
     if (threadIdx.x == 0) {
         uint64_t SI, SJ;
         tri_decode(sps[blockIdx.x], nS, SI, SJ);
         sSI = SI;
         sSJ = SJ;
+        hsum = 0;
     }
     __syncthreads();
-    const uint64_t I = sSI * SB + threadIdx.x / SB, J = sSJ * SB + threadIdx.x % SB;
-    bool keep = I < nT && J < nT && I <= J;
-    if (keep && b.lo) keep = !boxes_far(b.lo, b.hi, I, J, b.k, b.thr);
+    const uint64_t I = sSI * SB + threadIdx.x / (SB / 2);
+    const uint64_t p = sSJ * (SB / 2) + threadIdx.x % (SB / 2);
+    uint32_t mask = 0;
+    for (uint32_t h = 0; h < 2; ++h) {
+        const uint64_t J = 2 * p + h;
+        bool act = I < nTa && J < nTa && I <= J;
+        if (act && b.lo) act = !boxes_far(b.lo, b.hi, I, J, b.k, b.thr);
+        mask |= act ? (1u << h) : 0u;
+    }
+    const bool keep = mask != 0;
     const unsigned m = __ballot_sync(0xffffffffu, keep);
     const unsigned lane = threadIdx.x & 31, wid = threadIdx.x / 32;
     if (lane == 0) wsum[wid] = __popc(m);
+    const unsigned halves = __reduce_add_sync(0xffffffffu, __popc(mask));
+    if (lane == 0 && halves) atomicAdd(&hsum, halves);
     __syncthreads();
     if (threadIdx.x == 0) {
         unsigned tot = 0;
-        for (unsigned w = 0; w < SB * SB / 32; ++w) {
+        for (unsigned w = 0; w < EXPAND_THREADS / 32; ++w) {
             const unsigned c = wsum[w];
             wsum[w] = tot;
             tot += c;
         }
-        sbase = tot ? atomicAdd(count, (unsigned long long)tot) : 0ull;
+        sbase = tot ? atomicAdd(&count[0], (unsigned long long)tot) : 0ull;
+        if (hsum) atomicAdd(&count[1], (unsigned long long)hsum);
     }
     __syncthreads();
     if (keep)
         out[sbase + wsum[wid] + __popc(m & ((1u << lane) - 1u))] =
-            make_uint2((uint32_t)I, (uint32_t)J);
+            make_uint2((uint32_t)I, (uint32_t)p | (mask << 30));
+}
+
+// Band records -> pairs: a thread per record; block-level exclusive scan of
+// the popcounts, one global reservation per block.
+constexpr uint32_t EXPAND_BAND_THREADS = 256;
+__global__ void __launch_bounds__(EXPAND_BAND_THREADS) band_expand_kernel(
+    const BandRec* __restrict__ rec, uint64_t nrec, BandPair* out, uint64_t cap,
+    unsigned long long* cursor) {
+    using Scan = cub::BlockScan<uint32_t, EXPAND_BAND_THREADS>;
+    __shared__ typename Scan::TempStorage tmp;
+    __shared__ unsigned long long sbase;
+    const uint64_t e = blockIdx.x * (uint64_t)EXPAND_BAND_THREADS + threadIdx.x;
+    BandRec r{0, 0, 0, 0};
+    if (e < nrec) r = rec[e];
+    const uint32_t cnt = __popc(r.mask);
+    uint32_t off = 0, total = 0;
+    Scan(tmp).ExclusiveSum(cnt, off, total);
+    if (threadIdx.x == 0) sbase = total ? atomicAdd(cursor, (unsigned long long)total) : 0ull;
+    __syncthreads();
+    uint64_t o = sbase + off;
+    uint32_t m = r.mask;
+    const uint32_t flag = r.j0 & kBandBoth, j0 = r.j0 & ~kBandBoth;
+    while (m) {
+        const uint32_t c = __ffs(m) - 1;
+        m &= m - 1;
+        if (o < cap) out[o] = BandPair{r.i, (j0 + c) | flag};
+        ++o;
+    }
 }
 
 __global__ void sum_counts_kernel(const int32_t* counts, uint64_t n, unsigned long long* total) {
@@ -113,12 +157,15 @@ __global__ void scatter_counts_kernel(const int32_t* src, const uint32_t* perm, 
 
 }  // namespace
 
-// Builds the list of surviving tile pairs: super-block pairs first (one
-// thread each), then the tile pairs of the survivors (one block each).
-int build_worklist(uint64_t nT, const LearnedBoxes* boxes, float thr, DBuf<uint2>& work,
-                   uint64_t* nwork_out, cudaStream_t s) {
+// Builds the list of surviving blocks: super-block pairs first (one thread
+// each), then the blocks of the survivors (one thread block each).  nT: row
+// tiles (even); nTa: tiles holding data rows.
+int build_worklist(uint64_t nT, uint64_t nTa, const LearnedBoxes* boxes, float thr,
+                   DBuf<uint2>& work, uint64_t* nwork_out, uint64_t* ntiles_out, cudaStream_t s) {
     *nwork_out = 0;
+    *ntiles_out = 0;
     if (nT == 0) return EJOIN_OK;
+    if (nT % 2 || nTa > nT) return set_error(EJOIN_EINTERNAL, "work list: odd tile count");
     const uint64_t nS = (nT + SB - 1) / SB;
     const uint64_t nsp = nS * (nS + 1) / 2;
     if (nsp > 0xffffffffull) return set_error(EJOIN_EUNSUPPORTED, "work list too large");
@@ -127,7 +174,7 @@ int build_worklist(uint64_t nT, const LearnedBoxes* boxes, float thr, DBuf<uint2
     DBuf<uint32_t> sps;
     DBuf<unsigned long long> cnt;
     EJ_TRY(sps.alloc(nsp, s, "super-block pairs"));
-    EJ_TRY(cnt.alloc(2, s, "work-list counters"));
+    EJ_TRY(cnt.alloc(3, s, "work-list counters"));
     EJ_TRY(cnt.zero(s));
     superpairs_kernel<<<(unsigned)((nsp + 255) / 256), 256, 0, s>>>(nS, b, sps.p, cnt.p);
     EJ_CUDA(cudaGetLastError());
@@ -135,7 +182,7 @@ int build_worklist(uint64_t nT, const LearnedBoxes* boxes, float thr, DBuf<uint2
     unsigned long long nkeep = 0;
     EJ_CUDA(cudaMemcpyAsync(&nkeep, cnt.p, sizeof nkeep, cudaMemcpyDeviceToHost, s));
     EJ_CUDA(cudaStreamSynchronize(s));
-    EJ_TRY(work.alloc(nkeep ? nkeep * SB * SB : 1, s, "work list"));
+    EJ_TRY(work.alloc(nkeep ? nkeep * EXPAND_THREADS : 1, s, "work list"));
     if (nkeep) {
         if (nkeep > 0x7fffffffull) return set_error(EJOIN_EUNSUPPORTED, "work list too large");
         // back into triangular (row-major) order: consecutive work then shares row blocks
@@ -147,14 +194,29 @@ int build_worklist(uint64_t nT, const LearnedBoxes* boxes, float thr, DBuf<uint2
         EJ_TRY(tmp.alloc(tb, s, "sort scratch"));
         EJ_CUDA(cub::DeviceRadixSort::SortKeys(tmp.p, tb, sps.p, sorted.p, (int)nkeep, 0, 32, s));
         note_launch(4);
-        expand_kernel<<<(unsigned)nkeep, SB * SB, 0, s>>>(sorted.p, nT, nS, b, work.p, cnt.p + 1);
+        expand_kernel<<<(unsigned)nkeep, EXPAND_THREADS, 0, s>>>(sorted.p, nTa, nS, b, work.p,
+                                                                 cnt.p + 1);
         EJ_CUDA(cudaGetLastError());
         note_launch();
     }
-    unsigned long long total = 0;
-    EJ_CUDA(cudaMemcpyAsync(&total, cnt.p + 1, sizeof total, cudaMemcpyDeviceToHost, s));
+    unsigned long long tot[2] = {0, 0};
+    EJ_CUDA(cudaMemcpyAsync(tot, cnt.p + 1, sizeof tot, cudaMemcpyDeviceToHost, s));
     EJ_CUDA(cudaStreamSynchronize(s));
-    *nwork_out = total;
+    *nwork_out = tot[0];
+    *ntiles_out = tot[1];
+    return EJOIN_OK;
+}
+
+int launch_band_expand(const BandRec* rec, uint64_t nrec, BandPair* out, uint64_t cap,
+                       cudaStream_t s) {
+    if (nrec == 0) return EJOIN_OK;
+    DBuf<unsigned long long> cur;
+    EJ_TRY(cur.alloc(1, s, "band cursor"));
+    EJ_TRY(cur.zero(s));
+    band_expand_kernel<<<(unsigned)((nrec + EXPAND_BAND_THREADS - 1) / EXPAND_BAND_THREADS),
+                         EXPAND_BAND_THREADS, 0, s>>>(rec, nrec, out, cap, cur.p);
+    EJ_CUDA(cudaGetLastError());
+    note_launch();
     return EJOIN_OK;
 }
 

@@ -1,4 +1,4 @@
-// k_umma.cu -- the tcgen05 Gram screen (EJOIN_BF16 / BF16_SPLIT / FP16).
+// k_umma.cu -- the tcgen05 Gram screen (EJOIN_BF16 / BF16_SPLIT / FP16 / FP8_E4M3).
 //
 // Re-designs the reference's main tensor path,
 // distanceCalculationBruteForceTensorHalf (kernel_join.cu:328-524): there a
@@ -7,24 +7,35 @@
 // query norms in scalar code and bumps one global counter per hit with
 // sqrt(|d2|) <= eps.  Here:
 //
-//  * A persistent CTA per SM walks a list of 128x128 tile pairs (I <= J, the
-//    upper triangle only).  Warp 0 streams K-slabs of both row blocks into a
-//    6-stage shared-memory ring with TMA (128-byte swizzle).  One thread of
-//    warp 1 issues tcgen05.mma (M=128, N=128, K=16 per instruction) into one
-//    of two FP32 accumulators in tensor memory, so the next tile's MMAs run
-//    while 8 epilogue warps read the previous one.
-//  * Operand rows are [hi | lo | aug] (k_prep.cu).  With the hi+lo split the
-//    MMAs form hi*hi + hi*lo + lo*hi.  The aug slab adds -alpha_i - alpha_j,
-//    so the accumulator holds C_ij = q_i.q_j - alpha_i - alpha_j and the
-//    rigorous screen is a sign test:
+//  * A persistent CTA per SM walks a list of blocks of 128 rows (row tile I)
+//    x 256 columns (column tiles 2p, 2p+1), taking runs of consecutive list
+//    entries.  Each 128x128 half carries an "active" bit: it lies in the
+//    upper triangle (2p + h >= I) and was not pruned; inactive halves are
+//    computed but ignored.  N = 256 per MMA instruction: on GB300 a
+//    tcgen05.mma of 128x256x16 takes about as long to issue and retire as
+//    one of 128x128x16 (measured: 1.8 vs 0.92 PFLOP/s through the same TMA /
+//    MMA pipeline), so the wide tile doubles the tensor-pipe throughput.
+//  * Warp 0 streams the K-slabs of both blocks into a 4-stage ring with TMA
+//    (128-byte swizzle; a 128-row A slab and a 256-row B slab per stage; the
+//    aug boxes of a block go to a separate 2-slot ring).  Four stages in
+//    flight are what the hi+lo MMA sequence needs to reach the tensor-pipe
+//    peak (measured: 1.77 PFLOP/s with 4, 1.33 with 3).
+//    One thread of warp 1 issues tcgen05.mma (M=128, N=256, K=16 per
+//    instruction) into one of two FP32 accumulators of 256 tensor-memory
+//    columns each, so the next block's MMAs run while 16 epilogue warps read
+//    the previous one.
+//  * Operand rows are [hi | lo] (k_prep.cu) with a separate 16-element aug
+//    row (32-byte swizzle).  With the hi+lo split the MMAs form hi*hi + hi*lo
+//    + lo*hi.  The aug MMA adds -alpha_i - alpha_j, so the accumulator holds
+//    C_ij = q_i.q_j - alpha_i - alpha_j and the rigorous screen is a sign test:
 //        C >= 0          pair certainly within eps        (counted)
 //        C < -W_IJ       pair certainly outside eps
 //        otherwise       band: queued for the FP64 recheck
 //    W_IJ = max beta over tile I + max beta over tile J.
 //  * The epilogue packs sign bits with one funnel shift per element, counts
-//    rows with popc, transposes the 32x32 bit block across the warp to count
-//    columns (off-diagonal tiles credit both points), and flushes per-point
-//    counts once per tile.  No distance ever reaches global memory.
+//    rows with popc, transposes 32x32 bit blocks across the warp to count
+//    columns (off-diagonal tiles credit both points), and a flusher warp adds
+//    the per-block counts to global memory.  No distance reaches global memory.
 //
 // Every wait is bounded (umma_ptx.cuh); on expiry all roles stop, in-flight
 // copies and MMAs are drained (bounded) and tensor memory is freed.
@@ -34,19 +45,27 @@
 namespace ejoin {
 namespace {
 
-constexpr int NST = 5;                      // smem ring stages
-constexpr int SLAB_BYTES = 128 * 128;       // 128 rows x 128 bytes
-constexpr int AUG_BYTES = 128 * 32;         // 128 rows x 32 bytes (16 elements)
-// A slab | B slab | A aug | B aug; the aug boxes are loaded with the first
-// slab of every tile only
-constexpr int STAGE_BYTES = 2 * SLAB_BYTES + 2 * AUG_BYTES;
-constexpr uint32_t DATA_TX = 2 * SLAB_BYTES;
-constexpr uint32_t FIRST_TX = 2 * SLAB_BYTES + 2 * AUG_BYTES;
+constexpr int SLAB_A = 128 * 128;  // 128 rows x 128 bytes
+constexpr int SLAB_B = 256 * 128;  // 256 rows x 128 bytes
+constexpr int AUG_A = 128 * 32;    // 128 rows x 32 bytes (16 elements)
+constexpr int AUG_B = 256 * 32;
+// stage: A slab | B slab; aug slot: A aug | B aug (one per block); every part
+// starts on a 1024-byte boundary
+constexpr int STAGE_BYTES = SLAB_A + SLAB_B;
+constexpr int NST = 4;
+constexpr int AUG_SLOT = AUG_A + AUG_B;
+constexpr int NAUG = 2;
+constexpr uint32_t DATA_TX = SLAB_A + SLAB_B;
 constexpr int NUM_EPI_WARPS = 16;          // 4 per SM sub-partition (latency hiding)
-constexpr int FLUSH_WARP = 2 + NUM_EPI_WARPS;  // adds the per-tile counts to global memory
+constexpr int FLUSH_WARP = 2 + NUM_EPI_WARPS;  // adds the per-block counts to global memory
 constexpr int NTHREADS = (3 + NUM_EPI_WARPS) * 32;
-constexpr uint32_t TMEM_COLS = 256;         // two 128x128 FP32 accumulators
+constexpr uint32_t ACC_COLS = 256;         // one 128x256 FP32 accumulator
+constexpr uint32_t TMEM_COLS = 2 * ACC_COLS;
 constexpr uint32_t FULL = 0xffffffffu;
+
+// Work-list entry: x = row tile I; y = column pair p | active mask << 30
+// (bit h: the 128x128 half with column tile 2p + h is computed).
+constexpr uint32_t kPairMask = (1u << 30) - 1u;
 
 struct GramArgs {
     const uint2* work;
@@ -54,42 +73,47 @@ struct GramArgs {
     const float* tmax;
     const float* tsig;  // FP8: per-tile minimum row scale (null for 16-bit operands)
     int32_t* counts;
-    BandPair* band;
+    BandRec* band;
     uint64_t band_cap;
     DevStatus* st;
-    uint32_t nhi;    // 64-element data slabs per part
+    uint32_t nhi;    // data slabs (128-byte rows) per part
     uint32_t split;  // hi + lo
     uint32_t fmt;    // 16-bit operands: 0 = FP16, 1 = BF16 (instruction-descriptor format)
+    uint32_t lrun;   // log2 of the run length: entries a CTA takes consecutively
 };
 
-// Band width of tile pair (I, J): beta_i + beta_j <= W (Gram units; FP8
-// operands: divided by sigma_I sigma_J, the accumulator's unit).  The sum is
-// rounded up by the 2^-20 relative margin; division by the power-of-two
-// scales is exact.
-__device__ __forceinline__ float band_width(const GramArgs& a, uint2 w) {
-    const float s = __ldg(&a.tmax[w.x]) + __ldg(&a.tmax[w.y]);
-    float W = fmaf(fabsf(s), 9.5367431640625e-07f, s);
-    if (a.tsig) W = W / (__ldg(&a.tsig[w.x]) * __ldg(&a.tsig[w.y]));
-    return W;
+__device__ __forceinline__ uint2 entry_or_end(const GramArgs& a, uint64_t u) {
+    return u < a.nwork ? __ldg(&a.work[u]) : make_uint2(0xffffffffu, 0xffffffffu);
 }
 
-constexpr uint32_t BAND_SMEM = 1024;  // staged band entries per accumulator buffer
-constexpr uint32_t BAND_SKIP = 0xffffffffu;  // staged slot not used (recheck skips i >= n)
+// Entry idx (0, 1, 2, ...) of this CTA's sequence: runs of 2^lrun consecutive
+// work-list entries, runs dealt round-robin over the CTAs (so the CTAs
+// running at the same time stay within a window of the list that shares
+// operand rows in L2).  Increasing in idx.
+__device__ __forceinline__ uint64_t item_at(uint64_t idx, uint32_t lrun) {
+    const uint64_t k = idx >> lrun, r = idx & ((1ull << lrun) - 1ull);
+    return ((k * gridDim.x + blockIdx.x) << lrun) + r;
+}
+
+constexpr uint32_t BAND_SMEM = 192;   // staged band records per count buffer
 
 struct Ctl {
     uint64_t full[NST], empty[NST];
+    uint64_t gfull[NAUG], gempty[NAUG];  // aug slots
     uint64_t tfull[2], tempty[2];
     uint64_t ebar[2];   // epilogue warps done with the counts of buffer b
     uint64_t fdone[2];  // flusher done with (and cleared) the counts of buffer b
     uint64_t fin;
     uint32_t tmem_base;
     int rowacc[2][128];
-    int colacc[2][128];
+    int colacc[2][256];
     uint32_t band_n[2];                  // band entries staged for buffer b
-    BandPair band_buf[2][BAND_SMEM];     // staged band entries (flushed by the flusher warp)
+    BandRec band_buf[2][BAND_SMEM];      // staged band records (flushed by the flusher warp)
 };
 
-constexpr size_t SMEM_BYTES = 1024 + (size_t)NST * STAGE_BYTES + sizeof(Ctl);
+constexpr size_t RING_BYTES = (size_t)NST * STAGE_BYTES + (size_t)NAUG * AUG_SLOT;
+constexpr size_t SMEM_BYTES = 1024 + RING_BYTES + sizeof(Ctl);
+static_assert(SMEM_BYTES <= 232448, "shared memory budget");
 
 // 32x32 bit-matrix transpose across the warp: lane r holds row r (bit c =
 // column c); afterwards lane c holds column c (bit r = row r).
@@ -105,8 +129,8 @@ __device__ __forceinline__ uint32_t transpose32(uint32_t x, uint32_t lane) {
     return x;
 }
 
-// Element offset of K-slab `step` of a tile: [hi0, lo0, hi1, lo1, ...] with the
-// split, [hi0, hi1, ...] without.
+// Element offset of K-slab `step` of a block: [hi0, lo0, hi1, lo1, ...] with
+// the split, [hi0, hi1, ...] without.
 template <int OPK>
 __device__ __forceinline__ uint32_t slab_x(uint32_t step, uint32_t nhi, uint32_t split) {
     constexpr uint32_t E = OPK ? 128u : 64u;  // elements per 128-byte slab row
@@ -114,16 +138,80 @@ __device__ __forceinline__ uint32_t slab_x(uint32_t step, uint32_t nhi, uint32_t
     return E * step;
 }
 
+// In / band bit masks of one 32 x 32 chunk (lane = row, v[c] = column c).
+// Fast path: if max + W < 0 over the chunk, every pair in it is certainly out
+// (rounding of the FP32 add is monotone, so max + W >= 0 whenever any
+// element is >= -W).
+__device__ __forceinline__ bool classify(const uint32_t (&v)[32], float W, uint32_t& inm,
+                                         uint32_t& bandm) {
+    float m8[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+        m8[j] = fmaxf(fmaxf(__uint_as_float(v[j]), __uint_as_float(v[j + 8])),
+                      fmaxf(__uint_as_float(v[j + 16]), __uint_as_float(v[j + 24])));
+    const float mx = fmaxf(fmaxf(fmaxf(m8[0], m8[1]), fmaxf(m8[2], m8[3])),
+                           fmaxf(fmaxf(m8[4], m8[5]), fmaxf(m8[6], m8[7])));
+    inm = bandm = 0;
+    if (!__any_sync(FULL, mx + W >= 0.0f)) return false;
+    // sign bits, four independent 8-column chains
+    uint32_t ng[4] = {0, 0, 0, 0}, nw[4] = {0, 0, 0, 0};
+#pragma unroll
+    for (int c = 7; c >= 0; --c)
+#pragma unroll
+        for (int g = 0; g < 4; ++g) {
+            const uint32_t x = v[8 * g + c];
+            ng[g] = __funnelshift_l(x, ng[g], 1);
+            nw[g] = __funnelshift_l(__float_as_uint(__uint_as_float(x) + W), nw[g], 1);
+        }
+    const uint32_t neg = ng[0] | (ng[1] << 8) | (ng[2] << 16) | (ng[3] << 24);
+    const uint32_t negw = nw[0] | (nw[1] << 8) | (nw[2] << 16) | (nw[3] << 24);
+    inm = ~neg;
+    bandm = neg & ~negw;
+    return true;
+}
+
+// Band records of the two chunks of a warp: a lane with band pairs in a chunk
+// writes one record (its row, the chunk's first column, the bit mask).  Slots
+// come from one shared-memory reservation per warp (ranks from ballots);
+// records beyond the staging area go to global memory directly.
+__device__ __forceinline__ void stage_band(const GramArgs& a, Ctl& S, uint32_t b, uint32_t bd0,
+                                           uint32_t bd1, uint32_t row, uint32_t col0, bool diag,
+                                           uint32_t lane) {
+    const uint32_t b0 = __ballot_sync(FULL, bd0 != 0), b1 = __ballot_sync(FULL, bd1 != 0);
+    const uint32_t n0 = __popc(b0);
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(&S.band_n[b], n0 + __popc(b1));
+    base = __shfl_sync(FULL, base, 0);
+    const uint32_t lt = (1u << lane) - 1u;
+    const uint32_t flag = diag ? 0u : kBandBoth;
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        const uint32_t m = k ? bd1 : bd0;
+        if (!m) continue;
+        const uint32_t slot = base + (k ? n0 + __popc(b1 & lt) : __popc(b0 & lt));
+        const BandRec r{row, (col0 + 32u * k) | flag, m, 0u};
+        if (slot < BAND_SMEM) {
+            S.band_buf[b][slot] = r;
+        } else {
+            const unsigned long long g = atomicAdd(&a.st->band_count, 1ull);
+            atomicAdd(&a.st->band_pairs, (unsigned long long)__popc(m));
+            if (g < a.band_cap) a.band[g] = r;
+        }
+    }
+}
+
 // OPK 0: 16-bit operands, data MMAs kind::f16; OPK 1: E4M3 operands, data
 // MMAs kind::f8f6f4 (K = 32 per instruction, same 32-byte k-steps), the aug
 // MMA stays kind::f16 in BF16 and accumulates into the same tensor memory.
 template <int OPK>
 __global__ void __launch_bounds__(NTHREADS, 1)
-    gram_kernel(const __grid_constant__ CUtensorMap tq, const __grid_constant__ CUtensorMap taug,
+    gram_kernel(const __grid_constant__ CUtensorMap tqa, const __grid_constant__ CUtensorMap tqb,
+                const __grid_constant__ CUtensorMap taa, const __grid_constant__ CUtensorMap tab,
                 const GramArgs a) {
     extern __shared__ uint8_t smraw[];
     uint8_t* stages = (uint8_t*)(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
-    Ctl& S = *reinterpret_cast<Ctl*>(stages + (size_t)NST * STAGE_BYTES);
+    uint8_t* augs = stages + (size_t)NST * STAGE_BYTES;
+    Ctl& S = *reinterpret_cast<Ctl*>(stages + RING_BYTES);
     const uint32_t warp = threadIdx.x / 32, lane = threadIdx.x & 31;
 
     if (warp == 1) {
@@ -135,6 +223,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             ptx::mbar_init(&S.full[s], 1);
             ptx::mbar_init(&S.empty[s], 1);
         }
+        for (int g = 0; g < NAUG; ++g) {
+            ptx::mbar_init(&S.gfull[g], 1);
+            ptx::mbar_init(&S.gempty[g], 1);
+        }
         for (int b = 0; b < 2; ++b) {
             ptx::mbar_init(&S.tfull[b], 1);
             ptx::mbar_init(&S.tempty[b], NUM_EPI_WARPS);
@@ -143,10 +235,15 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         }
         ptx::mbar_init(&S.fin, 1);
         ptx::fence_barrier_init();
-        ptx::tma_prefetch_desc(&tq);
-        ptx::tma_prefetch_desc(&taug);
+        ptx::tma_prefetch_desc(&tqa);
+        ptx::tma_prefetch_desc(&tqb);
+        ptx::tma_prefetch_desc(&taa);
+        ptx::tma_prefetch_desc(&tab);
     }
-    for (int i = threadIdx.x; i < 512; i += NTHREADS) (&S.rowacc[0][0])[i] = 0;
+    for (int i = threadIdx.x; i < 2 * (128 + 256); i += NTHREADS) {
+        if (i < 256) (&S.rowacc[0][0])[i] = 0;
+        else (&S.colacc[0][0])[i - 256] = 0;
+    }
     if (threadIdx.x < 2) S.band_n[threadIdx.x] = 0;
     ptx::tc_fence_before();
     __syncthreads();
@@ -160,11 +257,29 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             uint32_t st = 0, ph = 0;
             uint32_t issued_ph[NST];
             uint32_t issued = 0;
+            uint32_t aug_ph[NAUG] = {0, 0};
+            uint64_t aug_issued = 0;
             bool ok = true;
-            uint2 wn = blockIdx.x < a.nwork ? __ldg(&a.work[blockIdx.x]) : make_uint2(0, 0);
-            for (uint64_t u = blockIdx.x; u < a.nwork && ok; u += gridDim.x) {
-                const uint2 w = wn;
-                if (u + gridDim.x < a.nwork) wn = __ldg(&a.work[u + gridDim.x]);  // prefetch
+            // entries are read one block ahead (their latency hides behind a block)
+            uint2 wnext = entry_or_end(a, item_at(0, a.lrun));
+            for (uint64_t idx = 0; ok; ++idx) {
+                const uint64_t u = item_at(idx, a.lrun);
+                if (u >= a.nwork) break;
+                const uint2 w = wnext;
+                wnext = entry_or_end(a, item_at(idx + 1, a.lrun));
+                const int32_t ya = (int32_t)(w.x * 128u);
+                const int32_t yb = (int32_t)((w.y & kPairMask) * 256u);
+                {
+                    // this block's aug boxes
+                    const uint32_t g = (uint32_t)(idx % NAUG), guse = (uint32_t)(idx / NAUG);
+                    if (!ptx::mbar_wait(&S.gempty[g], (guse & 1u) ^ 1u, a.st, 11)) break;
+                    uint8_t* sg = augs + (size_t)g * AUG_SLOT;
+                    ptx::mbar_arrive_expect_tx(&S.gfull[g], AUG_SLOT);
+                    ptx::tma_load_2d(sg, &taa, 0, ya, &S.gfull[g]);
+                    ptx::tma_load_2d(sg + AUG_A, &tab, 16, yb, &S.gfull[g]);
+                    aug_ph[g] = guse & 1u;
+                    ++aug_issued;
+                }
                 for (uint32_t step = 0; step < nsteps; ++step) {
                     if (!ptx::mbar_wait(&S.empty[st], ph ^ 1u, a.st, 10)) {
                         ok = false;
@@ -172,15 +287,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                     }
                     uint8_t* sa = stages + (size_t)st * STAGE_BYTES;
                     const int32_t x = (int32_t)slab_x<OPK>(step, a.nhi, a.split);
-                    ptx::mbar_arrive_expect_tx(&S.full[st], step == 0 ? FIRST_TX : DATA_TX);
-                    ptx::tma_load_2d(sa, &tq, x, (int32_t)(w.x * 128u), &S.full[st]);
-                    ptx::tma_load_2d(sa + SLAB_BYTES, &tq, x, (int32_t)(w.y * 128u), &S.full[st]);
-                    if (step == 0) {
-                        ptx::tma_load_2d(sa + 2 * SLAB_BYTES, &taug, 0, (int32_t)(w.x * 128u),
-                                         &S.full[st]);
-                        ptx::tma_load_2d(sa + 2 * SLAB_BYTES + AUG_BYTES, &taug, 16,
-                                         (int32_t)(w.y * 128u), &S.full[st]);
-                    }
+                    ptx::mbar_arrive_expect_tx(&S.full[st], DATA_TX);
+                    ptx::tma_load_2d(sa, &tqa, x, ya, &S.full[st]);
+                    ptx::tma_load_2d(sa + SLAB_A, &tqb, x, yb, &S.full[st]);
                     issued_ph[st] = ph;
                     ++issued;
                     if (++st == NST) {
@@ -190,19 +299,20 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 }
             }
             // drain: every issued copy has landed before the CTA can exit
-            const uint32_t last = issued < NST ? issued : NST;
+            const uint32_t last = issued < (uint32_t)NST ? issued : (uint32_t)NST;
             for (uint32_t k = 0; k < last; ++k) {
                 const uint32_t s = (st + NST - 1 - k) % NST;
-                ptx::mbar_wait(&S.full[s], issued_ph[s], a.st, 11);
+                ptx::mbar_wait_drain(&S.full[s], issued_ph[s]);
             }
+            for (uint32_t g = 0; g < NAUG; ++g)
+                if (aug_issued > g) ptx::mbar_wait_drain(&S.gfull[g], aug_ph[g]);
         }
     } else if (warp == 1) {
         // ------------------------------------------------ MMA issuer
         if (lane == 0) {
-            const uint32_t idesc =
-                OPK ? ptx::idesc_f32acc(0, 0, 128, 128) : ptx::idesc_f32acc(a.fmt, a.fmt, 128, 128);
-            const uint32_t idesc_aug =
-                OPK ? ptx::idesc_f32acc(1, 1, 128, 128) : idesc;
+            const uint32_t idesc = OPK ? ptx::idesc_f32acc(0, 0, 128, ACC_COLS)
+                                       : ptx::idesc_f32acc(a.fmt, a.fmt, 128, ACC_COLS);
+            const uint32_t idesc_aug = OPK ? ptx::idesc_f32acc(1, 1, 128, ACC_COLS) : idesc;
             auto mma = [&](uint32_t d, uint64_t ad, uint64_t bd, uint32_t acc_) {
                 if (OPK) ptx::mma_f8(d, ad, bd, idesc, acc_);
                 else ptx::mma_f16(d, ad, bd, idesc, acc_);
@@ -218,11 +328,12 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 }
                 return true;
             };
-            for (uint64_t u = blockIdx.x; u < a.nwork && ok; u += gridDim.x, ++it) {
+            for (uint64_t idx = 0; ok; ++idx, ++it) {
+                if (item_at(idx, a.lrun) >= a.nwork) break;
                 const uint32_t b = it & 1u, use = it >> 1;
                 if (!ptx::mbar_wait(&S.tempty[b], (use & 1u) ^ 1u, a.st, 21)) break;
                 ptx::tc_fence_after();
-                const uint32_t d_tmem = tmem + b * 128u;
+                const uint32_t d_tmem = tmem + b * ACC_COLS;
                 uint32_t acc = 0;
                 for (uint32_t c = 0; c < a.nhi && ok; ++c) {
                     uint32_t s_hi, s_lo = 0;
@@ -231,19 +342,22 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                     ptx::tc_fence_after();
                     uint8_t* st_hi = stages + (size_t)s_hi * STAGE_BYTES;
                     const uint64_t ah = ptx::sdesc_sw128(ptx::smem_u32(st_hi));
-                    const uint64_t bh = ptx::sdesc_sw128(ptx::smem_u32(st_hi + SLAB_BYTES));
+                    const uint64_t bh = ptx::sdesc_sw128(ptx::smem_u32(st_hi + SLAB_A));
                     if (c == 0) {
                         // aug: A side (alpha_i, -1) x B side (-1, alpha_j), one K = 16 step
-                        const uint64_t aa = ptx::sdesc_sw32(ptx::smem_u32(st_hi + 2 * SLAB_BYTES));
-                        const uint64_t ba =
-                            ptx::sdesc_sw32(ptx::smem_u32(st_hi + 2 * SLAB_BYTES + AUG_BYTES));
-                        ptx::mma_f16(d_tmem, aa, ba, idesc_aug, 0);
+                        const uint32_t g = (uint32_t)(idx % NAUG), guse = (uint32_t)(idx / NAUG);
+                        if (!ptx::mbar_wait(&S.gfull[g], guse & 1u, a.st, 22)) { ok = false; break; }
+                        ptx::tc_fence_after();
+                        uint8_t* sg = augs + (size_t)g * AUG_SLOT;
+                        ptx::mma_f16(d_tmem, ptx::sdesc_sw32(ptx::smem_u32(sg)),
+                                     ptx::sdesc_sw32(ptx::smem_u32(sg + AUG_A)), idesc_aug, 0);
+                        ptx::mma_commit(&S.gempty[g]);
                         acc = 1;
                     }
                     if (a.split) {
                         uint8_t* st_lo = stages + (size_t)s_lo * STAGE_BYTES;
                         const uint64_t al = ptx::sdesc_sw128(ptx::smem_u32(st_lo));
-                        const uint64_t bl = ptx::sdesc_sw128(ptx::smem_u32(st_lo + SLAB_BYTES));
+                        const uint64_t bl = ptx::sdesc_sw128(ptx::smem_u32(st_lo + SLAB_A));
 #pragma unroll
                         for (uint32_t kk = 0; kk < 4; ++kk) {
                             mma(d_tmem, ah + 2 * kk, bh + 2 * kk, acc);
@@ -263,114 +377,79 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             }
             // drain: all MMAs complete before tensor memory is freed
             ptx::mma_commit(&S.fin);
-            ptx::mbar_wait(&S.fin, 0, a.st, 22);
+            ptx::mbar_wait_drain(&S.fin, 0);
         }
     } else if (warp < FLUSH_WARP) {
         // ------------------------------------------------ epilogue warps
-        // warp e reads lane quarter (warp % 4) and the 32 columns 32 * (e / 4)
+        // warp e reads lane quarter (warp % 4) and the 64 columns 64 * (e / 4),
+        // which lie in half h = e / 8 (column tile 2p + h)
         const uint32_t ew = warp - 2;          // 0..15
         const uint32_t q = warp & 3u;          // tensor-memory lane quarter
-        const uint32_t cg = ew >> 2;           // column group
+        const uint32_t cg = ew >> 2;           // 64-column group
+        const uint32_t h = cg >> 1;            // half
         uint32_t it = 0;
-        // the next tile's (I, J) and margins are loaded one tile ahead, so
-        // their latency hides behind the current tile
-        uint2 w = blockIdx.x < a.nwork ? __ldg(&a.work[blockIdx.x]) : make_uint2(0, 0);
-        float W = blockIdx.x < a.nwork ? band_width(a, w) : 0.0f;
-        for (uint64_t u = blockIdx.x; u < a.nwork; u += gridDim.x, ++it) {
+        // band width of tiles (I, J): W >= beta_i + beta_j (Gram units; FP8
+        // operands: divided by sigma_I sigma_J, the accumulator's unit); the
+        // sum is rounded up by the 2^-20 relative margin, division by the
+        // power-of-two scales is exact.  0 for an inactive half.
+        auto half_width = [&](uint2 e) -> float {
+            if (e.x == 0xffffffffu || !((e.y >> (30 + h)) & 1u)) return 0.0f;
+            const uint32_t Je = 2u * (e.y & kPairMask) + h;
+            const float sm = __ldg(&a.tmax[e.x]) + __ldg(&a.tmax[Je]);
+            float Wv = fmaf(fabsf(sm), 9.5367431640625e-07f, sm);
+            if (a.tsig) Wv = Wv / (__ldg(&a.tsig[e.x]) * __ldg(&a.tsig[Je]));
+            return Wv;
+        };
+        // the next block's entry and band width are loaded one block ahead
+        uint2 w = entry_or_end(a, item_at(0, a.lrun));
+        float W = half_width(w);
+        for (uint64_t idx = 0;; ++idx, ++it) {
+            if (item_at(idx, a.lrun) >= a.nwork) break;
             const uint32_t b = it & 1u, use = it >> 1;
-            const bool has_next = u + gridDim.x < a.nwork;
-            uint2 wn = make_uint2(0, 0);
-            if (has_next) wn = __ldg(&a.work[u + gridDim.x]);
-            const bool diag = (w.x == w.y);
+            const uint2 wn = entry_or_end(a, item_at(idx + 1, a.lrun));
+            const uint32_t I = w.x, p = w.y & kPairMask, J = 2u * p + h;
+            const bool active = (w.y >> (30 + h)) & 1u;
+            const bool diag = (I == J);
             if (!ptx::mbar_wait(&S.tfull[b], use & 1u, a.st, 30)) break;
             ptx::tc_fence_after();
-            uint32_t v[32];
-            ptx::tmem_ld_32x32b_x32(tmem + ((q * 32u) << 16) + b * 128u + cg * 32u, v);
-            const float Wn = has_next ? band_width(a, wn) : 0.0f;
-            ptx::tmem_ld_wait();
+            uint32_t v0[32], v1[32];
+            const uint32_t taddr = tmem + ((q * 32u) << 16) + b * ACC_COLS + cg * 64u;
+            if (active) {
+                ptx::tmem_ld_32x32b_x32(taddr, v0);
+                ptx::tmem_ld_32x32b_x32(taddr + 32u, v1);
+            }
+            const float Wn = half_width(wn);
+            if (active) ptx::tmem_ld_wait();
             ptx::tc_fence_before();
             __syncwarp();
             if (lane == 0) ptx::mbar_arrive(&S.tempty[b]);
 
-            // Fast path: if max + W < 0 for the whole 32 x 32 chunk, every
-            // pair in it is certainly out (rounding of the FP32 add is
-            // monotone, so max + W >= 0 whenever any element is >= -W).
-            float m8[8];
-#pragma unroll
-            for (int j = 0; j < 8; ++j)
-                m8[j] = fmaxf(fmaxf(__uint_as_float(v[j]), __uint_as_float(v[j + 8])),
-                              fmaxf(__uint_as_float(v[j + 16]), __uint_as_float(v[j + 24])));
-            const float mx = fmaxf(fmaxf(fmaxf(m8[0], m8[1]), fmaxf(m8[2], m8[3])),
-                                   fmaxf(fmaxf(m8[4], m8[5]), fmaxf(m8[6], m8[7])));
-            const bool busy = __any_sync(FULL, mx + W >= 0.0f);
-            uint32_t inm = 0, bandm = 0;
-            if (busy) {
-                // sign bits, four independent 8-column chains
-                uint32_t ng[4] = {0, 0, 0, 0}, nw[4] = {0, 0, 0, 0};
-#pragma unroll
-                for (int c = 7; c >= 0; --c)
-#pragma unroll
-                    for (int g = 0; g < 4; ++g) {
-                        const uint32_t x = v[8 * g + c];
-                        ng[g] = __funnelshift_l(x, ng[g], 1);
-                        nw[g] = __funnelshift_l(__float_as_uint(__uint_as_float(x) + W), nw[g], 1);
-                    }
-                const uint32_t neg = ng[0] | (ng[1] << 8) | (ng[2] << 16) | (ng[3] << 24);
-                const uint32_t negw = nw[0] | (nw[1] << 8) | (nw[2] << 16) | (nw[3] << 24);
-                inm = ~neg;
-                bandm = neg & ~negw;
+            uint32_t in0 = 0, bd0 = 0, in1 = 0, bd1 = 0;
+            bool busy0 = false, busy1 = false;
+            if (active) {
+                busy0 = classify(v0, W, in0, bd0);
+                busy1 = classify(v1, W, in1, bd1);
             }
-            // the counts of buffer b were flushed and cleared for tile it - 2
+            // the counts of buffer b were flushed and cleared for block it - 2
             if (!ptx::mbar_wait(&S.fdone[b], (use & 1u) ^ 1u, a.st, 32)) break;
-            if (busy) {
+            if (busy0 || busy1) {
                 int* racc = S.rowacc[b];
                 int* cacc = S.colacc[b];
-                const uint32_t row = w.x * 128u + q * 32u + lane;
-                const uint32_t col0 = w.y * 128u + cg * 32u;
-                if (__any_sync(FULL, bandm != 0)) {
-                    // stage in shared memory (the flusher reserves global slots)
-                    const uint32_t nb = __popc(bandm);
-                    uint32_t incl = nb;
-#pragma unroll
-                    for (int o = 1; o < 32; o <<= 1) {
-                        const uint32_t t = __shfl_up_sync(FULL, incl, o);
-                        if (lane >= (uint32_t)o) incl += t;
+                const uint32_t row = I * 128u + q * 32u + lane;
+                const uint32_t col0 = p * 256u + cg * 64u;
+                if (__any_sync(FULL, (bd0 | bd1) != 0)) stage_band(a, S, b, bd0, bd1, row, col0, diag, lane);
+                if (!diag) {
+                    if (__any_sync(FULL, in0 != 0)) {
+                        const int cc = __popc(transpose32(in0, lane));
+                        if (cc) atomicAdd(&cacc[cg * 64u + lane], cc);
                     }
-                    const uint32_t total = __shfl_sync(FULL, incl, 31);
-                    uint32_t base = 0;
-                    if (lane == 31) base = atomicAdd(&S.band_n[b], total);
-                    base = __shfl_sync(FULL, base, 31);
-                    const bool fits = base + total <= BAND_SMEM;  // warp-uniform
-                    uint32_t slot = base + incl - nb;
-                    unsigned long long gslot = fits ? 0ull : band_reserve(a.st, nb);
-                    uint32_t m = bandm;
-                    while (m) {
-                        const uint32_t c = __ffs(m) - 1;
-                        m &= m - 1;
-                        BandPair bp;
-                        bp.i = row;
-                        bp.j = (col0 + c) | (diag ? 0u : kBandBoth);
-                        if (fits) {
-                            S.band_buf[b][slot++] = bp;
-                        } else {
-                            if (gslot < a.band_cap) a.band[gslot] = bp;
-                            ++gslot;
-                        }
-                    }
-                    if (!fits) {
-                        // mark this warp's staged slots unused
-                        for (uint32_t q2 = base + incl - nb; q2 < base + incl && q2 < BAND_SMEM; ++q2)
-                            S.band_buf[b][q2] = BandPair{BAND_SKIP, BAND_SKIP};
+                    if (__any_sync(FULL, in1 != 0)) {
+                        const int cc = __popc(transpose32(in1, lane));
+                        if (cc) atomicAdd(&cacc[cg * 64u + 32u + lane], cc);
                     }
                 }
-                if (__any_sync(FULL, inm != 0)) {
-                    if (!diag) {
-                        const int cc = __popc(transpose32(inm, lane));
-                        if (cc) atomicAdd(&cacc[cg * 32u + lane], cc);
-                    }
-                    const int rowcnt = __popc(inm);
-                    if (rowcnt) atomicAdd(&racc[q * 32u + lane], rowcnt);
-                }
+                const int rowcnt = __popc(in0) + __popc(in1);
+                if (rowcnt) atomicAdd(&racc[q * 32u + lane], rowcnt);
             }
             __syncwarp();
             if (lane == 0) ptx::mbar_arrive(&S.ebar[b]);
@@ -379,33 +458,48 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         }
     } else {
         // ------------------------------------------------ count flusher
-        // adds the per-tile row / column counts to global memory and clears
+        // adds the per-block row / column counts to global memory and clears
         // them, off the epilogue warps' critical path
         uint32_t it = 0;
-        for (uint64_t u = blockIdx.x; u < a.nwork; u += gridDim.x, ++it) {
+        uint2 wnext = entry_or_end(a, item_at(0, a.lrun));
+        for (uint64_t idx = 0;; ++idx, ++it) {
+            if (item_at(idx, a.lrun) >= a.nwork) break;
             const uint32_t b = it & 1u, use = it >> 1;
-            const uint2 w = __ldg(&a.work[u]);
+            const uint2 w = wnext;
+            wnext = entry_or_end(a, item_at(idx + 1, a.lrun));
             if (!ptx::mbar_wait(&S.ebar[b], use & 1u, a.st, 40)) break;
             int* racc = S.rowacc[b];
             int* cacc = S.colacc[b];
+            const uint32_t col_base = (w.y & kPairMask) * 256u;
 #pragma unroll
             for (int e = 0; e < 4; ++e) {
                 const uint32_t r = lane + 32 * e;
                 const int rv = racc[r];
                 if (rv) atomicAdd(&a.counts[w.x * 128u + r], rv);
                 racc[r] = 0;
-                const int cv = cacc[r];
-                if (cv) atomicAdd(&a.counts[w.y * 128u + r], cv);
-                cacc[r] = 0;
             }
-            // staged band entries of this tile: one global reservation, coalesced copy
+#pragma unroll
+            for (int e = 0; e < 8; ++e) {
+                const uint32_t c = lane + 32 * e;
+                const int cv = cacc[c];
+                if (cv) atomicAdd(&a.counts[col_base + c], cv);
+                cacc[c] = 0;
+            }
+            // staged band records of this block: one global reservation, coalesced
+            // copy, and their pair count
             const uint32_t nst = min(S.band_n[b], BAND_SMEM);
             if (nst) {
                 unsigned long long gbase = 0;
                 if (lane == 0) gbase = atomicAdd(&a.st->band_count, (unsigned long long)nst);
                 gbase = __shfl_sync(FULL, gbase, 0);
-                for (uint32_t e = lane; e < nst; e += 32)
-                    if (gbase + e < a.band_cap) a.band[gbase + e] = S.band_buf[b][e];
+                uint32_t np = 0;
+                for (uint32_t e = lane; e < nst; e += 32) {
+                    const BandRec r = S.band_buf[b][e];
+                    np += __popc(r.mask);
+                    if (gbase + e < a.band_cap) a.band[gbase + e] = r;
+                }
+                np = __reduce_add_sync(FULL, np);
+                if (lane == 0) atomicAdd(&a.st->band_pairs, (unsigned long long)np);
             }
             __syncwarp();
             if (lane == 0) S.band_n[b] = 0;
@@ -426,20 +520,24 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 
 int launch_gram16(const void* Q, const void* aug, uint64_t n_pad, const ScreenParams& P,
                   const uint2* work, uint64_t nwork, const float* tmax, const float* tsig,
-                  int32_t* counts, BandPair* band, uint64_t band_cap, DevStatus* st, int num_sms,
+                  int32_t* counts, BandRec* band, uint64_t band_cap, DevStatus* st, int num_sms,
                   cudaStream_t s) {
     if (nwork == 0) return EJOIN_OK;
     const bool fp8 = P.fmt == Fmt::E4M3;
-    if (n_pad % 128 || P.dp % (fp8 ? 128 : 64)) return set_error(EJOIN_EINTERNAL, "gram: bad padding");
-    if (n_pad > 0x7fffff80ull) return set_error(EJOIN_EUNSUPPORTED, "gram16: too many rows");
-    CUtensorMap map, amap;
+    if (n_pad % 256 || P.dp % (fp8 ? 128 : 64)) return set_error(EJOIN_EINTERNAL, "gram: bad padding");
+    if (n_pad > 0x7fffff00ull) return set_error(EJOIN_EUNSUPPORTED, "gram16: too many rows");
+    CUtensorMap ma, mb, maa, mab;
     const CUtensorMapDataType adt =
         P.fmt == Fmt::FP16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
-    if (fp8)
-        EJ_TRY(make_tmap_2d(&map, Q, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, P.width, n_pad, 128, 128));
-    else
-        EJ_TRY(make_tmap_2d(&map, Q, adt, 2, P.width, n_pad, 64, 128));
-    EJ_TRY(make_tmap_2d(&amap, aug, adt, 2, 32, n_pad, 16, 128));
+    if (fp8) {
+        EJ_TRY(make_tmap_2d(&ma, Q, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, P.width, n_pad, 128, 128));
+        EJ_TRY(make_tmap_2d(&mb, Q, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, P.width, n_pad, 128, 256));
+    } else {
+        EJ_TRY(make_tmap_2d(&ma, Q, adt, 2, P.width, n_pad, 64, 128));
+        EJ_TRY(make_tmap_2d(&mb, Q, adt, 2, P.width, n_pad, 64, 256));
+    }
+    EJ_TRY(make_tmap_2d(&maa, aug, adt, 2, 32, n_pad, 16, 128));
+    EJ_TRY(make_tmap_2d(&mab, aug, adt, 2, 32, n_pad, 16, 256));
     GramArgs a;
     a.work = work;
     a.nwork = nwork;
@@ -452,10 +550,16 @@ int launch_gram16(const void* Q, const void* aug, uint64_t n_pad, const ScreenPa
     a.nhi = P.dp / (fp8 ? 128 : 64);
     a.split = P.split ? 1u : 0u;
     a.fmt = P.fmt == Fmt::BF16 ? 1u : 0u;
+    // runs of consecutive entries per CTA (up to 16) while every CTA still gets
+    // several runs
+    uint32_t lrun = 4;
+    while (lrun > 0 && nwork < (uint64_t)num_sms * (4ull << lrun)) --lrun;
+    a.lrun = lrun;
     auto kern = fp8 ? gram_kernel<1> : gram_kernel<0>;
     EJ_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES));
-    const uint64_t grid = nwork < (uint64_t)num_sms ? nwork : (uint64_t)num_sms;
-    kern<<<(unsigned)grid, NTHREADS, SMEM_BYTES, s>>>(map, amap, a);
+    const uint64_t runs = (nwork + (1ull << lrun) - 1) >> lrun;
+    const uint64_t grid = runs < (uint64_t)num_sms ? runs : (uint64_t)num_sms;
+    kern<<<(unsigned)grid, NTHREADS, SMEM_BYTES, s>>>(ma, mb, maa, mab, a);
     EJ_CUDA(cudaGetLastError());
     note_launch();
     return EJOIN_OK;

@@ -82,6 +82,18 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, DevSta
     }
 }
 
+// Drain wait before exit: ends when the phase completes or after the same
+// deadline, whatever the other roles did (so that no copy or MMA the caller
+// issued is left in flight when the CTA exits, unless the hardware stalls).
+__device__ __forceinline__ bool mbar_wait_drain(uint64_t* bar, uint32_t parity) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = globaltimer();
+    for (uint32_t it = 1;; ++it) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if ((it & 255u) == 0 && globaltimer() - t0 > kWaitLimitNs) return false;
+    }
+}
+
 // ---------------------------------------------------------------- TMA --
 
 __device__ __forceinline__ void tma_prefetch_desc(const CUtensorMap* map) {
