@@ -68,6 +68,20 @@ def dist_env():
     return world, rank, local
 
 
+def replica_rate(ms, n, world, dist=None, device=None):
+    """Whole-job rate of `world` independent replicas, each joining n points:
+    the step time is the maximum over ranks (all_reduce MAX on the process
+    group), the rate counts every replica's n^2 ordered pairs.  Returns
+    (step ms, pairs/s)."""
+    if dist is not None and world > 1:
+        import torch
+
+        t = torch.tensor([ms], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms, world * float(n) * float(n) / (ms / 1e3)
+
+
 def workload(args):
     from tensor_bf_main_gb300 import datagen
 
@@ -237,12 +251,7 @@ def run_ours(args):
     torch.cuda.synchronize(dev)
     barrier()
     ck = clocks.stop()
-    ms = e0.elapsed_time(e1) / args.steps
-    if dist:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * float(n) * float(n) / (ms / 1e3)
+    ms, value = replica_rate(e0.elapsed_time(e1) / args.steps, n, world, dist, dev)
 
     # roofline of the dominant kernel (the Gram screen): executed MMA flops per
     # launch over its CUDA-event duration, against the measured sustained
