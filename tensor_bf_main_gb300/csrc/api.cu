@@ -464,7 +464,8 @@ static int run_screen16(Join& J, Fmt fmt, bool split, Learned& L) {
                           : (fmt == Fmt::FP16 ? EJOIN_FP16 : (split ? EJOIN_BF16_SPLIT : EJOIN_BF16));
     const void* Qp = fp8 ? (const void*)Q8.p : (const void*)Q.p;
     auto screen = [&](BandPair* band, uint64_t cap, DevStatus* st) {
-        return launch_gram16(Qp, Aug.p, n_pad, P, work.p, nwork, tmax.p, tsig.p, J.counts,
+        return launch_gram16(Qp, Aug.p, n_pad, P, work.p, nwork, tmax.p, beta.p, tsig.p, sig.p,
+                             J.counts,
                              reinterpret_cast<BandRec*>(band), cap, st, J.sms, J.s);
     };
     Recheck32 R;

@@ -243,8 +243,11 @@ int launch_dmma_join(const double* Y, uint64_t n_pad, uint32_t dp, const double*
 
 // k_umma.cu: tcgen05 Gram screen over a tile-pair work list (16-bit operands).
 // (FP8 operands: also the per-tile minimum row scale tsig.)
+// tmax / beta: per-tile / per-row out margins; FP8: tsig / sig per-tile
+// minimum / per-row scales.
 int launch_gram16(const void* Q, const void* aug, uint64_t n_pad, const ScreenParams& P,
-                  const uint2* work, uint64_t nwork, const float* tmax, const float* tsig,
+                  const uint2* work, uint64_t nwork, const float* tmax, const float* beta,
+                  const float* tsig, const float* sig,
                   int32_t* counts, BandRec* band, uint64_t band_cap, DevStatus* st, int num_sms,
                   cudaStream_t s);
 

@@ -176,70 +176,33 @@ __global__ void __launch_bounds__(256) band_recheck_kernel(const double* __restr
     if ((threadIdx.x & 31) == 0 && c) atomicAdd(&st->band_hits, (unsigned long long)c);
 }
 
-// Two-stage recheck of the band of the tensor-core screen, a thread per band
-// pair.  S = sum_c fl32(zf_ic - zf_jc)^2 over the FP32 coordinates of the
-// packed rows (16-byte loads when d % 4 == 0; four partial sums: any order
-// within the bound), then a rigorous decision that scales with the pair's own
-// distance:
+// Two-stage recheck of the band of the tensor-core screen.  For every band
+// pair, S = sum_c fl32(zf_ic - zf_jc)^2 over the FP32 coordinates of the
+// packed rows (any summation order: the bound covers it), then a rigorous
+// decision that scales with the pair's own distance:
 //   |w| = |zf_i - zf_j| differs from the exact scaled distance by at most
 //   rad_i + rad_j, and S from |w|^2 by the relative c32 (+ abs32), so
 //   S / (1 - c32) <= (sqrt(Tlo) - rad)^2   => neighbour
 //   S / (1 + c32) >  (sqrt(Thi) + rad)^2   => not a neighbour
 // Only the pairs left undecided (a tiny fraction) run the exact FP64 chain of
-// the reference arithmetic on the original rows.
-template <bool VEC4>
-__global__ void __launch_bounds__(256) band_recheck2_kernel(const double* __restrict__ X,
-                                                            uint32_t d,
-                                                            const uint32_t* __restrict__ perm,
-                                                            double T, Recheck32 R,
-                                                            const BandPair* __restrict__ band,
-                                                            uint64_t nband, uint64_t n,
-                                                            int32_t* counts, DevStatus* st) {
-    unsigned hits = 0, exact_runs = 0;
-    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < nband;
-         e += (uint64_t)gridDim.x * blockDim.x) {
-        const BandPair bp = band[e];
-        const uint32_t i = bp.i, j = bp.j & ~kBandBoth;
-        if (i >= n || j >= n) continue;
-        float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f, s3 = 0.0f;
-        if (VEC4) {
-            const float4* a = reinterpret_cast<const float4*>(R.Xf + (uint64_t)i * d);
-            const float4* b = reinterpret_cast<const float4*>(R.Xf + (uint64_t)j * d);
-#pragma unroll 4
-            for (uint32_t c = 0; c < d / 4; ++c) {
-                const float4 u = __ldg(&a[c]), v = __ldg(&b[c]);
-                const float t0 = u.x - v.x, t1 = u.y - v.y, t2 = u.z - v.z, t3 = u.w - v.w;
-                s0 = fmaf(t0, t0, s0);
-                s1 = fmaf(t1, t1, s1);
-                s2 = fmaf(t2, t2, s2);
-                s3 = fmaf(t3, t3, s3);
-            }
-        } else {
-            const float* a = R.Xf + (uint64_t)i * d;
-            const float* b = R.Xf + (uint64_t)j * d;
-            for (uint32_t c = 0; c < d; ++c) {
-                const float t = __ldg(&a[c]) - __ldg(&b[c]);
-                s0 = fmaf(t, t, s0);
-            }
-        }
-        const double Sd = (double)((s0 + s1) + (s2 + s3));
-        const double rr = (double)R.rad[i] + (double)R.rad[j];
-        const double lo = R.sTlo - rr;
-        const bool in = lo >= 0.0 && (Sd + R.abs32) / (1.0 - R.c32) <= lo * lo * (1.0 - 8 * kU);
-        const double hi = R.sThi + rr;
-        const bool out = (Sd - R.abs32) / (1.0 + R.c32) > hi * hi * (1.0 + 8 * kU);
-        bool hit = in;
-        if (!in && !out) {
-            ++exact_runs;
-            const uint64_t oi = perm ? perm[i] : i, oj = perm ? perm[j] : j;
-            hit = exact_d2(X + oi * (uint64_t)d, X + oj * (uint64_t)d, d) <= T;
-        }
-        if (hit) {
-            atomicAdd(&counts[i], 1);
-            if (bp.j & kBandBoth) atomicAdd(&counts[j], 1);
-            ++hits;
-        }
-    }
+// the reference arithmetic on the original rows.  Returns whether (i, j) is a
+// neighbour pair; counts the exact runs.
+__device__ __forceinline__ bool recheck_decide(const double* __restrict__ X, uint32_t d,
+                                               const uint32_t* __restrict__ perm, double T,
+                                               const Recheck32& R, uint32_t i, uint32_t j,
+                                               float S, unsigned& exact_runs) {
+    const double Sd = (double)S;
+    const double rr = (double)R.rad[i] + (double)R.rad[j];
+    const double lo = R.sTlo - rr;
+    if (lo >= 0.0 && (Sd + R.abs32) / (1.0 - R.c32) <= lo * lo * (1.0 - 8 * kU)) return true;
+    const double hi = R.sThi + rr;
+    if ((Sd - R.abs32) / (1.0 + R.c32) > hi * hi * (1.0 + 8 * kU)) return false;
+    ++exact_runs;
+    const uint64_t oi = perm ? perm[i] : i, oj = perm ? perm[j] : j;
+    return exact_d2(X + oi * (uint64_t)d, X + oj * (uint64_t)d, d) <= T;
+}
+
+__device__ __forceinline__ void recheck_totals(DevStatus* st, unsigned hits, unsigned exact_runs) {
     const unsigned c = __reduce_add_sync(0xffffffffu, hits);
     const unsigned x = __reduce_add_sync(0xffffffffu, exact_runs);
     if ((threadIdx.x & 31) == 0) {
@@ -248,21 +211,104 @@ __global__ void __launch_bounds__(256) band_recheck2_kernel(const double* __rest
     }
 }
 
+// Short rows (d <= 64, 16-byte aligned): a thread per pair streams both rows
+// with 16-byte loads (four partial sums): 32 pairs in flight per warp.
+__global__ void __launch_bounds__(256) band_recheck_thread_kernel(const double* __restrict__ X,
+                                                                  uint32_t d,
+                                                                  const uint32_t* __restrict__ perm,
+                                                                  double T, Recheck32 R,
+                                                                  const BandPair* __restrict__ band,
+                                                                  uint64_t nband, uint64_t n,
+                                                                  int32_t* counts, DevStatus* st) {
+    unsigned hits = 0, exact_runs = 0;
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < nband;
+         e += (uint64_t)gridDim.x * blockDim.x) {
+        const BandPair bp = band[e];
+        const uint32_t i = bp.i, j = bp.j & ~kBandBoth;
+        if (i >= n || j >= n) continue;
+        const float4* a = reinterpret_cast<const float4*>(R.Xf + (uint64_t)i * d);
+        const float4* b = reinterpret_cast<const float4*>(R.Xf + (uint64_t)j * d);
+        float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f, s3 = 0.0f;
+#pragma unroll 4
+        for (uint32_t c = 0; c < d / 4; ++c) {
+            const float4 u = __ldg(&a[c]), v = __ldg(&b[c]);
+            const float t0 = u.x - v.x, t1 = u.y - v.y, t2 = u.z - v.z, t3 = u.w - v.w;
+            s0 = fmaf(t0, t0, s0);
+            s1 = fmaf(t1, t1, s1);
+            s2 = fmaf(t2, t2, s2);
+            s3 = fmaf(t3, t3, s3);
+        }
+        if (recheck_decide(X, d, perm, T, R, i, j, (s0 + s1) + (s2 + s3), exact_runs)) {
+            atomicAdd(&counts[i], 1);
+            if (bp.j & kBandBoth) atomicAdd(&counts[j], 1);
+            ++hits;
+        }
+    }
+    recheck_totals(st, hits, exact_runs);
+}
+
+// Longer rows: a warp takes 32 band pairs; for each pair the lanes stream the
+// two rows (coalesced) and reduce S across the warp, and lane p then decides
+// pair p.
+__global__ void __launch_bounds__(256) band_recheck_warp_kernel(const double* __restrict__ X,
+                                                                uint32_t d,
+                                                                const uint32_t* __restrict__ perm,
+                                                                double T, Recheck32 R,
+                                                                const BandPair* __restrict__ band,
+                                                                uint64_t nband, uint64_t n,
+                                                                int32_t* counts, DevStatus* st) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / 32;
+    const uint64_t nwarps = (uint64_t)gridDim.x * blockDim.x / 32;
+    unsigned hits = 0, exact_runs = 0;
+    for (uint64_t base = warp * 32; base < nband; base += nwarps * 32) {
+        const uint64_t e = base + lane;
+        BandPair bp = {0xffffffffu, 0xffffffffu};
+        if (e < nband) bp = band[e];
+        const uint32_t mi = bp.i, mj = bp.j & ~kBandBoth;
+        const bool valid = e < nband && mi < n && mj < n;
+        float mine = 0.0f;
+        for (uint32_t q = 0; q < 32; ++q) {
+            const uint32_t i = __shfl_sync(0xffffffffu, mi, q);
+            const uint32_t j = __shfl_sync(0xffffffffu, mj, q);
+            const bool v = __shfl_sync(0xffffffffu, valid, q);
+            if (!v) continue;  // warp-uniform
+            const float* a = R.Xf + (uint64_t)i * d;
+            const float* b = R.Xf + (uint64_t)j * d;
+            float S = 0.0f;
+            for (uint32_t c = lane; c < d; c += 32) {
+                const float t = a[c] - b[c];
+                S = fmaf(t, t, S);
+            }
+            for (int o = 16; o; o >>= 1) S += __shfl_xor_sync(0xffffffffu, S, o);
+            if (lane == q) mine = S;
+        }
+        if (valid && recheck_decide(X, d, perm, T, R, mi, mj, mine, exact_runs)) {
+            atomicAdd(&counts[mi], 1);
+            if (bp.j & kBandBoth) atomicAdd(&counts[mj], 1);
+            ++hits;
+        }
+    }
+    recheck_totals(st, hits, exact_runs);
+}
+
 }  // namespace
 
 int launch_band_recheck2(const double* X, uint64_t n, uint32_t d, const uint32_t* perm, double T,
                          const Recheck32& R, const BandPair* band, uint64_t nband, int32_t* counts,
                          DevStatus* st, cudaStream_t s) {
     if (nband == 0) return EJOIN_OK;
-    // 16-byte loads need 16-byte aligned rows: d % 4 == 0 (Xf comes from the pool)
-    const bool vec4 = d % 4 == 0 && ((uintptr_t)R.Xf & 15) == 0;
-    const uint64_t blocks = std::min<uint64_t>((nband + 255) / 256, 152ull * 32);
-    if (vec4)
-        band_recheck2_kernel<true><<<(unsigned)blocks, 256, 0, s>>>(X, d, perm, T, R, band, nband,
-                                                                    n, counts, st);
-    else
-        band_recheck2_kernel<false><<<(unsigned)blocks, 256, 0, s>>>(X, d, perm, T, R, band, nband,
-                                                                     n, counts, st);
+    // measured on GB300: a thread per pair wins for rows of <= 256 bytes, a
+    // warp per pair (more pairs in flight per load) for longer rows
+    const bool thread = d <= 64 && d % 4 == 0 && ((uintptr_t)R.Xf & 15) == 0;
+    if (thread) {
+        const unsigned blocks = (unsigned)std::min<uint64_t>((nband + 255) / 256, 152ull * 32);
+        band_recheck_thread_kernel<<<blocks, 256, 0, s>>>(X, d, perm, T, R, band, nband, n, counts, st);
+    } else {
+        const uint64_t warps = (nband + 31) / 32;
+        const unsigned blocks = (unsigned)std::min<uint64_t>((warps + 7) / 8, 152ull * 64);
+        band_recheck_warp_kernel<<<blocks, 256, 0, s>>>(X, d, perm, T, R, band, nband, n, counts, st);
+    }
     EJ_CUDA(cudaGetLastError());
     note_launch();
     return EJOIN_OK;

@@ -312,9 +312,25 @@ __host__ __device__ inline uint32_t train_tile_pairs(uint32_t d) {
     tp = tp > 256u ? 256u : tp;
     return tp < 8u ? 8u : tp;
 }
+// Shared memory of train_step_kernel<K>: P transposed [d][K], the block's
+// gradient [K][d], the pair tile [TP][d + 1] (rounded up to whole float4s, so
+// that the coefficients start 16-byte aligned), the coefficients [TP][K].
+__host__ __device__ inline uint32_t train_tile_floats(uint32_t d) {
+    return (train_tile_pairs(d) * (d + 1) + 3u) & ~3u;
+}
 __host__ inline size_t train_smem_bytes(uint32_t k, uint32_t d) {
+    const uint32_t K = k <= 8 ? 8 : 16;
     const uint32_t tp = train_tile_pairs(d);
-    return (size_t)(2 * k * d + tp * (d + 1) + tp * k) * sizeof(float);
+    return (size_t)(2 * K * d + train_tile_floats(d) + tp * K) * sizeof(float);
+}
+// Pair slices of the backward pass: Q threads share a column c, each summing
+// every Q-th pair of the tile (their partials fit in the pair tile's space).
+__host__ __device__ inline uint32_t train_slices(uint32_t d, uint32_t K) {
+    const uint32_t tp = train_tile_pairs(d);
+    uint32_t q = d >= TRAIN_THREADS ? 1u : TRAIN_THREADS / d;
+    const uint32_t cap = tp * (d + 1) / (K * d);
+    q = q < cap ? q : cap;
+    return q < 1u ? 1u : q;
 }
 
 // Gradient and loss are accumulated in 64-bit fixed point (2^-40 units)
@@ -326,24 +342,31 @@ __device__ __forceinline__ void fix_add(unsigned long long* dst, float v) {
 }
 
 // Forward + hinge loss + backward for M pairs; G += dL/dP, loss += sum of
-// hinge terms / M (fixed-point accumulators).  A tile of TP pairs is staged once in
-// shared memory (row pitch d + 1: conflict-free) and serves the forward pass
-// (thread per pair) and the backward pass (thread per element of G).
+// hinge terms / M (fixed-point accumulators).  A tile of TP pairs is staged
+// once in shared memory (row pitch d + 1: conflict-free) and serves
+//   forward   thread per pair (warp per pair for d > 256); P is held
+//             transposed, so every coordinate reads its K weights with 16-byte
+//             broadcast loads;
+//   backward  Q threads per column c, each with K accumulators over every
+//             Q-th pair; the Q partials are then added in a fixed order.
 template <int K>
 __global__ void __launch_bounds__(TRAIN_THREADS) train_step_kernel(const float* __restrict__ P,
                                                                    uint32_t k, uint32_t d,
                                                                    PairBatch pb, uint64_t M,
                                                                    unsigned long long* G,
                                                                    unsigned long long* loss) {
-    extern __shared__ float sm[];
+    extern __shared__ float4 sm4[];
+    float* sm = reinterpret_cast<float*>(sm4);
     const uint32_t TP = train_tile_pairs(d);
     const uint32_t pitch = d + 1;
-    float* sP = sm;                // k * d
-    float* sG = sP + k * d;        // k * d: this block's gradient partial
-    float* sV = sG + k * d;        // TP * pitch
-    float* sC = sV + TP * pitch;   // TP * k coefficients
-    for (uint32_t e = threadIdx.x; e < k * d; e += blockDim.x) {
-        sP[e] = P[e];
+    const uint32_t Q = train_slices(d, K);
+    float* sPT = sm;               // d * K, P transposed, zero beyond k
+    float* sG = sPT + K * d;       // K * d: this block's gradient partial
+    float* sV = sG + K * d;        // TP * pitch (also the backward partials)
+    float* sC = sV + train_tile_floats(d);  // TP * K coefficients (16-byte aligned)
+    for (uint32_t e = threadIdx.x; e < K * d; e += blockDim.x) {
+        const uint32_t c = e / K, a = e % K;
+        sPT[e] = a < k ? P[a * d + c] : 0.0f;
         sG[e] = 0.0f;
     }
     const float invM = 1.0f / (float)M;
@@ -351,8 +374,31 @@ __global__ void __launch_bounds__(TRAIN_THREADS) train_step_kernel(const float* 
     for (uint64_t base = blockIdx.x * (uint64_t)TP; base < M; base += (uint64_t)gridDim.x * TP) {
         const uint32_t np = (M - base) < TP ? (uint32_t)(M - base) : TP;
         __syncthreads();
-        for (uint32_t e = threadIdx.x; e < np * d; e += blockDim.x)
-            sV[(e / d) * pitch + e % d] = pb.V[base * d + e];
+        {
+            // 16-byte loads, four in flight per thread (tile starts are 16-byte
+            // aligned: base is a multiple of TP, itself a multiple of 4 or d is)
+            const float* src = pb.V + base * d;
+            const uint32_t ne = np * d;
+            const bool al = (((uintptr_t)src) & 15) == 0;
+            const uint32_t n4 = al ? ne / 4 : 0;
+            const float4* src4 = reinterpret_cast<const float4*>(src);
+#pragma unroll 4
+            for (uint32_t e4 = threadIdx.x; e4 < n4; e4 += blockDim.x) {
+                const float4 v4 = __ldg(&src4[e4]);
+                const float vv[4] = {v4.x, v4.y, v4.z, v4.w};
+                uint32_t e = e4 * 4, r = e / d, c = e - r * d;
+#pragma unroll
+                for (int t = 0; t < 4; ++t) {
+                    sV[r * pitch + c] = vv[t];
+                    if (++c == d) {
+                        c = 0;
+                        ++r;
+                    }
+                }
+            }
+            for (uint32_t e = n4 * 4 + threadIdx.x; e < ne; e += blockDim.x)
+                sV[(e / d) * pitch + e % d] = src[e];
+        }
         __syncthreads();
         if (d <= 256) {
             // thread per pair
@@ -365,9 +411,15 @@ __global__ void __launch_bounds__(TRAIN_THREADS) train_step_kernel(const float* 
                     const float* v = sV + p * pitch;
                     for (uint32_t c = 0; c < d; ++c) {
                         const float vc = v[c];
+                        const float4* pt = reinterpret_cast<const float4*>(sPT + c * K);
 #pragma unroll
-                        for (int a = 0; a < K; ++a)
-                            if (a < (int)k) y[a] = fmaf(sP[a * d + c], vc, y[a]);
+                        for (int a4 = 0; a4 < K / 4; ++a4) {
+                            const float4 w = pt[a4];
+                            y[4 * a4 + 0] = fmaf(w.x, vc, y[4 * a4 + 0]);
+                            y[4 * a4 + 1] = fmaf(w.y, vc, y[4 * a4 + 1]);
+                            y[4 * a4 + 2] = fmaf(w.z, vc, y[4 * a4 + 2]);
+                            y[4 * a4 + 3] = fmaf(w.w, vc, y[4 * a4 + 3]);
+                        }
                     }
                     float r2 = 0.0f;
 #pragma unroll
@@ -379,8 +431,7 @@ __global__ void __launch_bounds__(TRAIN_THREADS) train_step_kernel(const float* 
                     }
                 }
 #pragma unroll
-                for (int a = 0; a < K; ++a)
-                    if (a < (int)k) sC[p * k + a] = coef * y[a];
+                for (int a = 0; a < K; ++a) sC[p * K + a] = coef * y[a];
             }
         } else {
             // warp per pair, lanes over coordinates (large d, few pairs per tile)
@@ -394,9 +445,15 @@ __global__ void __launch_bounds__(TRAIN_THREADS) train_step_kernel(const float* 
                     const float* v = sV + p * pitch;
                     for (uint32_t c = lane; c < d; c += 32) {
                         const float vc = v[c];
+                        const float4* pt = reinterpret_cast<const float4*>(sPT + c * K);
 #pragma unroll
-                        for (int a = 0; a < K; ++a)
-                            if (a < (int)k) y[a] = fmaf(sP[a * d + c], vc, y[a]);
+                        for (int a4 = 0; a4 < K / 4; ++a4) {
+                            const float4 w = pt[a4];
+                            y[4 * a4 + 0] = fmaf(w.x, vc, y[4 * a4 + 0]);
+                            y[4 * a4 + 1] = fmaf(w.y, vc, y[4 * a4 + 1]);
+                            y[4 * a4 + 2] = fmaf(w.z, vc, y[4 * a4 + 2]);
+                            y[4 * a4 + 3] = fmaf(w.w, vc, y[4 * a4 + 3]);
+                        }
                     }
 #pragma unroll
                     for (int a = 0; a < K; ++a)
@@ -415,18 +472,64 @@ __global__ void __launch_bounds__(TRAIN_THREADS) train_step_kernel(const float* 
                 }
                 if (lane == 0) {
 #pragma unroll
-                    for (int a = 0; a < K; ++a)
-                        if (a < (int)k) sC[p * k + a] = coef * y[a];
+                    for (int a = 0; a < K; ++a) sC[p * K + a] = coef * y[a];
                 }
             }
         }
         __syncthreads();
-        // G[a][c] += sum_p sC[p][a] * V[p][c]  (thread-owned elements: no atomics)
-        for (uint32_t el = threadIdx.x; el < k * d; el += blockDim.x) {
-            const uint32_t a = el / d, c = el % d;
-            float acc = 0.0f;
-            for (uint32_t p = 0; p < np; ++p) acc = fmaf(sC[p * k + a], sV[p * pitch + c], acc);
-            sG[el] += acc;
+        // G[a][c] += sum_p sC[p][a] * V[p][c]
+        if (Q == 1) {
+            for (uint32_t c = threadIdx.x; c < d; c += blockDim.x) {
+                float acc[K];
+#pragma unroll
+                for (int a = 0; a < K; ++a) acc[a] = 0.0f;
+                for (uint32_t p = 0; p < np; ++p) {
+                    const float v = sV[p * pitch + c];
+                    const float4* cp = reinterpret_cast<const float4*>(sC + p * K);
+#pragma unroll
+                    for (int a4 = 0; a4 < K / 4; ++a4) {
+                        const float4 w = cp[a4];
+                        acc[4 * a4 + 0] = fmaf(w.x, v, acc[4 * a4 + 0]);
+                        acc[4 * a4 + 1] = fmaf(w.y, v, acc[4 * a4 + 1]);
+                        acc[4 * a4 + 2] = fmaf(w.z, v, acc[4 * a4 + 2]);
+                        acc[4 * a4 + 3] = fmaf(w.w, v, acc[4 * a4 + 3]);
+                    }
+                }
+#pragma unroll
+                for (int a = 0; a < K; ++a) sG[a * d + c] += acc[a];
+            }
+        } else {
+            const bool own = threadIdx.x < d * Q;
+            const uint32_t c = threadIdx.x % d, q = threadIdx.x / d;
+            float acc[K];
+#pragma unroll
+            for (int a = 0; a < K; ++a) acc[a] = 0.0f;
+            if (own) {
+                for (uint32_t p = q; p < np; p += Q) {
+                    const float v = sV[p * pitch + c];
+                    const float4* cp = reinterpret_cast<const float4*>(sC + p * K);
+#pragma unroll
+                    for (int a4 = 0; a4 < K / 4; ++a4) {
+                        const float4 w = cp[a4];
+                        acc[4 * a4 + 0] = fmaf(w.x, v, acc[4 * a4 + 0]);
+                        acc[4 * a4 + 1] = fmaf(w.y, v, acc[4 * a4 + 1]);
+                        acc[4 * a4 + 2] = fmaf(w.z, v, acc[4 * a4 + 2]);
+                        acc[4 * a4 + 3] = fmaf(w.w, v, acc[4 * a4 + 3]);
+                    }
+                }
+            }
+            __syncthreads();  // the pair tile is free: it holds the partials now
+            float* red = sV;  // [Q][K][d]
+            if (own) {
+#pragma unroll
+                for (int a = 0; a < K; ++a) red[(q * K + a) * d + c] = acc[a];
+            }
+            __syncthreads();
+            for (uint32_t el = threadIdx.x; el < K * d; el += blockDim.x) {
+                float t = 0.0f;
+                for (uint32_t qq = 0; qq < Q; ++qq) t += red[qq * K * d + el];
+                sG[el] += t;
+            }
         }
     }
     __syncthreads();
@@ -444,8 +547,8 @@ __global__ void adam_renorm_kernel(float* P, unsigned long long* G, float* m1, f
                                    uint32_t k, uint32_t d, float lr, float b1, float b2, float c1,
                                    float c2, int renorm, float* sigma_out) {
     __shared__ float M[16 * 16], A[16 * 16], B[16 * 16];
-    __shared__ float v[16], w[16];
-    __shared__ float lam, amax;
+    __shared__ float v[16];
+    __shared__ float lam;
     const uint32_t nel = k * d;
     for (uint32_t e = threadIdx.x; e < nel; e += blockDim.x) {
         const float g = (float)((double)(long long)G[e] / kFix);
@@ -471,50 +574,51 @@ __global__ void adam_renorm_kernel(float* P, unsigned long long* G, float* m1, f
         }
     }
     __syncthreads();
-    for (int sq = 0; sq < 5; ++sq) {
-        if (threadIdx.x == 0) {
+    // the k x k part runs in warp 0 (warp-level synchronisation only): five
+    // normalised squarings, 8 power-iteration steps, the Rayleigh quotient
+    if (wid == 0) {
+        const uint32_t kk = k * k;
+        for (int sq = 0; sq < 5; ++sq) {
             float mx = 0.0f;
-            for (uint32_t e = 0; e < k * k; ++e) mx = fmaxf(mx, fabsf(A[e]));
-            amax = mx > 0.0f ? 1.0f / mx : 0.0f;
+            for (uint32_t e = lane; e < kk; e += 32) mx = fmaxf(mx, fabsf(A[e]));
+            for (int o = 16; o; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+            const float inv = mx > 0.0f ? 1.0f / mx : 0.0f;
+            for (uint32_t e = lane; e < kk; e += 32) {
+                const uint32_t a = e / k, b = e % k;
+                float s = 0.0f;
+                for (uint32_t c = 0; c < k; ++c) s = fmaf(A[a * k + c] * inv, A[c * k + b] * inv, s);
+                B[e] = s;
+            }
+            __syncwarp();
+            for (uint32_t e = lane; e < kk; e += 32) A[e] = B[e];
+            __syncwarp();
         }
-        __syncthreads();
-        const float inv = amax;
-        for (uint32_t e = threadIdx.x; e < k * k; e += blockDim.x) {
-            const uint32_t a = e / k, b = e % k;
+        float vl = lane < k ? 1.0f + 0.01f * lane : 0.0f;  // lane a holds v[a]
+        for (int it = 0; it < 8; ++it) {
+            if (lane < k) v[lane] = vl;
+            __syncwarp();
             float s = 0.0f;
-            for (uint32_t c = 0; c < k; ++c) s = fmaf(A[a * k + c] * inv, A[c * k + b] * inv, s);
-            B[e] = s;
+            if (lane < k)
+                for (uint32_t b = 0; b < k; ++b) s = fmaf(A[lane * k + b], v[b], s);
+            float nn = s * s;
+            for (int o = 16; o; o >>= 1) nn += __shfl_xor_sync(0xffffffffu, nn, o);
+            vl = nn > 0.0f ? s * rsqrtf(nn) : 0.0f;
+            __syncwarp();
         }
-        __syncthreads();
-        for (uint32_t e = threadIdx.x; e < k * k; e += blockDim.x) A[e] = B[e];
-        __syncthreads();
-    }
-    if (threadIdx.x < k) v[threadIdx.x] = 1.0f + 0.01f * threadIdx.x;
-    __syncthreads();
-    for (int it = 0; it < 8; ++it) {
-        if (threadIdx.x < k) {
-            float s = 0.0f;
-            for (uint32_t b = 0; b < k; ++b) s = fmaf(A[threadIdx.x * k + b], v[b], s);
-            w[threadIdx.x] = s;
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            float nn = 0.0f;
-            for (uint32_t b = 0; b < k; ++b) nn = fmaf(w[b], w[b], nn);
-            const float inv = nn > 0.0f ? rsqrtf(nn) : 0.0f;
-            for (uint32_t b = 0; b < k; ++b) v[b] = w[b] * inv;
-        }
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) {
+        if (lane < k) v[lane] = vl;
+        __syncwarp();
         float num = 0.0f, den = 0.0f;
-        for (uint32_t a = 0; a < k; ++a) {
+        if (lane < k) {
             float s = 0.0f;
-            for (uint32_t b = 0; b < k; ++b) s = fmaf(M[a * k + b], v[b], s);
-            num = fmaf(v[a], s, num);
-            den = fmaf(v[a], v[a], den);
+            for (uint32_t b = 0; b < k; ++b) s = fmaf(M[lane * k + b], v[b], s);
+            num = vl * s;
+            den = vl * vl;
         }
-        lam = den > 0.0f ? num / den : 0.0f;
+        for (int o = 16; o; o >>= 1) {
+            num += __shfl_xor_sync(0xffffffffu, num, o);
+            den += __shfl_xor_sync(0xffffffffu, den, o);
+        }
+        if (lane == 0) lam = den > 0.0f ? num / den : 0.0f;
     }
     __syncthreads();
     const float sig = sqrtf(fmaxf(lam, 0.0f)) * 1.02f;

@@ -29,9 +29,10 @@
 //    + lo*hi.  The aug MMA adds -alpha_i - alpha_j, so the accumulator holds
 //    C_ij = q_i.q_j - alpha_i - alpha_j and the rigorous screen is a sign test:
 //        C >= 0          pair certainly within eps        (counted)
-//        C < -W_IJ       pair certainly outside eps
+//        C < -W_iJ       pair certainly outside eps
 //        otherwise       band: queued for the FP64 recheck
-//    W_IJ = max beta over tile I + max beta over tile J.
+//    W_iJ = beta_i + max beta over tile J >= beta_i + beta_j (one value per
+//    row and column tile, so the test costs the same as a tile-wide width).
 //  * The epilogue packs sign bits with one funnel shift per element, counts
 //    rows with popc, transposes 32x32 bit blocks across the warp to count
 //    columns (off-diagonal tiles credit both points), and a flusher warp adds
@@ -70,8 +71,10 @@ constexpr uint32_t kPairMask = (1u << 30) - 1u;
 struct GramArgs {
     const uint2* work;
     uint64_t nwork;
-    const float* tmax;
+    const float* tmax;  // per 128-row tile: max beta
+    const float* beta;  // per row: beta (out margin, Gram units)
     const float* tsig;  // FP8: per-tile minimum row scale (null for 16-bit operands)
+    const float* sig;   // FP8: per-row scale
     int32_t* counts;
     BandRec* band;
     uint64_t band_cap;
@@ -136,6 +139,25 @@ __device__ __forceinline__ uint32_t slab_x(uint32_t step, uint32_t nhi, uint32_t
     constexpr uint32_t E = OPK ? 128u : 64u;  // elements per 128-byte slab row
     if (split) return (step & 1) ? E * nhi + E * (step >> 1) : E * (step >> 1);
     return E * step;
+}
+
+// Column counts of one 32 x 32 in-mask (lane = row): sparse masks (at most
+// 3 bits per lane) add per bit to shared memory, denser ones transpose the
+// bit block across the warp and add one count per column.
+__device__ __forceinline__ void col_counts(uint32_t inm, int* cacc, uint32_t lane) {
+    const uint32_t mp = __reduce_max_sync(FULL, __popc(inm));
+    if (mp == 0) return;
+    if (mp <= 3) {
+        uint32_t m = inm;
+        while (m) {
+            const uint32_t c = __ffs(m) - 1;
+            m &= m - 1;
+            atomicAdd(&cacc[c], 1);
+        }
+    } else {
+        const int cc = __popc(transpose32(inm, lane));
+        if (cc) atomicAdd(&cacc[lane], cc);
+    }
 }
 
 // In / band bit masks of one 32 x 32 chunk (lane = row, v[c] = column c).
@@ -388,21 +410,23 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         const uint32_t cg = ew >> 2;           // 64-column group
         const uint32_t h = cg >> 1;            // half
         uint32_t it = 0;
-        // band width of tiles (I, J): W >= beta_i + beta_j (Gram units; FP8
-        // operands: divided by sigma_I sigma_J, the accumulator's unit); the
+        // band width of row i against column tile J: W >= beta_i + beta_j
+        // (Gram units; FP8 operands: divided by sigma_i sigma_J,min, the
+        // accumulator's unit for pair (i, j) being 1 / (sigma_i sigma_j)); the
         // sum is rounded up by the 2^-20 relative margin, division by the
         // power-of-two scales is exact.  0 for an inactive half.
-        auto half_width = [&](uint2 e) -> float {
+        auto row_width = [&](uint2 e) -> float {
             if (e.x == 0xffffffffu || !((e.y >> (30 + h)) & 1u)) return 0.0f;
             const uint32_t Je = 2u * (e.y & kPairMask) + h;
-            const float sm = __ldg(&a.tmax[e.x]) + __ldg(&a.tmax[Je]);
+            const uint32_t r = e.x * 128u + q * 32u + lane;
+            const float sm = __ldg(&a.beta[r]) + __ldg(&a.tmax[Je]);
             float Wv = fmaf(fabsf(sm), 9.5367431640625e-07f, sm);
-            if (a.tsig) Wv = Wv / (__ldg(&a.tsig[e.x]) * __ldg(&a.tsig[Je]));
+            if (a.tsig) Wv = Wv / (__ldg(&a.sig[r]) * __ldg(&a.tsig[Je]));
             return Wv;
         };
-        // the next block's entry and band width are loaded one block ahead
+        // the next block's entry and band widths are loaded one block ahead
         uint2 w = entry_or_end(a, item_at(0, a.lrun));
-        float W = half_width(w);
+        float W = row_width(w);
         for (uint64_t idx = 0;; ++idx, ++it) {
             if (item_at(idx, a.lrun) >= a.nwork) break;
             const uint32_t b = it & 1u, use = it >> 1;
@@ -418,7 +442,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 ptx::tmem_ld_32x32b_x32(taddr, v0);
                 ptx::tmem_ld_32x32b_x32(taddr + 32u, v1);
             }
-            const float Wn = half_width(wn);
+            const float Wn = row_width(wn);
             if (active) ptx::tmem_ld_wait();
             ptx::tc_fence_before();
             __syncwarp();
@@ -439,14 +463,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 const uint32_t col0 = p * 256u + cg * 64u;
                 if (__any_sync(FULL, (bd0 | bd1) != 0)) stage_band(a, S, b, bd0, bd1, row, col0, diag, lane);
                 if (!diag) {
-                    if (__any_sync(FULL, in0 != 0)) {
-                        const int cc = __popc(transpose32(in0, lane));
-                        if (cc) atomicAdd(&cacc[cg * 64u + lane], cc);
-                    }
-                    if (__any_sync(FULL, in1 != 0)) {
-                        const int cc = __popc(transpose32(in1, lane));
-                        if (cc) atomicAdd(&cacc[cg * 64u + 32u + lane], cc);
-                    }
+                    col_counts(in0, cacc + cg * 64u, lane);
+                    col_counts(in1, cacc + cg * 64u + 32u, lane);
                 }
                 const int rowcnt = __popc(in0) + __popc(in1);
                 if (rowcnt) atomicAdd(&racc[q * 32u + lane], rowcnt);
@@ -519,7 +537,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 }  // namespace
 
 int launch_gram16(const void* Q, const void* aug, uint64_t n_pad, const ScreenParams& P,
-                  const uint2* work, uint64_t nwork, const float* tmax, const float* tsig,
+                  const uint2* work, uint64_t nwork, const float* tmax, const float* beta,
+                  const float* tsig, const float* sig,
                   int32_t* counts, BandRec* band, uint64_t band_cap, DevStatus* st, int num_sms,
                   cudaStream_t s) {
     if (nwork == 0) return EJOIN_OK;
@@ -542,7 +561,10 @@ int launch_gram16(const void* Q, const void* aug, uint64_t n_pad, const ScreenPa
     a.work = work;
     a.nwork = nwork;
     a.tmax = tmax;
+    a.beta = beta;
     a.tsig = fp8 ? tsig : nullptr;
+    a.sig = fp8 ? sig : nullptr;
+    if (!tmax || !beta || (fp8 && (!tsig || !sig))) return set_error(EJOIN_EINTERNAL, "gram: margins missing");
     a.counts = counts;
     a.band = band;
     a.band_cap = band_cap;
