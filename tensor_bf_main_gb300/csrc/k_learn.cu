@@ -78,6 +78,8 @@ __global__ void __launch_bounds__(PJ_ROWS) project_kernel(
     __shared__ float sP[K * PJ_CH];
     __shared__ unsigned int smn[4][K], smx[4][K];
     const uint32_t t = threadIdx.x, lane = t & 31, w = t >> 5;
+    // every chunk is a whole number of float4s when d % 4 == 0 (cw then too)
+    const bool vec4 = d % 4 == 0 && (((uintptr_t)Y32) & 15) == 0;
     const float NaNf = __int_as_float(0x7fc00000);
     const float c1 = (float)(d + 4) * 5.9604644775390625e-08f * 1.0000153f;  // (d+4) 2^-24 (1+2^-16)
     uint32_t lo[K], hi[K];
@@ -95,10 +97,26 @@ __global__ void __launch_bounds__(PJ_ROWS) project_kernel(
         for (uint32_t c0 = 0; c0 < d; c0 += PJ_CH) {
             const uint32_t cw = min(PJ_CH, d - c0);
             __syncthreads();
-            for (uint32_t e = t; e < PJ_ROWS * PJ_CH; e += PJ_ROWS) {
-                const uint32_t r = e / PJ_CH, c = e % PJ_CH;
-                sY[r * (PJ_CH + 1) + c] =
-                    (i0 + r < n && c < cw) ? Y32[(i0 + r) * d + c0 + c] : 0.0f;
+            if (vec4) {
+                // 16-byte loads, several in flight per thread (rows 16-byte aligned)
+#pragma unroll 4
+                for (uint32_t e4 = t; e4 < PJ_ROWS * PJ_CH / 4; e4 += PJ_ROWS) {
+                    const uint32_t r = e4 / (PJ_CH / 4), c = (e4 % (PJ_CH / 4)) * 4;
+                    float4 v4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                    if (i0 + r < n && c < cw)
+                        v4 = __ldg(reinterpret_cast<const float4*>(Y32 + (i0 + r) * d + c0 + c));
+                    float* dst = sY + r * (PJ_CH + 1) + c;
+                    dst[0] = v4.x;
+                    dst[1] = v4.y;
+                    dst[2] = v4.z;
+                    dst[3] = v4.w;
+                }
+            } else {
+                for (uint32_t e = t; e < PJ_ROWS * PJ_CH; e += PJ_ROWS) {
+                    const uint32_t r = e / PJ_CH, c = e % PJ_CH;
+                    sY[r * (PJ_CH + 1) + c] =
+                        (i0 + r < n && c < cw) ? Y32[(i0 + r) * d + c0 + c] : 0.0f;
+                }
             }
             for (uint32_t e = t; e < K * PJ_CH; e += PJ_ROWS) {
                 const uint32_t a = e / PJ_CH, c = e % PJ_CH;

@@ -351,25 +351,34 @@ __device__ __forceinline__ float round_fmt_f(float v, int fbits, float min_norma
 }
 
 // Squared norm of q accumulated in FP32 (round to nearest): each term passes
-// through at most ceil(dp / 32) lane-chain FMAs and 5 shuffle-tree additions,
+// through at most `chain` lane-chain FMAs and `levels` shuffle-tree additions,
 // so |computed - exact| <= gamma * exact + (dp + 160) 2^-149 (underflow), with
-// gamma = (ceil(dp / 32) + 6) 2^-24 (1.01 covers gamma_m's denominator).
+// gamma = (chain + levels + 1) 2^-24 (1.01 covers gamma_m's denominator).
 struct NormBound {
     double rel, abs;
 };
-__device__ __forceinline__ NormBound fp32_norm_bound(uint32_t dp) {
-    return {((dp + 31) / 32 + 6) * 5.9604644775390625e-08 * 1.01, (dp + 160) * 1.4012984643248171e-45};
+__device__ __forceinline__ NormBound fp32_norm_bound(uint32_t dp, uint32_t chain, uint32_t levels) {
+    return {(chain + levels + 1) * 5.9604644775390625e-08 * 1.01, (dp + 160) * 1.4012984643248171e-45};
 }
 
-// A warp packs 32 consecutive rows.  Phase 1 (lanes over coordinates, one row
-// at a time): z = s * Y32 (exact power-of-two scaling of the FP32 centred
-// copy), hi = round(z), lo = round(z - hi) (split), ef = z - hi - lo; every
-// FP32 subtraction here is exact.  The residual to the exact centred point is
-// (Yerr_i s, from the centring pass) + |ef| (+ 2^-126 per flushed coordinate).
-// Per row: nq = |q|^2 (FP32, bounded by fp32_norm_bound) and in FP32 rounded
-// up: |ef|^2, |(|hi| + |lo|)|^2, |lo|^2.  The FP32 coordinates z and a per-row
-// radius go to Xf / rad for the FP32 band pre-check.  Phase 2 (lane = row):
-// the FP64 threshold arithmetic (alpha, beta), the aug slab.
+// Bit pattern of a value already representable in the 16-bit format.
+__device__ __forceinline__ uint16_t bits16f(float x, Fmt f) {
+    if (f == Fmt::BF16) return (uint16_t)(__float_as_uint(x) >> 16);
+    return __half_as_ushort(__float2half_rn(x));
+}
+
+// A warp packs 32 consecutive rows.  Phase 1, two rows at a time (half-warp
+// h takes row 2 it + h; lane l of the half handles coordinates 4l .. 4l+3 of
+// every 64-wide slab, 16-byte loads): z = s * Y32 (exact power-of-two scaling
+// of the FP32 centred copy), hi = round(z), lo = round(z - hi) (split),
+// ef = z - hi - lo; every FP32 subtraction here is exact.  The residual to the
+// exact centred point is (Yerr_i s, from the centring pass) + |ef| (+ 2^-126
+// per flushed coordinate).  Per row: nq = |q|^2 (FP32, bounded by
+// fp32_norm_bound) and in FP32 rounded up: |ef|^2, |(|hi| + |lo|)|^2, |lo|^2.
+// The FP32 coordinates z and a per-row radius go to Xf / rad for the FP32
+// band pre-check.  Phase 2 (lane L = row 2 (L % 16) + L / 16, whose sums the
+// half-warp reduction left in that lane): the FP64 threshold arithmetic
+// (alpha, beta), the aug slab.
 template <Fmt F>
 __global__ void __launch_bounds__(256) pack16_kernel(const float* __restrict__ Y32, uint64_t n,
                                                      uint64_t n_pad,
@@ -379,27 +388,45 @@ __global__ void __launch_bounds__(256) pack16_kernel(const float* __restrict__ Y
                                                      uint16_t* Q, uint16_t* Aug, float* beta,
                                                      float* Xf, float* rad) {
     const uint64_t p0 = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / 32 * 32;
-    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t lane = threadIdx.x & 31, hw = lane >> 4, l = lane & 15;
     if (p0 >= n_pad) return;
     const FmtInfo fi = fmt_info(F);
     const float mnf = (float)fi.min_normal;
     const float sf = (float)P.scale;
+    // 16-byte access to Y32 / Xf rows needs d % 4 == 0 (and aligned bases)
+    const bool v4 = P.d % 4 == 0 && (((uintptr_t)Y32 | (uintptr_t)Xf) & 15) == 0;
     float m_nq = 0, m_e2 = 0, m_a2 = 0, m_l2 = 0;
     uint64_t m_src = 0;
     bool m_good = false;
-    for (uint32_t r = 0; r < 32; ++r) {
-        const uint64_t p = p0 + r;
+    for (uint32_t it = 0; it < 16; ++it) {
+        const uint64_t p = p0 + 2 * it + hw;
         const uint64_t src = p < n ? (perm ? perm[p] : p) : 0;
         const bool good = p < n && !bad[src];
         uint16_t* row = Q + p * (uint64_t)P.width;
         float nq = 0, e2 = 0, a2 = 0, l2 = 0;
-        for (uint32_t k = lane; k < P.dp; k += 32) {
-            float hi = 0.0f, lo = 0.0f, zf = 0.0f;
-            if (good && k < P.d) {
-                zf = Y32[src * P.d + k] * sf;  // exact power-of-two scaling
+        for (uint32_t k0 = 4 * l; k0 < P.dp; k0 += 64) {
+            float z[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+            if (good && k0 < P.d) {
+                if (v4) {
+                    const float4 y = __ldg(reinterpret_cast<const float4*>(Y32 + src * P.d + k0));
+                    z[0] = y.x;
+                    z[1] = y.y;
+                    z[2] = y.z;
+                    z[3] = y.w;
+                } else {
+#pragma unroll
+                    for (int t = 0; t < 4; ++t)
+                        if (k0 + t < P.d) z[t] = __ldg(&Y32[src * P.d + k0 + t]);
+                }
+            }
+            uint16_t hb[4], lb[4];
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+                float zf = z[t] * sf;  // exact power-of-two scaling
                 if (fabsf(zf) < 1.1754944e-38f) zf = 0.0f;  // keep Xf free of FP32 subnormals
-                hi = round_fmt_f(zf, fi.fbits, mnf);
+                const float hi = round_fmt_f(zf, fi.fbits, mnf);
                 float ef = zf - hi;  // exact
+                float lo = 0.0f;
                 if (P.split) {
                     lo = round_fmt_f(ef, fi.fbits, mnf);
                     ef = ef - lo;  // exact
@@ -410,18 +437,34 @@ __global__ void __launch_bounds__(256) pack16_kernel(const float* __restrict__ Y
                 e2 = __fmaf_ru(ef, ef, e2);
                 a2 = __fmaf_ru(aq, aq, a2);
                 l2 = __fmaf_ru(lo, lo, l2);
+                hb[t] = bits16f(hi, F);
+                lb[t] = bits16f(lo, F);
+                z[t] = zf;
             }
-            row[k] = to_bits16(hi, F);
-            if (P.split) row[P.dp + k] = to_bits16(lo, F);
-            if (k < P.d) Xf[p * P.d + k] = zf;
+            // k0 is a multiple of 4 and rows are 128-byte multiples: 8-byte stores
+            *reinterpret_cast<uint2*>(row + k0) =
+                make_uint2(hb[0] | ((uint32_t)hb[1] << 16), hb[2] | ((uint32_t)hb[3] << 16));
+            if (P.split)
+                *reinterpret_cast<uint2*>(row + P.dp + k0) =
+                    make_uint2(lb[0] | ((uint32_t)lb[1] << 16), lb[2] | ((uint32_t)lb[3] << 16));
+            if (k0 < P.d) {
+                if (v4) {
+                    *reinterpret_cast<float4*>(Xf + p * P.d + k0) = make_float4(z[0], z[1], z[2], z[3]);
+                } else {
+#pragma unroll
+                    for (int t = 0; t < 4; ++t)
+                        if (k0 + t < P.d) Xf[p * P.d + k0 + t] = z[t];
+                }
+            }
         }
-        for (int o = 16; o; o >>= 1) {
+        // reduction within the half-warp (xor offsets < 16 stay in the half)
+        for (int o = 8; o; o >>= 1) {
             nq = __fadd_rn(nq, __shfl_xor_sync(0xffffffffu, nq, o));
             e2 = __fadd_ru(e2, __shfl_xor_sync(0xffffffffu, e2, o));
             a2 = __fadd_ru(a2, __shfl_xor_sync(0xffffffffu, a2, o));
             l2 = __fadd_ru(l2, __shfl_xor_sync(0xffffffffu, l2, o));
         }
-        if (lane == r) {
+        if (l == it) {
             m_nq = nq;
             m_e2 = e2;
             m_a2 = a2;
@@ -430,13 +473,13 @@ __global__ void __launch_bounds__(256) pack16_kernel(const float* __restrict__ Y
             m_good = good;
         }
     }
-    // ---- phase 2: row p0 + lane
-    const uint64_t p = p0 + lane;
+    // ---- phase 2: row p0 + 2 (lane % 16) + lane / 16
+    const uint64_t p = p0 + 2 * l + hw;
     double ah[3] = {0, 0, 0};
     double b = 0.0;
     float radius = INFINITY;  // bad and padding rows: the FP32 pre-check never decides
     if (m_good) {
-        const NormBound nb = fp32_norm_bound(P.dp);
+        const NormBound nb = fp32_norm_bound(P.dp, P.dp / 16, 4);
         const double nup = (double)m_nq * (1 + nb.rel) + nb.abs;
         const double ndn = (double)m_nq * (1 - nb.rel) - nb.abs;
         const double a2u = (double)m_a2, lu = (double)m_l2;
@@ -580,7 +623,7 @@ __global__ void __launch_bounds__(256) pack8_kernel(const float* __restrict__ Y3
     double b = 0.0, rsig = 1.0;
     float radius = INFINITY;
     if (m_good) {
-        const NormBound nb = fp32_norm_bound(P.dp);
+        const NormBound nb = fp32_norm_bound(P.dp, (P.dp + 31) / 32, 5);
         const double nup = (double)m_nq * (1 + nb.rel) + nb.abs;
         const double ndn = (double)m_nq * (1 - nb.rel) - nb.abs;
         const double a2u = nup;  // |(|q|)|^2 = |q|^2
