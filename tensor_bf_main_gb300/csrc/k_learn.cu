@@ -278,42 +278,62 @@ struct PairBatch {
 
 // Half uniform random pairs, half pairs close in the current order (perm);
 // differences and distances from the FP32 centred copy (training needs no
-// exactness).  Pairs with a non-finite row are inactive.  A warp builds one
-// pair at a time: lanes over coordinates (coalesced row reads and writes).
+// exactness).  Pairs with a non-finite row are inactive.  A group of 8 lanes
+// builds one pair (16-byte loads when d % 4 == 0), so a warp has 4 pairs in
+// flight.
 __global__ void sample_pairs_kernel(const float* __restrict__ Y32, const uint8_t* __restrict__ bad,
                                     uint64_t n, uint32_t d, const uint32_t* __restrict__ perm,
                                     uint64_t M, uint64_t seed, double eps, uint32_t window,
                                     PairBatch pb) {
-    const uint32_t lane = threadIdx.x & 31;
+    constexpr uint32_t G = 8;
+    const uint32_t lane = threadIdx.x & 31, g = lane % G;
     const uint64_t gw = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / 32;
     const uint64_t nw = (uint64_t)gridDim.x * blockDim.x / 32;
     const float lo = (float)(eps * 1.02), cap = (float)(2.0 * eps);
-    for (uint64_t e = gw; e < M; e += nw) {
-        const uint64_t h1 = splitmix64(seed ^ (e * 0x9E3779B97F4A7C15ull));
-        const uint64_t h2 = splitmix64(h1);
-        uint64_t i, j;
-        if (e & 1) {
-            i = h1 % n;
-            j = h2 % n;
-        } else {
-            const uint64_t t = h1 % n;
-            uint64_t u = t + 1 + (h2 % window);
-            if (u >= n) u = t >= 1 + (h2 % window) ? t - 1 - (h2 % window) : 0;
-            i = perm ? perm[t] : t;
-            j = perm ? perm[u] : u;
+    const bool v4 = d % 4 == 0 && (((uintptr_t)Y32 | (uintptr_t)pb.V) & 15) == 0;
+    for (uint64_t base = gw * (32 / G); base < M; base += nw * (32 / G)) {  // warp-uniform
+        const uint64_t e = base + lane / G;
+        const bool act = e < M;
+        uint64_t i = 0, j = 0;
+        if (act) {
+            const uint64_t h1 = splitmix64(seed ^ (e * 0x9E3779B97F4A7C15ull));
+            const uint64_t h2 = splitmix64(h1);
+            if (e & 1) {
+                i = h1 % n;
+                j = h2 % n;
+            } else {
+                const uint64_t t = h1 % n;
+                uint64_t u = t + 1 + (h2 % window);
+                if (u >= n) u = t >= 1 + (h2 % window) ? t - 1 - (h2 % window) : 0;
+                i = perm ? perm[t] : t;
+                j = perm ? perm[u] : u;
+            }
         }
-        const float* a = Y32 + i * d;
-        const float* b = Y32 + j * d;
-        float* v = pb.V + e * d;
         float s = 0.0f;
-#pragma unroll 4
-        for (uint32_t c = lane; c < d; c += 32) {
-            const float t = a[c] - b[c];
-            s = fmaf(t, t, s);
-            v[c] = t;
+        if (act) {
+            const float* a = Y32 + i * d;
+            const float* b = Y32 + j * d;
+            float* v = pb.V + e * d;
+            if (v4) {
+#pragma unroll 2
+                for (uint32_t c = g; c < d / 4; c += G) {
+                    const float4 x = __ldg(reinterpret_cast<const float4*>(a) + c);
+                    const float4 y = __ldg(reinterpret_cast<const float4*>(b) + c);
+                    const float4 t = make_float4(x.x - y.x, x.y - y.y, x.z - y.z, x.w - y.w);
+                    s = fmaf(t.x, t.x, fmaf(t.y, t.y, fmaf(t.z, t.z, fmaf(t.w, t.w, s))));
+                    reinterpret_cast<float4*>(v)[c] = t;
+                }
+            } else {
+                for (uint32_t c = g; c < d; c += G) {
+                    const float t = a[c] - b[c];
+                    s = fmaf(t, t, s);
+                    v[c] = t;
+                }
+            }
         }
-        for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-        if (lane == 0) {
+#pragma unroll
+        for (uint32_t o = G / 2; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (act && g == 0) {
             const float delta = sqrtf(s);
             float t = 0.0f;
             if (!bad[i] && !bad[j] && delta > lo) t = fminf(delta, cap);
@@ -560,13 +580,15 @@ __global__ void __launch_bounds__(TRAIN_THREADS) train_step_kernel(const float* 
 // One Adam step on P from G (G is cleared for the next step), then the
 // power-iteration renormalisation P <- P / max(1, 1.02 s): s is the Rayleigh
 // quotient estimate of ||P||_2 from (P P^T)^32 (five normalised squarings, so
-// it converges when the leading eigenvalues are close).  One block; k <= 16.
+// it converges when the leading eigenvalues are close).  One block; k <= 16;
+// P is kept in shared memory (k * d floats, dynamic) between the phases.
 __global__ void adam_renorm_kernel(float* P, unsigned long long* G, float* m1, float* m2,
                                    uint32_t k, uint32_t d, float lr, float b1, float b2, float c1,
                                    float c2, int renorm, float* sigma_out) {
     __shared__ float M[16 * 16], A[16 * 16], B[16 * 16];
     __shared__ float v[16];
     __shared__ float lam;
+    extern __shared__ float sPa[];  // k * d
     const uint32_t nel = k * d;
     for (uint32_t e = threadIdx.x; e < nel; e += blockDim.x) {
         const float g = (float)((double)(long long)G[e] / kFix);
@@ -575,7 +597,9 @@ __global__ void adam_renorm_kernel(float* P, unsigned long long* G, float* m1, f
         const float b = b2 * m2[e] + (1.0f - b2) * g * g;
         m1[e] = a;
         m2[e] = b;
-        P[e] -= lr * (a / c1) / (sqrtf(b / c2) + 1e-8f);
+        const float pv = P[e] - lr * (a / c1) / (sqrtf(b / c2) + 1e-8f);
+        sPa[e] = pv;
+        if (!renorm) P[e] = pv;
     }
     if (!renorm) return;
     __syncthreads();
@@ -584,14 +608,13 @@ __global__ void adam_renorm_kernel(float* P, unsigned long long* G, float* m1, f
     for (uint32_t e = wid; e < k * k; e += nw) {
         const uint32_t a = e / k, b = e % k;
         float s = 0.0f;
-        for (uint32_t c = lane; c < d; c += 32) s = fmaf(P[a * d + c], P[b * d + c], s);
+        for (uint32_t c = lane; c < d; c += 32) s = fmaf(sPa[a * d + c], sPa[b * d + c], s);
         for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
         if (lane == 0) {
             M[e] = s;
             A[e] = s;
         }
     }
-    __syncthreads();
     // the k x k part runs in warp 0 (warp-level synchronisation only): five
     // normalised squarings, 8 power-iteration steps, the Rayleigh quotient
     if (wid == 0) {
@@ -641,7 +664,7 @@ __global__ void adam_renorm_kernel(float* P, unsigned long long* G, float* m1, f
     __syncthreads();
     const float sig = sqrtf(fmaxf(lam, 0.0f)) * 1.02f;
     const float scale = sig > 1.0f ? 1.0f / sig : 1.0f;
-    for (uint32_t e = threadIdx.x; e < nel; e += blockDim.x) P[e] *= scale;
+    for (uint32_t e = threadIdx.x; e < nel; e += blockDim.x) P[e] = sPa[e] * scale;
     if (threadIdx.x == 0 && sigma_out) *sigma_out = sig;
 }
 
@@ -756,6 +779,10 @@ int train_projection_dev(const float* Y32, const uint8_t* bad, uint64_t n, uint3
     const float b1 = 0.9f, b2 = 0.999f, lr = 0.02f;
     const size_t shm = train_smem_bytes(k, d);
     if (shm > 220 * 1024) return set_error(EJOIN_EUNSUPPORTED, "projection too large for training");
+    const size_t ashm = (size_t)k * d * sizeof(float);  // adam_renorm_kernel: P in shared memory
+    if (ashm > 220 * 1024) return set_error(EJOIN_EUNSUPPORTED, "projection too large for training");
+    EJ_CUDA(cudaFuncSetAttribute(adam_renorm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)ashm));
     auto step_fn = k <= 8 ? train_step_kernel<8> : train_step_kernel<16>;
     EJ_CUDA(cudaFuncSetAttribute(step_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
     const uint32_t tp = train_tile_pairs(d);
@@ -787,7 +814,7 @@ int train_projection_dev(const float* Y32, const uint8_t* bad, uint64_t n, uint3
             EJ_CUDA(cudaGetLastError());
             const float c1 = 1.0f - powf(b1, (float)(t_step + 1));
             const float c2 = 1.0f - powf(b2, (float)(t_step + 1));
-            adam_renorm_kernel<<<1, 256, 0, s>>>(P.p, G.p, m1.p, m2.p, k, d, lr, b1, b2, c1, c2, 1,
+            adam_renorm_kernel<<<1, 256, ashm, s>>>(P.p, G.p, m1.p, m2.p, k, d, lr, b1, b2, c1, c2, 1,
                                                  nullptr);
             EJ_CUDA(cudaGetLastError());
             note_launch(2);
@@ -871,7 +898,11 @@ extern "C" int ejoin_testing_renormalise(float* P, uint32_t k, uint32_t d, float
     EJ_TRY(dG.zero(s));
     EJ_CUDA(cudaMemcpyAsync(dP.p, P, nel * sizeof(float), cudaMemcpyHostToDevice, s));
     // zero gradient and learning rate: the Adam part leaves P unchanged
-    adam_renorm_kernel<<<1, 256, 0, s>>>(dP.p, dG.p, dZ.p, dZ.p + nel, k, d, 0.0f, 0.9f, 0.999f,
+    const size_t ashm = nel * sizeof(float);
+    if (ashm > 220 * 1024) return set_error(EJOIN_EUNSUPPORTED, "projection too large");
+    EJ_CUDA(cudaFuncSetAttribute(adam_renorm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)ashm));
+    adam_renorm_kernel<<<1, 256, ashm, s>>>(dP.p, dG.p, dZ.p, dZ.p + nel, k, d, 0.0f, 0.9f, 0.999f,
                                          1.0f, 1.0f, 1, dS.p);
     EJ_CUDA(cudaGetLastError());
     EJ_CUDA(cudaMemcpyAsync(P, dP.p, nel * sizeof(float), cudaMemcpyDeviceToHost, s));
