@@ -126,6 +126,21 @@ int ejoin_self_join(const double* points, uint64_t n, uint32_t d, double eps,
                     const ejoin_options* opt, int32_t* counts_out, uint64_t* total_out,
                     ejoin_stats* stats_out);
 
+/* Neighbour lists of the exact self-join (CSR): the points j with
+ * sqrt(d2(i, j)) <= eps for every point i in input order, ascending, i itself
+ * included -- list i has the length ejoin_self_join reports as count i.
+ *   offsets    n + 1 entries: list i is neighbors[offsets[i] .. offsets[i+1])
+ *   neighbors  capacity entries, may be NULL (then only offsets and the total
+ *              are computed); if capacity is below the total, offsets and
+ *              *total_out are filled, neighbors is not written and
+ *              EJOIN_ENOMEM is returned (call again with a larger buffer)
+ * Host or device pointers.  The total must stay below 2^31.  No reference
+ * counterpart: the reference returns only the total (gpu_join.cu:210-322);
+ * its result-set kernels (kernel_join.cu:139-162) are dead code. */
+int ejoin_neighbor_lists(const double* points, uint64_t n, uint32_t d, double eps,
+                         const ejoin_options* opt, uint64_t* offsets, uint32_t* neighbors,
+                         uint64_t capacity, uint64_t* total_out, ejoin_stats* stats_out);
+
 /* Counts for the query rows `rows[0..nq)` against all n points (same exact
  * predicate), computed with the FP64 direct kernel.  Used to check sampled
  * rows of large joins.  No reference counterpart (the reference has no

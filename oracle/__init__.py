@@ -60,6 +60,10 @@ def lib():
         L.oracle_self_join.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint32,
                                        ctypes.c_uint64, ctypes.c_double, ctypes.c_void_p,
                                        ctypes.c_void_p, ctypes.c_int]
+        L.oracle_neighbor_lists.restype = ctypes.c_int
+        L.oracle_neighbor_lists.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint32,
+                                            ctypes.c_uint64, ctypes.c_double, ctypes.c_void_p,
+                                            ctypes.c_void_p, ctypes.c_int]
         L.oracle_import_dataset.restype = ctypes.c_int
         L.oracle_import_dataset.argtypes = [ctypes.c_char_p, ctypes.c_uint32,
                                             ctypes.POINTER(ctypes.c_void_p),
@@ -97,6 +101,22 @@ def self_join(x, eps: float, nthreads: int = 0):
     if rc:
         raise RuntimeError(f"oracle_self_join failed: {rc}")
     return counts, int(total.value)
+
+
+def neighbor_lists(x, eps: float, nthreads: int = 0):
+    """CSR neighbour lists (ascending, self included): (offsets uint64[n+1],
+    neighbors uint32[total])."""
+    x = _as_rows(x)
+    n, d = x.shape
+    counts, total = self_join(x, eps, nthreads)
+    offsets = np.zeros(n + 1, dtype=np.uint64)
+    offsets[1:] = np.cumsum(counts.astype(np.uint64))
+    nb = np.zeros(max(total, 1), dtype=np.uint32)
+    rc = lib().oracle_neighbor_lists(x.ctypes.data, n, d, d, float(eps), offsets.ctypes.data,
+                                     nb.ctypes.data, nthreads)
+    if rc:
+        raise RuntimeError(f"oracle_neighbor_lists failed: {rc}")
+    return offsets, nb[:total]
 
 
 def query_counts(x, eps: float, rows, nthreads: int = 0):

@@ -152,6 +152,35 @@ int oracle_self_join(const double* x, uint64_t n, uint32_t d, uint64_t ld, doubl
     return 0;
 }
 
+/* Neighbour lists of the self-join (CSR): with offsets[] from the per-point
+ * counts (offsets[i+1] - offsets[i] = count of row i), row i's entries are
+ * the j in 0..n-1, ascending, with d2(x_i, x_j) <= T -- the predicate of
+ * kernel_join.cu:194 restated as d2 <= T, the same chain as the counts. */
+int oracle_neighbor_lists(const double* x, uint64_t n, uint32_t d, uint64_t ld, double eps,
+                          const uint64_t* offsets, uint32_t* nb, int nthreads)
+{
+    if (!x && n) return -1;
+    if (ld < d) return -2;
+    const double T = oracle_threshold(eps);
+    int overflow = 0;
+#ifdef _OPENMP
+    if (nthreads <= 0) nthreads = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads) reduction(|:overflow)
+#endif
+    for (int64_t i = 0; i < (int64_t)n; ++i) {
+        const double* a = x + (uint64_t)i * ld;
+        uint64_t o = offsets[i];
+        for (uint64_t j = 0; j < n; ++j)
+            if (pair_d2(a, x + j * ld, d) <= T) {
+                if (o < offsets[i + 1]) nb[o] = (uint32_t)j;
+                else overflow = 1;
+                ++o;
+            }
+    }
+    (void)nthreads;
+    return overflow ? -3 : 0;
+}
+
 /* Restatement of dataset.cu:10-39.  Reads values with the same pair of
  * fscanf formats, closes a row every `dim` values and drops a trailing
  * partial row.  On success *out is a malloc'd row-major n x dim array

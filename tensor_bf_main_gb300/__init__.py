@@ -104,7 +104,7 @@ EXPORTED = [
     "ejoin_default_options", "ejoin_self_join", "ejoin_query_counts", "ejoin_train_projection",
     "ejoin_certify_spectral_norm", "ejoin_threshold", "ejoin_import_dataset",
     "ejoin_import_binary", "ejoin_free", "ejoin_last_error", "ejoin_version",
-    "ejoin_gpu_join_main_brute_force", "ejoin_self_join_noalloc",
+    "ejoin_gpu_join_main_brute_force", "ejoin_self_join_noalloc", "ejoin_neighbor_lists",
 ]
 
 # Test hooks declared in include/ejoin_testing.h.
@@ -127,6 +127,8 @@ def load_library(path: str = LIB_PATH):
     L.ejoin_self_join.argtypes = [vp, u64, u32, dbl, ctypes.POINTER(Options), vp, ctypes.POINTER(u64),
                                   ctypes.POINTER(Stats)]
     L.ejoin_query_counts.argtypes = [vp, u64, u32, dbl, vp, u64, ctypes.POINTER(Options), vp]
+    L.ejoin_neighbor_lists.argtypes = [vp, u64, u32, dbl, ctypes.POINTER(Options), vp, vp, u64,
+                                       ctypes.POINTER(u64), ctypes.POINTER(Stats)]
     L.ejoin_train_projection.argtypes = [vp, u64, u32, dbl, ctypes.POINTER(Options), vp,
                                          ctypes.POINTER(dbl), ctypes.POINTER(Stats)]
     L.ejoin_certify_spectral_norm.argtypes = [vp, u32, u32, ctypes.POINTER(dbl)]
@@ -221,6 +223,26 @@ def self_join(points, eps: float, precision="auto", proj_k: int = 0, device: int
                              ctypes.byref(st)))
     del keep
     return out, int(total.value), (st.as_dict() if stats else None)
+
+
+def neighbor_lists(points, eps: float, precision="auto", proj_k: int = 0, device: int = 0, **kw):
+    """Neighbour lists of the exact self-join (CSR, input order, ascending,
+    self included).  Returns (offsets uint64[n+1], neighbors uint32[total],
+    stats_dict).  Two library calls: the first sizes the lists."""
+    L = load_library()
+    ptr, n, d, ld, keep = _points_arg(points)
+    o = _options(device=device, precision=precision, proj_k=proj_k, ld=ld if ld != d else 0, **kw)
+    offsets = np.zeros(n + 1, dtype=np.uint64)
+    total = ctypes.c_uint64(0)
+    st = Stats()
+    _check(L.ejoin_neighbor_lists(ptr, n, d, float(eps), ctypes.byref(o), offsets.ctypes.data,
+                                  None, 0, ctypes.byref(total), ctypes.byref(st)))
+    nb = np.zeros(max(int(total.value), 1), dtype=np.uint32)
+    _check(L.ejoin_neighbor_lists(ptr, n, d, float(eps), ctypes.byref(o), offsets.ctypes.data,
+                                  nb.ctypes.data, nb.shape[0], ctypes.byref(total),
+                                  ctypes.byref(st)))
+    del keep
+    return offsets, nb[: int(total.value)], st.as_dict()
 
 
 def query_counts(points, eps: float, rows, device: int = 0):

@@ -30,7 +30,7 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompil
               "-I", INCLUDE, "-I", CSRC, "-diag-suppress", "177"]
 
 CU_SOURCES = ["api.cu", "k_direct.cu", "k_prep.cu", "k_dmma.cu", "k_umma.cu", "k_misc.cu",
-              "k_learn.cu", "k_noalloc.cu"]
+              "k_learn.cu", "k_noalloc.cu", "k_lists.cu"]
 CPP_SOURCES = ["host.cpp"]
 
 

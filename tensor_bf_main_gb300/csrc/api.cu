@@ -181,6 +181,7 @@ struct Join {
     ejoin_stats* st;
     int32_t* counts;         // device, >= n_pad entries, packed-row order
     const uint32_t* perm;    // packed row -> original row (null = identity)
+    const Emit* em = nullptr;  // neighbour-list emission (null: counts only)
 };
 
 static uint64_t round_up(uint64_t v, uint64_t m) { return (v + m - 1) / m * m; }
@@ -247,7 +248,7 @@ static int run_direct(Join& J) {
     EventTimer t;
     EJ_CUDA(cudaMemsetAsync(J.counts, 0, J.n * sizeof(int32_t), J.s));
     t.start(J.s);
-    EJ_TRY(launch_direct_selfjoin(J.X, J.n, J.d, J.T, J.counts, J.s));
+    EJ_TRY(launch_direct_selfjoin(J.X, J.n, J.d, J.T, J.counts, J.em, J.s));
     t.stop(J.s);
     J.st->ms_gram = t.ms();
     const double pairs = (double)J.n * (double)(J.n + 1) / 2.0;
@@ -257,6 +258,8 @@ static int run_direct(Join& J) {
 }
 
 static int run_dmma(Join& J) {
+    // pair emission runs on the exact judge (the DMMA epilogue only counts)
+    if (J.em) return run_direct(J);
     EventTimer tp, tg, tr;
     tp.start(J.s);
     DBuf<uint8_t> bad;
@@ -398,7 +401,8 @@ static int run_screen16(Join& J, Fmt fmt, bool split, Learned& L) {
     if (!fp32_ok) return run_dmma(J);
     // rows padded to whole 128 x 256 blocks of the Gram kernel
     const uint64_t n_pad = round_up(J.n, 256);
-    if (J.opt.proj_k) EJ_TRY(prepare_learned(J, Y32.p, Yerr.p, bad.p, n_pad, L));
+    // a second pass of the same join (pair emission) reuses the ordering
+    if (J.opt.proj_k && L.k == 0) EJ_TRY(prepare_learned(J, Y32.p, Yerr.p, bad.p, n_pad, L));
     tp.start(J.s);
     ScreenParams P;
     const bool fp8 = (fmt == Fmt::E4M3);
@@ -465,8 +469,8 @@ static int run_screen16(Join& J, Fmt fmt, bool split, Learned& L) {
     const void* Qp = fp8 ? (const void*)Q8.p : (const void*)Q.p;
     auto screen = [&](BandPair* band, uint64_t cap, DevStatus* st) {
         return launch_gram16(Qp, Aug.p, n_pad, P, work.p, nwork, tmax.p, beta.p, tsig.p, sig.p,
-                             J.counts,
-                             reinterpret_cast<BandRec*>(band), cap, st, J.sms, J.s);
+                             J.counts, reinterpret_cast<BandRec*>(band), cap, st, J.em, J.sms,
+                             J.s);
     };
     Recheck32 R;
     R.Xf = Xf.p;
@@ -483,7 +487,7 @@ static int run_screen16(Join& J, Fmt fmt, bool split, Learned& L) {
         EJ_TRY(launch_band_expand(reinterpret_cast<const BandRec*>(band), nrec, pairs.p, npairs,
                                   J.s));
         return launch_band_recheck2(J.X, J.n, J.d, J.perm, J.T, R, pairs.p, npairs, J.counts, st,
-                                    J.s);
+                                    J.em, J.s);
     };
     // generous first queue (capped at a quarter of free memory by
     // band_budget): an overflow re-runs the whole screen
@@ -500,9 +504,19 @@ static int resolve_precision(int p, uint32_t d) {
     return p;
 }
 
+// Neighbour-list request of self_join_impl: offsets [n + 1] and neighbors
+// [capacity] (host or device; neighbors may be null: offsets only).  status
+// becomes EJOIN_ENOMEM when capacity is below the total (lists not written).
+struct ListsReq {
+    uint64_t* offsets;
+    uint32_t* neighbors;
+    uint64_t capacity;
+    int status = EJOIN_OK;
+};
+
 static int self_join_impl(const double* points, uint64_t n, uint32_t d, double eps,
                           const ejoin_options* opt_in, int32_t* counts_out, uint64_t* total_out,
-                          ejoin_stats* stats_out) {
+                          ejoin_stats* stats_out, ListsReq* lists = nullptr) {
     ejoin_options opt;
     ejoin_default_options(&opt);
     if (opt_in) {
@@ -554,18 +568,22 @@ static int self_join_impl(const double* points, uint64_t n, uint32_t d, double e
     J.counts = cbuf.p;
     int prec = resolve_precision(opt.precision, d);
     stats.precision = prec;
-    if (n > 0 && !isnan(T) && T >= 0.0) {
-        EJ_TRY(stage_points(points, n, d, ld, xbuf, &J.X, s));
-        if (isinf(T)) prec = EJOIN_FP64_DIRECT;  // every non-NaN pair counts: judge only
+    const bool run = n > 0 && !isnan(T) && T >= 0.0;
+    auto run_once = [&]() -> int {
         switch (prec) {
-            case EJOIN_FP64_DIRECT: EJ_TRY(run_direct(J)); break;
-            case EJOIN_FP64_DMMA: EJ_TRY(run_dmma(J)); break;
-            case EJOIN_FP16: EJ_TRY(run_screen16(J, Fmt::FP16, false, learned)); break;
-            case EJOIN_BF16: EJ_TRY(run_screen16(J, Fmt::BF16, false, learned)); break;
-            case EJOIN_BF16_SPLIT: EJ_TRY(run_screen16(J, Fmt::BF16, true, learned)); break;
-            case EJOIN_FP8_E4M3: EJ_TRY(run_screen16(J, Fmt::E4M3, false, learned)); break;
+            case EJOIN_FP64_DIRECT: return run_direct(J);
+            case EJOIN_FP64_DMMA: return run_dmma(J);
+            case EJOIN_FP16: return run_screen16(J, Fmt::FP16, false, learned);
+            case EJOIN_BF16: return run_screen16(J, Fmt::BF16, false, learned);
+            case EJOIN_BF16_SPLIT: return run_screen16(J, Fmt::BF16, true, learned);
+            case EJOIN_FP8_E4M3: return run_screen16(J, Fmt::E4M3, false, learned);
             default: return set_error(EJOIN_EINVAL, "unknown precision %d", prec);
         }
+    };
+    if (run) {
+        EJ_TRY(stage_points(points, n, d, ld, xbuf, &J.X, s));
+        if (isinf(T)) prec = EJOIN_FP64_DIRECT;  // every non-NaN pair counts: judge only
+        EJ_TRY(run_once());
     }
     DBuf<unsigned long long> tot;
     EJ_TRY(tot.alloc(1, s, "total"));
@@ -589,6 +607,60 @@ static int self_join_impl(const double* points, uint64_t n, uint32_t d, double e
     }
     unsigned long long total = 0;
     EJ_CUDA(cudaMemcpyAsync(&total, tot.p, sizeof total, cudaMemcpyDeviceToHost, s));
+    if (lists) {
+        // offsets from the counts (input order); the lists from a second pass
+        // of the same join that emits its pairs (capacities: at most one
+        // record or pair per counted pair)
+        EJ_CUDA(cudaStreamSynchronize(s));
+        DBuf<int32_t> corig;
+        const int32_t* cin = J.counts;
+        if (J.perm && n) {
+            EJ_TRY(corig.alloc(n, s, "counts in input order"));
+            EJ_TRY(scatter_counts(J.counts, J.perm, n, corig.p, s));
+            cin = corig.p;
+        }
+        DBuf<unsigned long long> off;
+        EJ_TRY(off.alloc(n + 1, s, "list offsets"));
+        EJ_TRY(csr_offsets(cin, n, total, off.p, s));
+        const bool off_dev = is_device_ptr(lists->offsets);
+        EJ_CUDA(cudaMemcpyAsync(lists->offsets, off.p, (n + 1) * sizeof(uint64_t),
+                                off_dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s));
+        if (lists->neighbors && lists->capacity < total) {
+            lists->status = EJOIN_ENOMEM;
+            set_error(EJOIN_ENOMEM, "neighbour buffer holds %llu of %llu entries",
+                      (unsigned long long)lists->capacity, (unsigned long long)total);
+        } else if (lists->neighbors && total > 0) {
+            DBuf<BandRec> inq;
+            DBuf<BandPair> pq;
+            DBuf<unsigned long long> cnt;
+            EJ_TRY(inq.alloc(total, s, "emitted records"));
+            EJ_TRY(pq.alloc(total, s, "emitted pairs"));
+            EJ_TRY(cnt.alloc(2, s, "emission counters"));
+            EJ_TRY(cnt.zero(s));
+            Emit em{inq.p, total, pq.p, total, cnt.p};
+            J.em = &em;
+            EJ_CUDA(cudaMemsetAsync(J.counts, 0, n_pad * sizeof(int32_t), s));
+            EJ_TRY(run_once());
+            J.em = nullptr;
+            unsigned long long hc[2];
+            EJ_CUDA(cudaMemcpyAsync(hc, cnt.p, sizeof hc, cudaMemcpyDeviceToHost, s));
+            EJ_CUDA(cudaStreamSynchronize(s));
+            if (hc[0] > total || hc[1] > total)
+                return set_error(EJOIN_EINTERNAL, "neighbour lists: emission overflow");
+            const bool nb_dev = is_device_ptr(lists->neighbors);
+            DBuf<uint32_t> nbuf;
+            uint32_t* nb = lists->neighbors;
+            if (!nb_dev) {
+                EJ_TRY(nbuf.alloc(total, s, "neighbour lists"));
+                nb = nbuf.p;
+            }
+            EJ_TRY(csr_fill(off.p, n, total, inq.p, hc[0], pq.p, hc[1], J.perm, nb, s));
+            if (!nb_dev)
+                EJ_CUDA(cudaMemcpyAsync(lists->neighbors, nb, total * sizeof(uint32_t),
+                                        cudaMemcpyDeviceToHost, s));
+        }
+        EJ_CUDA(cudaStreamSynchronize(s));
+    }
     tt.stop(s);
     EJ_CUDA(cudaStreamSynchronize(s));
     stats.ms_total = tt.ms();
@@ -626,6 +698,16 @@ int ejoin_self_join(const double* points, uint64_t n, uint32_t d, double eps,
                     ejoin_stats* stats_out) {
     clear_error();
     return self_join_impl(points, n, d, eps, opt, counts_out, total_out, stats_out);
+}
+
+int ejoin_neighbor_lists(const double* points, uint64_t n, uint32_t d, double eps,
+                         const ejoin_options* opt, uint64_t* offsets, uint32_t* neighbors,
+                         uint64_t capacity, uint64_t* total_out, ejoin_stats* stats_out) {
+    clear_error();
+    if (!offsets) return set_error(EJOIN_EINVAL, "offsets is NULL");
+    ListsReq req{offsets, neighbors, capacity};
+    EJ_TRY(self_join_impl(points, n, d, eps, opt, nullptr, total_out, stats_out, &req));
+    return req.status;
 }
 
 int ejoin_query_counts(const double* points, uint64_t n, uint32_t d, double eps,

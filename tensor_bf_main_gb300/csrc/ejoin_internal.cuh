@@ -121,6 +121,25 @@ struct BandRec {
     uint32_t pad;
 };
 
+// Pair emission for neighbour lists (null when only counts are wanted):
+// in-records of the tensor-core screen and single pairs (band hits, direct
+// judge hits), appended through the counters cnt[0] / cnt[1]; entries beyond
+// a capacity are dropped and detected by the caller from the counters.
+struct Emit {
+    BandRec* inq;
+    uint64_t inq_cap;
+    BandPair* pq;
+    uint64_t pq_cap;
+    unsigned long long* cnt;  // [0] in-records, [1] pairs
+};
+
+// Kernels take an Emit by value; cnt == null means no emission.
+__device__ __forceinline__ void emit_pair(const Emit& em, BandPair bp) {
+    if (!em.cnt) return;
+    const unsigned long long slot = atomicAdd(&em.cnt[1], 1ull);
+    if (slot < em.pq_cap) em.pq[slot] = bp;
+}
+
 // Status word written by kernels whose waits are bounded.
 struct DevStatus {
     unsigned int timeout;    // a bounded wait expired (where: code below)
@@ -229,6 +248,7 @@ struct JoinCtx;  // api.cu
 
 // k_direct.cu
 int launch_direct_selfjoin(const double* X, uint64_t n, uint32_t d, double T, int32_t* counts,
+                           const Emit* em,
                            cudaStream_t s);
 int launch_direct_query(const double* X, uint64_t n, uint32_t d, double T, const uint64_t* rows,
                         uint64_t nq, int32_t* counts, cudaStream_t s);
@@ -248,7 +268,8 @@ int launch_dmma_join(const double* Y, uint64_t n_pad, uint32_t dp, const double*
 int launch_gram16(const void* Q, const void* aug, uint64_t n_pad, const ScreenParams& P,
                   const uint2* work, uint64_t nwork, const float* tmax, const float* beta,
                   const float* tsig, const float* sig,
-                  int32_t* counts, BandRec* band, uint64_t band_cap, DevStatus* st, int num_sms,
+                  int32_t* counts, BandRec* band, uint64_t band_cap, DevStatus* st, const Emit* em,
+                  int num_sms,
                   cudaStream_t s);
 
 // k_misc.cu
@@ -284,9 +305,18 @@ int cert_spectral_norm(const float* P, uint32_t k, uint32_t d, double* out);
 // Expands band records into pairs (any order); out holds Sum popc(mask).
 int launch_band_expand(const BandRec* rec, uint64_t nrec, BandPair* out, uint64_t cap,
                        cudaStream_t s);
+// k_lists.cu: CSR neighbour lists.  offsets [n + 1] from the per-point counts
+// (input order); csr_fill scatters the emitted pairs (packed indices, perm:
+// packed -> input row) into nb [total] and sorts every list.
+int csr_offsets(const int32_t* counts, uint64_t n, uint64_t total, unsigned long long* offsets,
+                cudaStream_t s);
+int csr_fill(const unsigned long long* offsets, uint64_t n, uint64_t total, const BandRec* inq,
+             uint64_t nin, const BandPair* pq, uint64_t np, const uint32_t* perm, uint32_t* nb,
+             cudaStream_t s);
+
 int launch_band_recheck2(const double* X, uint64_t n, uint32_t d, const uint32_t* perm, double T,
                          const Recheck32& R, const BandPair* band, uint64_t nband, int32_t* counts,
-                         DevStatus* st, cudaStream_t s);
+                         DevStatus* st, const Emit* em, cudaStream_t s);
 
 // k_prep.cu
 // Centring statistics.  bad[i] = 1 for rows with a non-finite coordinate;

@@ -67,7 +67,7 @@ __device__ __forceinline__ void tile_chains(double acc[4][4], double (*SA)[PADK]
 __global__ void __launch_bounds__(256) direct_selfjoin_kernel(const double* __restrict__ X,
                                                               uint64_t n, uint32_t d, double T,
                                                               uint64_t nT, uint64_t tiles,
-                                                              int32_t* counts) {
+                                                              int32_t* counts, Emit em) {
     __shared__ double SA[KC][PADK];
     __shared__ double SB[KC][PADK];
     __shared__ int rowc[TB], colc[TB];
@@ -102,6 +102,7 @@ __global__ void __launch_bounds__(256) direct_selfjoin_kernel(const double* __re
             if (i < n && j < n && acc[rr][cc] <= T) {
                 atomicAdd(&rowc[ty + 16 * rr], 1);
                 if (!diag) atomicAdd(&colc[tx + 16 * cc], 1);
+                emit_pair(em, BandPair{(uint32_t)i, (uint32_t)j | (diag ? 0u : kBandBoth)});
             }
         }
     }
@@ -219,7 +220,8 @@ __global__ void __launch_bounds__(256) band_recheck_thread_kernel(const double* 
                                                                   double T, Recheck32 R,
                                                                   const BandPair* __restrict__ band,
                                                                   uint64_t nband, uint64_t n,
-                                                                  int32_t* counts, DevStatus* st) {
+                                                                  int32_t* counts, DevStatus* st,
+                                                                  Emit em) {
     unsigned hits = 0, exact_runs = 0;
     for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < nband;
          e += (uint64_t)gridDim.x * blockDim.x) {
@@ -241,6 +243,7 @@ __global__ void __launch_bounds__(256) band_recheck_thread_kernel(const double* 
         if (recheck_decide(X, d, perm, T, R, i, j, (s0 + s1) + (s2 + s3), exact_runs)) {
             atomicAdd(&counts[i], 1);
             if (bp.j & kBandBoth) atomicAdd(&counts[j], 1);
+            emit_pair(em, bp);
             ++hits;
         }
     }
@@ -256,7 +259,8 @@ __global__ void __launch_bounds__(256) band_recheck_warp_kernel(const double* __
                                                                 double T, Recheck32 R,
                                                                 const BandPair* __restrict__ band,
                                                                 uint64_t nband, uint64_t n,
-                                                                int32_t* counts, DevStatus* st) {
+                                                                int32_t* counts, DevStatus* st,
+                                                                Emit em) {
     const uint32_t lane = threadIdx.x & 31;
     const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / 32;
     const uint64_t nwarps = (uint64_t)gridDim.x * blockDim.x / 32;
@@ -286,6 +290,7 @@ __global__ void __launch_bounds__(256) band_recheck_warp_kernel(const double* __
         if (valid && recheck_decide(X, d, perm, T, R, mi, mj, mine, exact_runs)) {
             atomicAdd(&counts[mi], 1);
             if (bp.j & kBandBoth) atomicAdd(&counts[mj], 1);
+            emit_pair(em, bp);
             ++hits;
         }
     }
@@ -296,18 +301,19 @@ __global__ void __launch_bounds__(256) band_recheck_warp_kernel(const double* __
 
 int launch_band_recheck2(const double* X, uint64_t n, uint32_t d, const uint32_t* perm, double T,
                          const Recheck32& R, const BandPair* band, uint64_t nband, int32_t* counts,
-                         DevStatus* st, cudaStream_t s) {
+                         DevStatus* st, const Emit* em, cudaStream_t s) {
     if (nband == 0) return EJOIN_OK;
+    const Emit e = em ? *em : Emit{nullptr, 0, nullptr, 0, nullptr};
     // measured on GB300: a thread per pair wins for rows of <= 256 bytes, a
     // warp per pair (more pairs in flight per load) for longer rows
     const bool thread = d <= 64 && d % 4 == 0 && ((uintptr_t)R.Xf & 15) == 0;
     if (thread) {
         const unsigned blocks = (unsigned)std::min<uint64_t>((nband + 255) / 256, 152ull * 32);
-        band_recheck_thread_kernel<<<blocks, 256, 0, s>>>(X, d, perm, T, R, band, nband, n, counts, st);
+        band_recheck_thread_kernel<<<blocks, 256, 0, s>>>(X, d, perm, T, R, band, nband, n, counts, st, e);
     } else {
         const uint64_t warps = (nband + 31) / 32;
         const unsigned blocks = (unsigned)std::min<uint64_t>((warps + 7) / 8, 152ull * 64);
-        band_recheck_warp_kernel<<<blocks, 256, 0, s>>>(X, d, perm, T, R, band, nband, n, counts, st);
+        band_recheck_warp_kernel<<<blocks, 256, 0, s>>>(X, d, perm, T, R, band, nband, n, counts, st, e);
     }
     EJ_CUDA(cudaGetLastError());
     note_launch();
@@ -315,7 +321,7 @@ int launch_band_recheck2(const double* X, uint64_t n, uint32_t d, const uint32_t
 }
 
 int launch_direct_selfjoin(const double* X, uint64_t n, uint32_t d, double T, int32_t* counts,
-                           cudaStream_t s) {
+                           const Emit* em, cudaStream_t s) {
     if (n == 0) return EJOIN_OK;
     uint64_t nT = (n + TB - 1) / TB;
     uint64_t tiles = nT * (nT + 1) / 2;
@@ -324,8 +330,9 @@ int launch_direct_selfjoin(const double* X, uint64_t n, uint32_t d, double T, in
     if (gy > 65535)
         return set_error(EJOIN_EUNSUPPORTED, "direct join: %llu tile pairs exceed the grid",
                          (unsigned long long)tiles);
+    const Emit e = em ? *em : Emit{nullptr, 0, nullptr, 0, nullptr};
     direct_selfjoin_kernel<<<dim3((unsigned)gx, (unsigned)gy), 256, 0, s>>>(X, n, d, T, nT, tiles,
-                                                                            counts);
+                                                                            counts, e);
     EJ_CUDA(cudaGetLastError());
     note_launch();
     return EJOIN_OK;

@@ -83,6 +83,7 @@ struct GramArgs {
     uint32_t split;  // hi + lo
     uint32_t fmt;    // 16-bit operands: 0 = FP16, 1 = BF16 (instruction-descriptor format)
     uint32_t lrun;   // log2 of the run length: entries a CTA takes consecutively
+    Emit em;         // neighbour-list emission (em.cnt null: counts only)
 };
 
 __device__ __forceinline__ uint2 entry_or_end(const GramArgs& a, uint64_t u) {
@@ -219,6 +220,29 @@ __device__ __forceinline__ void stage_band(const GramArgs& a, Ctl& S, uint32_t b
             atomicAdd(&a.st->band_pairs, (unsigned long long)__popc(m));
             if (g < a.band_cap) a.band[g] = r;
         }
+    }
+}
+
+// In-records of the two chunks of a warp (neighbour lists): a lane with
+// in-pairs in a chunk appends (row, first column | both, mask); one global
+// reservation per warp.
+__device__ __forceinline__ void emit_in(const GramArgs& a, uint32_t in0, uint32_t in1,
+                                        uint32_t row, uint32_t col0, bool diag, uint32_t lane) {
+    const uint32_t b0 = __ballot_sync(FULL, in0 != 0), b1 = __ballot_sync(FULL, in1 != 0);
+    const uint32_t n0 = __popc(b0), tot = n0 + __popc(b1);
+    if (!tot) return;
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(&a.em.cnt[0], (unsigned long long)tot);
+    base = __shfl_sync(FULL, base, 0);
+    const uint32_t lt = (1u << lane) - 1u;
+    const uint32_t flag = diag ? 0u : kBandBoth;
+    if (in0) {
+        const unsigned long long slot = base + __popc(b0 & lt);
+        if (slot < a.em.inq_cap) a.em.inq[slot] = BandRec{row, col0 | flag, in0, 0u};
+    }
+    if (in1) {
+        const unsigned long long slot = base + n0 + __popc(b1 & lt);
+        if (slot < a.em.inq_cap) a.em.inq[slot] = BandRec{row, (col0 + 32u) | flag, in1, 0u};
     }
 }
 
@@ -468,6 +492,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 }
                 const int rowcnt = __popc(in0) + __popc(in1);
                 if (rowcnt) atomicAdd(&racc[q * 32u + lane], rowcnt);
+                if (a.em.cnt) emit_in(a, in0, in1, row, col0, diag, lane);
             }
             __syncwarp();
             if (lane == 0) ptx::mbar_arrive(&S.ebar[b]);
@@ -539,7 +564,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 int launch_gram16(const void* Q, const void* aug, uint64_t n_pad, const ScreenParams& P,
                   const uint2* work, uint64_t nwork, const float* tmax, const float* beta,
                   const float* tsig, const float* sig,
-                  int32_t* counts, BandRec* band, uint64_t band_cap, DevStatus* st, int num_sms,
+                  int32_t* counts, BandRec* band, uint64_t band_cap, DevStatus* st, const Emit* em,
+                  int num_sms,
                   cudaStream_t s) {
     if (nwork == 0) return EJOIN_OK;
     const bool fp8 = P.fmt == Fmt::E4M3;
@@ -564,6 +590,7 @@ int launch_gram16(const void* Q, const void* aug, uint64_t n_pad, const ScreenPa
     a.beta = beta;
     a.tsig = fp8 ? tsig : nullptr;
     a.sig = fp8 ? sig : nullptr;
+    a.em = em ? *em : Emit{nullptr, 0, nullptr, 0, nullptr};
     if (!tmax || !beta || (fp8 && (!tsig || !sig))) return set_error(EJOIN_EINTERNAL, "gram: margins missing");
     a.counts = counts;
     a.band = band;

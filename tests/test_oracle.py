@@ -70,3 +70,17 @@ def test_oracle_query_counts(oracle_mod):
     full, _ = oracle_mod.self_join(x, 0.6)
     rows = np.array([0, 5, 299, 17])
     assert oracle_mod.query_counts(x, 0.6, rows).tolist() == full[rows].tolist()
+
+
+def test_oracle_neighbor_lists_golden(oracle_mod):
+    """The oracle's lists have the golden counts as lengths and hold exactly
+    the pairs a direct restatement of the predicate selects."""
+    g = json.load(open(os.path.join(GOLDEN, "join_golden.json")))["files"]["test100"]
+    x = np.fromfile(os.path.join(GOLDEN, "test100.f64"), dtype="<f8").reshape(-1, g["d"])
+    case = g["cases"][len(g["cases"]) // 2]
+    off, nb = oracle_mod.neighbor_lists(x, case["eps"])
+    assert np.diff(off.astype(np.int64)).tolist() == case["counts"]
+    T = oracle_mod.threshold(case["eps"])
+    for i in range(0, x.shape[0], 7):
+        ref = [j for j in range(x.shape[0]) if oracle_mod.pair_d2(x[i], x[j]) <= T]
+        assert nb[off[i]:off[i + 1]].tolist() == ref
