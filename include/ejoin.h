@@ -141,6 +141,17 @@ int ejoin_neighbor_lists(const double* points, uint64_t n, uint32_t d, double ep
                          const ejoin_options* opt, uint64_t* offsets, uint32_t* neighbors,
                          uint64_t capacity, uint64_t* total_out, ejoin_stats* stats_out);
 
+/* Join of two point sets: for every query row q, the number of points j with
+ * sqrt(d2(q, x_j)) <= eps (d2 formed as the reference's FP64 kernel forms it,
+ * kernel_join.cu:168-200).  queries nq x d and points n x d, row-major with
+ * the same row stride opt->ld, host or device; counts_out nq int32 (host or
+ * device, may be NULL); total_out their sum.  Same precision modes as
+ * ejoin_self_join, counts exact in every mode; opt->proj_k must be 0.  No
+ * reference counterpart (the reference joins a set with itself only). */
+int ejoin_join_counts(const double* queries, uint64_t nq, const double* points, uint64_t n,
+                      uint32_t d, double eps, const ejoin_options* opt, int32_t* counts_out,
+                      uint64_t* total_out, ejoin_stats* stats_out);
+
 /* Counts for the query rows `rows[0..nq)` against all n points (same exact
  * predicate), computed with the FP64 direct kernel.  Used to check sampled
  * rows of large joins.  No reference counterpart (the reference has no

@@ -60,6 +60,10 @@ def lib():
         L.oracle_self_join.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint32,
                                        ctypes.c_uint64, ctypes.c_double, ctypes.c_void_p,
                                        ctypes.c_void_p, ctypes.c_int]
+        L.oracle_cross_counts.restype = ctypes.c_int
+        L.oracle_cross_counts.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p,
+                                          ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint64,
+                                          ctypes.c_double, ctypes.c_void_p, ctypes.c_int]
         L.oracle_neighbor_lists.restype = ctypes.c_int
         L.oracle_neighbor_lists.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint32,
                                             ctypes.c_uint64, ctypes.c_double, ctypes.c_void_p,
@@ -101,6 +105,19 @@ def self_join(x, eps: float, nthreads: int = 0):
     if rc:
         raise RuntimeError(f"oracle_self_join failed: {rc}")
     return counts, int(total.value)
+
+
+def cross_counts(q, x, eps: float, nthreads: int = 0):
+    """For every query row, the number of points within eps."""
+    q, x = _as_rows(q), _as_rows(x)
+    if q.shape[1] != x.shape[1]:
+        raise ValueError("queries and points differ in dimension")
+    counts = np.zeros(q.shape[0], dtype=np.int32)
+    rc = lib().oracle_cross_counts(q.ctypes.data, q.shape[0], x.ctypes.data, x.shape[0], x.shape[1],
+                                   x.shape[1], float(eps), counts.ctypes.data, nthreads)
+    if rc:
+        raise RuntimeError(f"oracle_cross_counts failed: {rc}")
+    return counts
 
 
 def neighbor_lists(x, eps: float, nthreads: int = 0):

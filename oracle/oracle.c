@@ -140,6 +140,35 @@ int oracle_query_counts(const double* x, uint64_t n, uint32_t d, uint64_t ld,
     return 0;
 }
 
+/* Join of two point sets: for every query row q (nq x d, stride ld), the
+ * points x_j (n x d, stride ld) with d2(q, x_j) <= T, the same chain as the
+ * self-join ((q - x)^2 and (x - q)^2 are bitwise equal). */
+int oracle_cross_counts(const double* q, uint64_t nq, const double* x, uint64_t n, uint32_t d,
+                        uint64_t ld, double eps, int32_t* counts, int nthreads)
+{
+    if ((!q && nq) || (!x && n)) return -1;
+    if (ld < d) return -2;
+    const double T = oracle_threshold(eps);
+#ifdef _OPENMP
+    if (nthreads <= 0) nthreads = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads)
+#endif
+    for (int64_t qi = 0; qi < (int64_t)nq; ++qi) {
+        const double* a = q + (uint64_t)qi * ld;
+        int64_t c = 0;
+        uint64_t j = 0;
+        double d2[4];
+        for (; j + 4 <= n; j += 4) {
+            pair_d2_x4(a, x + j * ld, x + (j + 1) * ld, x + (j + 2) * ld, x + (j + 3) * ld, d, d2);
+            c += (d2[0] <= T) + (d2[1] <= T) + (d2[2] <= T) + (d2[3] <= T);
+        }
+        for (; j < n; ++j) c += (pair_d2(a, x + j * ld, d) <= T);
+        counts[qi] = (int32_t)c;
+    }
+    (void)nthreads;
+    return 0;
+}
+
 /* Full self-join: per-point counts (self included) and their uint64 sum. */
 int oracle_self_join(const double* x, uint64_t n, uint32_t d, uint64_t ld, double eps,
                      int32_t* counts, uint64_t* total, int nthreads)

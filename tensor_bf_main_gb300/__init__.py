@@ -105,6 +105,7 @@ EXPORTED = [
     "ejoin_certify_spectral_norm", "ejoin_threshold", "ejoin_import_dataset",
     "ejoin_import_binary", "ejoin_free", "ejoin_last_error", "ejoin_version",
     "ejoin_gpu_join_main_brute_force", "ejoin_self_join_noalloc", "ejoin_neighbor_lists",
+    "ejoin_join_counts",
 ]
 
 # Test hooks declared in include/ejoin_testing.h.
@@ -129,6 +130,8 @@ def load_library(path: str = LIB_PATH):
     L.ejoin_query_counts.argtypes = [vp, u64, u32, dbl, vp, u64, ctypes.POINTER(Options), vp]
     L.ejoin_neighbor_lists.argtypes = [vp, u64, u32, dbl, ctypes.POINTER(Options), vp, vp, u64,
                                        ctypes.POINTER(u64), ctypes.POINTER(Stats)]
+    L.ejoin_join_counts.argtypes = [vp, u64, vp, u64, u32, dbl, ctypes.POINTER(Options), vp,
+                                    ctypes.POINTER(u64), ctypes.POINTER(Stats)]
     L.ejoin_train_projection.argtypes = [vp, u64, u32, dbl, ctypes.POINTER(Options), vp,
                                          ctypes.POINTER(dbl), ctypes.POINTER(Stats)]
     L.ejoin_certify_spectral_norm.argtypes = [vp, u32, u32, ctypes.POINTER(dbl)]
@@ -243,6 +246,24 @@ def neighbor_lists(points, eps: float, precision="auto", proj_k: int = 0, device
                                   ctypes.byref(st)))
     del keep
     return offsets, nb[: int(total.value)], st.as_dict()
+
+
+def join_counts(queries, points, eps: float, precision="auto", device: int = 0, **kw):
+    """Join of two point sets: for every query row, the number of points within
+    eps (exact).  Returns (counts int32[nq], total, stats_dict)."""
+    L = load_library()
+    qptr, nq, dq, ldq, keepq = _points_arg(queries)
+    ptr, n, d, ld, keep = _points_arg(points)
+    if dq != d or ldq != ld:
+        raise ValueError("queries and points need the same dimension and row stride")
+    o = _options(device=device, precision=precision, ld=ld if ld != d else 0, **kw)
+    out = np.zeros(nq, dtype=np.int32)
+    total = ctypes.c_uint64(0)
+    st = Stats()
+    _check(L.ejoin_join_counts(qptr, nq, ptr, n, d, float(eps), ctypes.byref(o), out.ctypes.data,
+                               ctypes.byref(total), ctypes.byref(st)))
+    del keep, keepq
+    return out, int(total.value), st.as_dict()
 
 
 def query_counts(points, eps: float, rows, device: int = 0):

@@ -374,6 +374,73 @@ static double screen_scale(Fmt f, double maxabs, uint32_t d) {
     return ldexp(1.0, e);
 }
 
+// Parameters of the 16-bit / FP8 screen for data with max |centred coord|
+// maxabs (see pack16_kernel / pack8_kernel for the bounds they feed).
+static ScreenParams screen_params(Fmt fmt, bool split, uint32_t d, double maxabs, double T,
+                                  double acc_bound_scale, double* kprod_out) {
+    ScreenParams P;
+    const bool fp8 = (fmt == Fmt::E4M3);
+    P.fmt = fmt;
+    P.split = split ? 1 : 0;
+    P.d = d;
+    P.dp = (uint32_t)round_up(d, fp8 ? 128 : 64);
+    P.width = P.dp * (split ? 2 : 1);
+    P.scale = screen_scale(fmt, maxabs, d);
+    double Tlo, Thi;
+    oracle_band(T, d, &Tlo, &Thi);
+    const double s2 = P.scale * P.scale;
+    // Every finite pair has s_q = |q_i - q_j|^2 <= 4 max|q|^2 (<= 2^14 for FP16
+    // by the choice of scale, <= 4d for BF16 / FP8): capping T far above that
+    // keeps both tests exact while bounding the margins in the operand range.
+    const double cap_t = (fmt == Fmt::FP16) ? 32768.0 : 1.152921504606846976e18;
+    P.Tlo = std::min(Tlo * s2, cap_t);
+    P.Thi = std::min(Thi * s2, cap_t);
+    P.sTlo = sqrt(P.Tlo) * (1 - 4 * kU);
+    P.sThi = sqrt(P.Thi) * (1 + 4 * kU);
+    const double kprod = (split ? 3.0 : 1.0) * P.dp + 16.0;  // + the aug K = 16 step
+    const double scale_opt = acc_bound_scale > 0 ? acc_bound_scale : 1.0;
+    P.cacc = scale_opt * (kprod + 16.0) * ldexp(1.0, -22);
+    P.absacc = (kprod + 16.0) * ldexp(1.0, -125);
+    P.clamp_lo = (fmt == Fmt::FP16) ? -16384.0 : -kTwo100;
+    *kprod_out = kprod;
+    return P;
+}
+
+// One packed operand side: operands, aug rows, margins, FP32 coordinates.
+struct PackedSide {
+    uint64_t n_pad = 0;
+    DBuf<uint16_t> Q, Aug;
+    DBuf<uint8_t> Q8;
+    DBuf<float> beta, tmax, Xf, rad, sig, tsig;
+    const void* operands(const ScreenParams& P) const {
+        return P.fmt == Fmt::E4M3 ? (const void*)Q8.p : (const void*)Q.p;
+    }
+};
+
+static int pack_side(const float* Y32, const float* Yerr, const uint8_t* bad, uint64_t n,
+                     uint64_t n_pad, const uint32_t* perm, const ScreenParams& P, PackedSide& S,
+                     cudaStream_t s) {
+    const bool fp8 = P.fmt == Fmt::E4M3;
+    S.n_pad = n_pad;
+    if (fp8) EJ_TRY(S.Q8.alloc(n_pad * P.width, s, "packed FP8 operands"));
+    else EJ_TRY(S.Q.alloc(n_pad * P.width, s, "packed operands"));
+    EJ_TRY(S.Aug.alloc(n_pad * 32, s, "aug operands"));
+    EJ_TRY(S.beta.alloc(n_pad, s, "out margins"));
+    EJ_TRY(S.tmax.alloc(n_pad / 128, s, "tile margins"));
+    EJ_TRY(S.Xf.alloc(n_pad * P.d, s, "FP32 coordinates"));
+    EJ_TRY(S.rad.alloc(n_pad, s, "FP32 radii"));
+    if (fp8) {
+        EJ_TRY(S.sig.alloc(n_pad, s, "row scales"));
+        EJ_TRY(S.tsig.alloc(n_pad / 128, s, "tile scales"));
+        EJ_TRY(launch_pack8(Y32, Yerr, n, n_pad, perm, bad, P, S.Q8.p, S.Aug.p, S.beta.p, S.sig.p,
+                            S.Xf.p, S.rad.p, S.tsig.p, s));
+    } else {
+        EJ_TRY(launch_pack16(Y32, Yerr, n, n_pad, perm, bad, P, S.Q.p, S.Aug.p, S.beta.p, S.Xf.p,
+                             S.rad.p, s));
+    }
+    return launch_tile_max(S.beta.p, nullptr, n_pad, S.tmax.p, s);
+}
+
 // L owns the permutation that J.perm points to; it must outlive the final
 // scatter of the counts, so the caller keeps it.
 static int run_screen16(Join& J, Fmt fmt, bool split, Learned& L) {
@@ -404,50 +471,11 @@ static int run_screen16(Join& J, Fmt fmt, bool split, Learned& L) {
     // a second pass of the same join (pair emission) reuses the ordering
     if (J.opt.proj_k && L.k == 0) EJ_TRY(prepare_learned(J, Y32.p, Yerr.p, bad.p, n_pad, L));
     tp.start(J.s);
-    ScreenParams P;
     const bool fp8 = (fmt == Fmt::E4M3);
-    P.fmt = fmt;
-    P.split = split ? 1 : 0;
-    P.d = J.d;
-    P.dp = (uint32_t)round_up(J.d, fp8 ? 128 : 64);
-    P.width = P.dp * (split ? 2 : 1);
-    P.scale = screen_scale(fmt, maxabs, J.d);
-    double Tlo, Thi;
-    oracle_band(J.T, J.d, &Tlo, &Thi);
-    const double s2 = P.scale * P.scale;
-    // Every finite pair has s_q = |q_i - q_j|^2 <= 4 max|q|^2 (<= 2^14 for FP16
-    // by the choice of scale, <= 4d for BF16 / FP8): capping T far above that
-    // keeps both tests exact while bounding the margins in the operand range.
-    const double cap_t = (fmt == Fmt::FP16) ? 32768.0 : 1.152921504606846976e18;
-    P.Tlo = std::min(Tlo * s2, cap_t);
-    P.Thi = std::min(Thi * s2, cap_t);
-    P.sTlo = sqrt(P.Tlo) * (1 - 4 * kU);
-    P.sThi = sqrt(P.Thi) * (1 + 4 * kU);
-    const double kprod = (split ? 3.0 : 1.0) * P.dp + 16.0;  // + the aug K = 16 step
-    const double scale_opt = J.opt.acc_bound_scale > 0 ? J.opt.acc_bound_scale : 1.0;
-    P.cacc = scale_opt * (kprod + 16.0) * ldexp(1.0, -22);
-    P.absacc = (kprod + 16.0) * ldexp(1.0, -125);
-    P.clamp_lo = (fmt == Fmt::FP16) ? -16384.0 : -kTwo100;
-    DBuf<uint16_t> Q, Aug;
-    DBuf<uint8_t> Q8;
-    DBuf<float> beta, tmax, Xf, rad, sig, tsig;
-    if (fp8) EJ_TRY(Q8.alloc(n_pad * P.width, J.s, "packed FP8 operands"));
-    else EJ_TRY(Q.alloc(n_pad * P.width, J.s, "packed operands"));
-    EJ_TRY(Aug.alloc(n_pad * 32, J.s, "aug operands"));
-    EJ_TRY(beta.alloc(n_pad, J.s, "out margins"));
-    EJ_TRY(tmax.alloc(n_pad / 128, J.s, "tile margins"));
-    EJ_TRY(Xf.alloc(n_pad * J.d, J.s, "FP32 coordinates"));
-    EJ_TRY(rad.alloc(n_pad, J.s, "FP32 radii"));
-    if (fp8) {
-        EJ_TRY(sig.alloc(n_pad, J.s, "row scales"));
-        EJ_TRY(tsig.alloc(n_pad / 128, J.s, "tile scales"));
-        EJ_TRY(launch_pack8(Y32.p, Yerr.p, J.n, n_pad, J.perm, bad.p, P, Q8.p, Aug.p, beta.p,
-                            sig.p, Xf.p, rad.p, tsig.p, J.s));
-    } else {
-        EJ_TRY(launch_pack16(Y32.p, Yerr.p, J.n, n_pad, J.perm, bad.p, P, Q.p, Aug.p, beta.p,
-                             Xf.p, rad.p, J.s));
-    }
-    EJ_TRY(launch_tile_max(beta.p, nullptr, n_pad, tmax.p, J.s));
+    double kprod = 0;
+    const ScreenParams P = screen_params(fmt, split, J.d, maxabs, J.T, J.opt.acc_bound_scale, &kprod);
+    PackedSide side;
+    EJ_TRY(pack_side(Y32.p, Yerr.p, bad.p, J.n, n_pad, J.perm, P, side, J.s));
     tp.stop(J.s);
     J.st->ms_prep = ms_center + tp.ms();
     const uint64_t nT = n_pad / 128;
@@ -466,15 +494,20 @@ static int run_screen16(Join& J, Fmt fmt, bool split, Learned& L) {
     J.st->gram_flops = 2.0 * kprod * 128.0 * 256.0 * (double)nwork;
     J.st->precision = fp8 ? EJOIN_FP8_E4M3
                           : (fmt == Fmt::FP16 ? EJOIN_FP16 : (split ? EJOIN_BF16_SPLIT : EJOIN_BF16));
-    const void* Qp = fp8 ? (const void*)Q8.p : (const void*)Q.p;
+    const void* Qp = side.operands(P);
     auto screen = [&](BandPair* band, uint64_t cap, DevStatus* st) {
-        return launch_gram16(Qp, Aug.p, n_pad, P, work.p, nwork, tmax.p, beta.p, tsig.p, sig.p,
+        const GramSide gs{Qp, side.Aug.p, n_pad};
+        return launch_gram16(gs, gs, P, work.p, nwork, side.tmax.p, side.beta.p, side.tsig.p,
+                             side.sig.p, false,
                              J.counts, reinterpret_cast<BandRec*>(band), cap, st, J.em, J.sms,
                              J.s);
     };
     Recheck32 R;
-    R.Xf = Xf.p;
-    R.rad = rad.p;
+    R.Xf = R.Xfb = side.Xf.p;
+    R.rad = R.radb = side.rad.p;
+    R.Xb = J.X;
+    R.nb = J.n;
+    R.permb = J.perm;
     R.sTlo = P.sTlo;
     R.sThi = P.sThi;
     R.c32 = (J.d + 8) * ldexp(1.0, -24) * 1.01;
@@ -751,6 +784,174 @@ int ejoin_query_counts(const double* points, uint64_t n, uint32_t d, double eps,
         EJ_CUDA(cudaMemcpyAsync(counts_out, cbuf.p, nq * sizeof(int32_t),
                                 out_dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s));
     EJ_CUDA(cudaStreamSynchronize(s));
+    return EJOIN_OK;
+}
+
+// Join of two point sets on the tensor-core screen: queries are the A side
+// (rows, counted), points the B side; both centred with the points' mean and
+// packed with one scale.  Data outside the FP32 path's range, FP64 modes and
+// eps = inf take the exact FP64 judge.
+static int cross_join(Join& J, const double* Xq, uint64_t nq, int prec, int32_t* qcounts) {
+    const bool fp64 = prec == EJOIN_FP64_DIRECT || prec == EJOIN_FP64_DMMA || isinf(J.T);
+    if (!fp64) {
+        const Fmt fmt = prec == EJOIN_FP16 ? Fmt::FP16 : (prec == EJOIN_FP8_E4M3 ? Fmt::E4M3 : Fmt::BF16);
+        const bool split = prec == EJOIN_BF16_SPLIT;
+        EventTimer tp, tg, tr;
+        tp.start(J.s);
+        DBuf<uint8_t> badx, badq;
+        DBuf<double> mu;
+        DBuf<float> Yx, Ex, Yq, Eq;
+        EJ_TRY(badx.alloc(J.n, J.s, "row flags"));
+        EJ_TRY(badq.alloc(nq, J.s, "query flags"));
+        EJ_TRY(mu.alloc(J.d, J.s, "mean"));
+        EJ_TRY(Yx.alloc(J.n * J.d, J.s, "FP32 centred points"));
+        EJ_TRY(Ex.alloc(J.n, J.s, "centring error bounds"));
+        EJ_TRY(Yq.alloc(nq * J.d, J.s, "FP32 centred queries"));
+        EJ_TRY(Eq.alloc(nq, J.s, "centring error bounds"));
+        CenterStats cx, cq;
+        EJ_TRY(launch_center_stats(J.X, J.n, J.d, badx.p, mu.p, Yx.p, Ex.p, &cx, J.s));
+        EJ_TRY(launch_center_stats(Xq, nq, J.d, badq.p, mu.p, Yq.p, Eq.p, &cq, J.s, true));
+        const double maxabs = std::max(cx.maxy, cq.maxy);
+        const bool flushed = cx.flushed || cq.flushed;
+        const bool fp32_ok = !cx.range && !cq.range &&
+                             (maxabs == 0.0 ? !flushed : (maxabs >= 0x1p-50 && maxabs <= 0x1p50));
+        if (fp32_ok) {
+            double kprod = 0;
+            const ScreenParams P =
+                screen_params(fmt, split, J.d, maxabs, J.T, J.opt.acc_bound_scale, &kprod);
+            PackedSide sx, sq;
+            const uint64_t npx = round_up(J.n, 256), npq = round_up(nq, 128);
+            EJ_TRY(pack_side(Yx.p, Ex.p, badx.p, J.n, npx, nullptr, P, sx, J.s));
+            EJ_TRY(pack_side(Yq.p, Eq.p, badq.p, nq, npq, nullptr, P, sq, J.s));
+            tp.stop(J.s);
+            J.st->ms_prep = tp.ms();
+            DBuf<uint2> work;
+            uint64_t nwork = 0, ntiles = 0;
+            const uint64_t nTq = (nq + 127) / 128, nTx = (J.n + 127) / 128;
+            EJ_TRY(build_worklist_cross(nTq, nTx, work, &nwork, &ntiles, J.s));
+            J.st->tile_pairs_total = nTq * nTx;
+            J.st->tile_pairs_run = ntiles;
+            J.st->reserved[1] = (double)nwork;
+            J.st->gram_flops = 2.0 * kprod * 128.0 * 256.0 * (double)nwork;
+            J.st->precision = prec;
+            Join Jq = J;  // counts of the screen: the queries (A side)
+            Jq.counts = qcounts;
+            const GramSide A{sq.operands(P), sq.Aug.p, npq}, B{sx.operands(P), sx.Aug.p, npx};
+            auto screen = [&](BandPair* band, uint64_t cap, DevStatus* st) {
+                return launch_gram16(A, B, P, work.p, nwork, sx.tmax.p, sq.beta.p, sx.tsig.p,
+                                     sq.sig.p, true, qcounts, reinterpret_cast<BandRec*>(band), cap,
+                                     st, nullptr, J.sms, J.s);
+            };
+            Recheck32 R;
+            R.Xf = sq.Xf.p;
+            R.rad = sq.rad.p;
+            R.Xfb = sx.Xf.p;
+            R.radb = sx.rad.p;
+            R.Xb = J.X;
+            R.nb = J.n;
+            R.permb = nullptr;
+            R.sTlo = P.sTlo;
+            R.sThi = P.sThi;
+            R.c32 = (J.d + 8) * ldexp(1.0, -24) * 1.01;
+            R.abs32 = (J.d + 8) * ldexp(1.0, -148);
+            auto recheck = [&](const BandPair* band, uint64_t nrec, uint64_t npairs, DevStatus* st) {
+                if (npairs == 0) return EJOIN_OK;
+                DBuf<BandPair> pairs;
+                EJ_TRY(pairs.alloc(npairs, J.s, "band pairs"));
+                EJ_TRY(launch_band_expand(reinterpret_cast<const BandRec*>(band), nrec, pairs.p,
+                                          npairs, J.s));
+                return launch_band_recheck2(Xq, nq, J.d, nullptr, J.T, R, pairs.p, npairs, qcounts,
+                                            st, nullptr, J.s);
+            };
+            const uint64_t cap0 = std::max<uint64_t>(1u << 22, 256 * (nq + J.n));
+            return screen_and_recheck(Jq, cap0, screen, recheck, npq, tg, tr, 2);
+        }
+    }
+    EventTimer tg;
+    tg.start(J.s);
+    EJ_CUDA(cudaMemsetAsync(qcounts, 0, nq * sizeof(int32_t), J.s));
+    EJ_TRY(launch_direct_query(J.X, J.n, J.d, J.T, nullptr, nq, qcounts, J.s, Xq));
+    tg.stop(J.s);
+    J.st->ms_gram = tg.ms();
+    J.st->precision = EJOIN_FP64_DIRECT;
+    J.st->gram_flops = 3.0 * J.d * (double)nq * (double)J.n;
+    return EJOIN_OK;
+}
+
+int ejoin_join_counts(const double* queries, uint64_t nq, const double* points, uint64_t n,
+                      uint32_t d, double eps, const ejoin_options* opt_in, int32_t* counts_out,
+                      uint64_t* total_out, ejoin_stats* stats_out) {
+    clear_error();
+    ejoin_options opt;
+    ejoin_default_options(&opt);
+    if (opt_in) {
+        if (opt_in->struct_size != sizeof(ejoin_options))
+            return set_error(EJOIN_EINVAL, "ejoin_options.struct_size mismatch");
+        opt = *opt_in;
+    }
+    if (d == 0 || (n && !points) || (nq && !queries)) return set_error(EJOIN_EINVAL, "bad arguments");
+    if (n > 0x7fffff00ull || nq > 0x7fffff00ull)
+        return set_error(EJOIN_EUNSUPPORTED, "point sets above 2^31 - 256 rows");
+    if (opt.proj_k) return set_error(EJOIN_EUNSUPPORTED, "learned pruning is for self joins (proj_k must be 0)");
+    if (opt.precision < EJOIN_FP64_DIRECT || opt.precision > EJOIN_AUTO)
+        return set_error(EJOIN_EINVAL, "unknown precision mode %d", opt.precision);
+    if (opt.acc_bound_scale < 1.0) return set_error(EJOIN_EINVAL, "acc_bound_scale must be >= 1");
+    const uint64_t ld = opt.ld ? opt.ld : d;
+    if (ld < d) return set_error(EJOIN_EINVAL, "row stride < d");
+    ejoin_stats stats;
+    memset(&stats, 0, sizeof stats);
+    stats.n = n;
+    stats.d = d;
+    DeviceScope ds;
+    int sms = 0;
+    EJ_TRY(check_device(opt.device, &sms));
+    EJ_TRY(ds.enter(opt.device));
+    cudaStream_t s = opt.stream ? (cudaStream_t)opt.stream : cudaStreamPerThread;
+    const double T = threshold(eps);
+    const uint64_t launches0 = launches_so_far();
+    EventTimer tt;
+    tt.start(s);
+    Join J;
+    J.s = s;
+    J.sms = sms;
+    J.n = n;
+    J.d = d;
+    J.eps = eps;
+    J.T = T;
+    J.opt = opt;
+    J.st = &stats;
+    J.perm = nullptr;
+    DBuf<double> xbuf, qbuf;
+    DBuf<int32_t> cbuf;
+    const uint64_t npq = round_up(std::max<uint64_t>(nq, 1), 128);
+    EJ_TRY(cbuf.alloc(npq, s, "query counts"));
+    EJ_TRY(cbuf.zero(s));
+    int prec = resolve_precision(opt.precision, d);
+    stats.precision = prec;
+    if (n > 0 && nq > 0 && !isnan(T) && T >= 0.0) {
+        const double* Xq = nullptr;
+        EJ_TRY(stage_points(points, n, d, ld, xbuf, &J.X, s));
+        EJ_TRY(stage_points(queries, nq, d, ld, qbuf, &Xq, s));
+        EJ_TRY(cross_join(J, Xq, nq, prec, cbuf.p));
+    }
+    DBuf<unsigned long long> tot;
+    EJ_TRY(tot.alloc(1, s, "total"));
+    EJ_TRY(tot.zero(s));
+    EJ_TRY(sum_counts(cbuf.p, nq, tot.p, s));
+    if (counts_out && nq)
+        EJ_CUDA(cudaMemcpyAsync(counts_out, cbuf.p, nq * sizeof(int32_t),
+                                is_device_ptr(counts_out) ? cudaMemcpyDeviceToDevice
+                                                          : cudaMemcpyDeviceToHost, s));
+    unsigned long long total = 0;
+    EJ_CUDA(cudaMemcpyAsync(&total, tot.p, sizeof total, cudaMemcpyDeviceToHost, s));
+    tt.stop(s);
+    EJ_CUDA(cudaStreamSynchronize(s));
+    stats.ms_total = tt.ms();
+    stats.kernel_launches = launches_so_far() - launches0;
+    const double computed = (double)n * (double)nq;
+    stats.band_fraction = computed > 0 ? (double)stats.band_pairs / computed : 0.0;
+    if (total_out) *total_out = total;
+    if (stats_out) *stats_out = stats;
     return EJOIN_OK;
 }
 

@@ -151,9 +151,16 @@ struct DevStatus {
 };
 
 // Constants of the FP32 band pre-check (scaled space of the 16-bit screen).
+// Pairs (i, j) take row i from side A and row j from side B; for a self join
+// the two sides are the same arrays.
 struct Recheck32 {
-    const float* Xf;   // [n_pad][d] FP32 coordinates, packed order
-    const float* rad;  // per-row radius (|zf - s (x - mu)| bound; inf = undecidable row)
+    const float* Xf;   // A: [n_pad][d] FP32 coordinates, packed order
+    const float* rad;  // A: per-row radius (|zf - s (x - mu)| bound; inf = undecidable row)
+    const float* Xfb;  // B: the same for the second point set
+    const float* radb;
+    const double* Xb;  // B: original FP64 rows (the exact chain)
+    uint64_t nb;       // B: rows
+    const uint32_t* permb;  // B: packed -> original row (null = identity)
     double sTlo, sThi; // sqrt of the scaled oracle thresholds (down / up)
     double c32;        // relative bound of the FP32 squared-difference sum
     double abs32;      // absolute bound (FP32 underflow)
@@ -250,8 +257,10 @@ struct JoinCtx;  // api.cu
 int launch_direct_selfjoin(const double* X, uint64_t n, uint32_t d, double T, int32_t* counts,
                            const Emit* em,
                            cudaStream_t s);
+// Query counts against all n rows of X: query rows rows[q] of X, or (Xq
+// non-null) the rows of a separate nq x d array Xq.
 int launch_direct_query(const double* X, uint64_t n, uint32_t d, double T, const uint64_t* rows,
-                        uint64_t nq, int32_t* counts, cudaStream_t s);
+                        uint64_t nq, int32_t* counts, cudaStream_t s, const double* Xq = nullptr);
 int launch_band_recheck(const double* X, uint64_t n, uint32_t d, const uint32_t* perm, double T,
                         const BandPair* band, uint64_t nband, int32_t* counts, DevStatus* st,
                         cudaStream_t s);
@@ -263,14 +272,22 @@ int launch_dmma_join(const double* Y, uint64_t n_pad, uint32_t dp, const double*
 
 // k_umma.cu: tcgen05 Gram screen over a tile-pair work list (16-bit operands).
 // (FP8 operands: also the per-tile minimum row scale tsig.)
-// tmax / beta: per-tile / per-row out margins; FP8: tsig / sig per-tile
-// minimum / per-row scales.
-int launch_gram16(const void* Q, const void* aug, uint64_t n_pad, const ScreenParams& P,
-                  const uint2* work, uint64_t nwork, const float* tmax, const float* beta,
-                  const float* tsig, const float* sig,
-                  int32_t* counts, BandRec* band, uint64_t band_cap, DevStatus* st, const Emit* em,
-                  int num_sms,
-                  cudaStream_t s);
+// One operand side of the tensor-core Gram screen: packed rows [n_pad][W]
+// and aug rows [n_pad][32].
+struct GramSide {
+    const void* Q;
+    const void* aug;
+    uint64_t n_pad;
+};
+// Rows of A against columns of B over the blocks of the work list.  tmax_b:
+// per 128-row tile of B, max beta; beta_a: per row of A; FP8: tsig_b / sig_a
+// per-tile minimum / per-row scales.  cross: A and B are different point
+// sets (only A's rows are counted, every block as a diagonal one); else A is
+// B and the upper-triangle blocks credit both sides.
+int launch_gram16(const GramSide& A, const GramSide& B, const ScreenParams& P, const uint2* work,
+                  uint64_t nwork, const float* tmax_b, const float* beta_a, const float* tsig_b,
+                  const float* sig_a, bool cross, int32_t* counts, BandRec* band, uint64_t band_cap,
+                  DevStatus* st, const Emit* em, int num_sms, cudaStream_t s);
 
 // k_misc.cu
 // Ordered list of 128 x 256 blocks (row tile I, column tiles 2p, 2p+1)
@@ -280,6 +297,10 @@ int launch_gram16(const void* Q, const void* aug, uint64_t n_pad, const ScreenPa
 // pairs are dropped first).  ntiles_out: active 128 x 128 tile pairs.
 int build_worklist(uint64_t nT, uint64_t nTa, const LearnedBoxes* boxes, float thr,
                    DBuf<uint2>& work, uint64_t* nwork_out, uint64_t* ntiles_out, cudaStream_t s);
+// All blocks of a join of two point sets: nTa row tiles (with data) against
+// nTb column tiles (with data; B padded to whole 256-row pairs).
+int build_worklist_cross(uint64_t nTa, uint64_t nTb, DBuf<uint2>& work, uint64_t* nwork_out,
+                         uint64_t* ntiles_out, cudaStream_t s);
 int sum_counts(const int32_t* counts, uint64_t n, unsigned long long* dev_total, cudaStream_t s);
 int scatter_counts(const int32_t* src, const uint32_t* perm, uint64_t n, int32_t* dst,
                    cudaStream_t s);
@@ -328,8 +349,10 @@ struct CenterStats {
     bool range = false;    // a coordinate beyond 2^120: the FP32 copy is unusable
     bool flushed = false;  // a nonzero coordinate below 2^-126 was replaced by 0
 };
+// mu_given: mu holds the mean to use (another point set's, FP32-representable).
 int launch_center_stats(const double* X, uint64_t n, uint32_t d, uint8_t* bad, double* mu,
-                        float* Y32, float* Yerr, CenterStats* out, cudaStream_t s);
+                        float* Y32, float* Yerr, CenterStats* out, cudaStream_t s,
+                        bool mu_given = false);
 // FP64 centred copy Y[n_pad][dp] and per-row thresholds h, g for the DMMA screen.
 int launch_pack_dmma(const double* X, uint64_t n, uint64_t n_pad, const uint32_t* perm,
                      const uint8_t* bad, const double* mu, const DmmaParams& P, double* Y,

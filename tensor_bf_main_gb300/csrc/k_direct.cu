@@ -114,9 +114,11 @@ __global__ void __launch_bounds__(256) direct_selfjoin_kernel(const double* __re
     }
 }
 
+// Query rows: rows[q] of X, or (Xq non-null) row q of a separate array Xq.
 __global__ void __launch_bounds__(256) direct_query_kernel(const double* __restrict__ X, uint64_t n,
                                                            uint32_t d, double T,
                                                            const uint64_t* __restrict__ rows,
+                                                           const double* __restrict__ Xq,
                                                            uint64_t nq, int32_t* counts) {
     __shared__ double SA[KC][PADK];
     __shared__ double SB[KC][PADK];
@@ -131,7 +133,8 @@ __global__ void __launch_bounds__(256) direct_query_kernel(const double* __restr
         for (int cc = 0; cc < 4; ++cc) acc[rr][cc] = 0.0;
     for (uint32_t k0 = 0; k0 < d; k0 += KC) {
         __syncthreads();
-        stage_tile(SA, X, n, d, Q * TB, k0, rows, nq);
+        if (Xq) stage_tile(SA, Xq, nq, d, Q * TB, k0, nullptr, 0);
+        else stage_tile(SA, X, n, d, Q * TB, k0, rows, nq);
         stage_tile(SB, X, n, d, J * TB, k0, nullptr, 0);
         __syncthreads();
         tile_chains(acc, SA, SB, ty, tx);
@@ -193,14 +196,14 @@ __device__ __forceinline__ bool recheck_decide(const double* __restrict__ X, uin
                                                const Recheck32& R, uint32_t i, uint32_t j,
                                                float S, unsigned& exact_runs) {
     const double Sd = (double)S;
-    const double rr = (double)R.rad[i] + (double)R.rad[j];
+    const double rr = (double)R.rad[i] + (double)R.radb[j];
     const double lo = R.sTlo - rr;
     if (lo >= 0.0 && (Sd + R.abs32) / (1.0 - R.c32) <= lo * lo * (1.0 - 8 * kU)) return true;
     const double hi = R.sThi + rr;
     if ((Sd - R.abs32) / (1.0 + R.c32) > hi * hi * (1.0 + 8 * kU)) return false;
     ++exact_runs;
-    const uint64_t oi = perm ? perm[i] : i, oj = perm ? perm[j] : j;
-    return exact_d2(X + oi * (uint64_t)d, X + oj * (uint64_t)d, d) <= T;
+    const uint64_t oi = perm ? perm[i] : i, oj = R.permb ? R.permb[j] : j;
+    return exact_d2(X + oi * (uint64_t)d, R.Xb + oj * (uint64_t)d, d) <= T;
 }
 
 __device__ __forceinline__ void recheck_totals(DevStatus* st, unsigned hits, unsigned exact_runs) {
@@ -227,9 +230,9 @@ __global__ void __launch_bounds__(256) band_recheck_thread_kernel(const double* 
          e += (uint64_t)gridDim.x * blockDim.x) {
         const BandPair bp = band[e];
         const uint32_t i = bp.i, j = bp.j & ~kBandBoth;
-        if (i >= n || j >= n) continue;
+        if (i >= n || j >= R.nb) continue;
         const float4* a = reinterpret_cast<const float4*>(R.Xf + (uint64_t)i * d);
-        const float4* b = reinterpret_cast<const float4*>(R.Xf + (uint64_t)j * d);
+        const float4* b = reinterpret_cast<const float4*>(R.Xfb + (uint64_t)j * d);
         float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f, s3 = 0.0f;
 #pragma unroll 4
         for (uint32_t c = 0; c < d / 4; ++c) {
@@ -270,7 +273,7 @@ __global__ void __launch_bounds__(256) band_recheck_warp_kernel(const double* __
         BandPair bp = {0xffffffffu, 0xffffffffu};
         if (e < nband) bp = band[e];
         const uint32_t mi = bp.i, mj = bp.j & ~kBandBoth;
-        const bool valid = e < nband && mi < n && mj < n;
+        const bool valid = e < nband && mi < n && mj < R.nb;
         float mine = 0.0f;
         for (uint32_t q = 0; q < 32; ++q) {
             const uint32_t i = __shfl_sync(0xffffffffu, mi, q);
@@ -278,7 +281,7 @@ __global__ void __launch_bounds__(256) band_recheck_warp_kernel(const double* __
             const bool v = __shfl_sync(0xffffffffu, valid, q);
             if (!v) continue;  // warp-uniform
             const float* a = R.Xf + (uint64_t)i * d;
-            const float* b = R.Xf + (uint64_t)j * d;
+            const float* b = R.Xfb + (uint64_t)j * d;
             float S = 0.0f;
             for (uint32_t c = lane; c < d; c += 32) {
                 const float t = a[c] - b[c];
@@ -306,7 +309,7 @@ int launch_band_recheck2(const double* X, uint64_t n, uint32_t d, const uint32_t
     const Emit e = em ? *em : Emit{nullptr, 0, nullptr, 0, nullptr};
     // measured on GB300: a thread per pair wins for rows of <= 256 bytes, a
     // warp per pair (more pairs in flight per load) for longer rows
-    const bool thread = d <= 64 && d % 4 == 0 && ((uintptr_t)R.Xf & 15) == 0;
+    const bool thread = d <= 64 && d % 4 == 0 && (((uintptr_t)R.Xf | (uintptr_t)R.Xfb) & 15) == 0;
     if (thread) {
         const unsigned blocks = (unsigned)std::min<uint64_t>((nband + 255) / 256, 152ull * 32);
         band_recheck_thread_kernel<<<blocks, 256, 0, s>>>(X, d, perm, T, R, band, nband, n, counts, st, e);
@@ -339,13 +342,20 @@ int launch_direct_selfjoin(const double* X, uint64_t n, uint32_t d, double T, in
 }
 
 int launch_direct_query(const double* X, uint64_t n, uint32_t d, double T, const uint64_t* rows,
-                        uint64_t nq, int32_t* counts, cudaStream_t s) {
+                        uint64_t nq, int32_t* counts, cudaStream_t s, const double* Xq) {
     if (n == 0 || nq == 0) return EJOIN_OK;
-    uint64_t gx = (n + TB - 1) / TB, gy = (nq + TB - 1) / TB;
-    if (gx > 0x7fffffffull || gy > 65535) return set_error(EJOIN_EUNSUPPORTED, "query grid too large");
-    direct_query_kernel<<<dim3((unsigned)gx, (unsigned)gy), 256, 0, s>>>(X, n, d, T, rows, nq, counts);
-    EJ_CUDA(cudaGetLastError());
-    note_launch();
+    const uint64_t gx = (n + TB - 1) / TB;
+    if (gx > 0x7fffffffull) return set_error(EJOIN_EUNSUPPORTED, "query grid too large");
+    // the grid's y extent is limited: queries in chunks of 65535 tiles
+    const uint64_t chunk = 65535ull * TB;
+    for (uint64_t q0 = 0; q0 < nq; q0 += chunk) {
+        const uint64_t m = std::min<uint64_t>(chunk, nq - q0);
+        direct_query_kernel<<<dim3((unsigned)gx, (unsigned)((m + TB - 1) / TB)), 256, 0, s>>>(
+            X, n, d, T, rows ? rows + q0 : nullptr, Xq ? Xq + q0 * (uint64_t)d : nullptr, m,
+            counts + q0);
+        EJ_CUDA(cudaGetLastError());
+        note_launch();
+    }
     return EJOIN_OK;
 }
 

@@ -112,6 +112,25 @@ __global__ void __launch_bounds__(EXPAND_THREADS) expand_kernel(const uint32_t* 
             make_uint2((uint32_t)I, (uint32_t)p | (mask << 30));
 }
 
+// Work list of a join of two point sets (rows: nTa tiles of A, columns: the
+// pairs of B's nTb tiles), all blocks, in super-blocks of 16 row tiles x 8
+// column pairs (row-major inside, super-blocks row-major) so that concurrent
+// CTAs share operand rows in L2.  Closed form: every super-row but the last
+// holds 16 npb entries, every super-block but the last of its super-row
+// 8 qh entries (qh row tiles in the super-row).  Mask bit h: tile 2p + h < nTb.
+__global__ void cross_work_kernel(uint64_t nTa, uint64_t nTb, uint64_t total, uint2* out) {
+    const uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (e >= total) return;
+    const uint64_t npb = (nTb + 1) / 2;
+    const uint64_t SI = e / (16 * npb), rem = e - SI * 16 * npb;
+    const uint64_t qh = min((uint64_t)16, nTa - SI * 16);
+    const uint64_t SP = rem / (qh * 8), rem2 = rem - SP * qh * 8;
+    const uint64_t pw = min((uint64_t)8, npb - SP * 8);
+    const uint64_t I = SI * 16 + rem2 / pw, p = SP * 8 + rem2 % pw;
+    const uint32_t mask = 1u | (2 * p + 1 < nTb ? 2u : 0u);
+    out[e] = make_uint2((uint32_t)I, (uint32_t)p | (mask << 30));
+}
+
 // Band records -> pairs: a thread per record; block-level exclusive scan of
 // the popcounts, one global reservation per block.
 constexpr uint32_t EXPAND_BAND_THREADS = 256;
@@ -215,6 +234,19 @@ int launch_band_expand(const BandRec* rec, uint64_t nrec, BandPair* out, uint64_
     EJ_TRY(cur.zero(s));
     band_expand_kernel<<<(unsigned)((nrec + EXPAND_BAND_THREADS - 1) / EXPAND_BAND_THREADS),
                          EXPAND_BAND_THREADS, 0, s>>>(rec, nrec, out, cap, cur.p);
+    EJ_CUDA(cudaGetLastError());
+    note_launch();
+    return EJOIN_OK;
+}
+
+int build_worklist_cross(uint64_t nTa, uint64_t nTb, DBuf<uint2>& work, uint64_t* nwork_out,
+                         uint64_t* ntiles_out, cudaStream_t s) {
+    const uint64_t total = nTa * ((nTb + 1) / 2);
+    *nwork_out = total;
+    *ntiles_out = nTa * nTb;
+    if (total == 0) return EJOIN_OK;
+    EJ_TRY(work.alloc(total, s, "work list"));
+    cross_work_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(nTa, nTb, total, work.p);
     EJ_CUDA(cudaGetLastError());
     note_launch();
     return EJOIN_OK;

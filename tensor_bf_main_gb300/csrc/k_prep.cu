@@ -73,6 +73,12 @@ __global__ void sample_mean_kernel(const double* __restrict__ psum, const uint32
     mu[k] = (double)f;
 }
 
+// a given FP32-representable mean (stored as double) as FP32
+__global__ void mu_float_kernel(const double* __restrict__ mu, uint32_t d, float* muf) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < d) muf[k] = (float)mu[k];
+}
+
 constexpr uint32_t kCenterRange = 1u;  // a finite |x| >= 2^120: FP32 path unusable
 constexpr uint32_t kCenterFlush = 2u;  // a nonzero |x| < 2^-126 was replaced by 0
 
@@ -720,13 +726,17 @@ __global__ void tile_max_kernel(const float* __restrict__ beta, const float4* __
 }  // namespace
 
 int launch_center_stats(const double* X, uint64_t n, uint32_t d, uint8_t* bad, double* mu,
-                        float* Y32, float* Yerr, CenterStats* out, cudaStream_t s) {
+                        float* Y32, float* Yerr, CenterStats* out, cudaStream_t s, bool mu_given) {
     *out = CenterStats{};
     DBuf<float> muf;
     EJ_TRY(muf.alloc(d, s, "FP32 mean"));
     const uint64_t S = std::min<uint64_t>(n, kMeanSample);
     const uint32_t nb = (uint32_t)((S + kMeanRowsPerBlock - 1) / kMeanRowsPerBlock);
-    if (nb) {
+    if (mu_given) {
+        mu_float_kernel<<<(d + 127) / 128, 128, 0, s>>>(mu, d, muf.p);
+        EJ_CUDA(cudaGetLastError());
+        note_launch();
+    } else if (nb) {
         DBuf<double> psum;
         DBuf<uint32_t> pcnt;
         EJ_TRY(psum.alloc((size_t)nb * d, s, "sample column sums"));

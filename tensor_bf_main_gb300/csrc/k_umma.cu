@@ -83,6 +83,7 @@ struct GramArgs {
     uint32_t split;  // hi + lo
     uint32_t fmt;    // 16-bit operands: 0 = FP16, 1 = BF16 (instruction-descriptor format)
     uint32_t lrun;   // log2 of the run length: entries a CTA takes consecutively
+    uint32_t cross;  // rows of A against a different set B: count rows only
     Emit em;         // neighbour-list emission (em.cnt null: counts only)
 };
 
@@ -457,7 +458,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             const uint2 wn = entry_or_end(a, item_at(idx + 1, a.lrun));
             const uint32_t I = w.x, p = w.y & kPairMask, J = 2u * p + h;
             const bool active = (w.y >> (30 + h)) & 1u;
-            const bool diag = (I == J);
+            const bool diag = a.cross || (I == J);  // credit rows only
             if (!ptx::mbar_wait(&S.tfull[b], use & 1u, a.st, 30)) break;
             ptx::tc_fence_after();
             uint32_t v0[32], v1[32];
@@ -561,28 +562,28 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 
 }  // namespace
 
-int launch_gram16(const void* Q, const void* aug, uint64_t n_pad, const ScreenParams& P,
-                  const uint2* work, uint64_t nwork, const float* tmax, const float* beta,
-                  const float* tsig, const float* sig,
-                  int32_t* counts, BandRec* band, uint64_t band_cap, DevStatus* st, const Emit* em,
-                  int num_sms,
-                  cudaStream_t s) {
+int launch_gram16(const GramSide& A, const GramSide& B, const ScreenParams& P, const uint2* work,
+                  uint64_t nwork, const float* tmax, const float* beta, const float* tsig,
+                  const float* sig, bool cross, int32_t* counts, BandRec* band, uint64_t band_cap,
+                  DevStatus* st, const Emit* em, int num_sms, cudaStream_t s) {
     if (nwork == 0) return EJOIN_OK;
     const bool fp8 = P.fmt == Fmt::E4M3;
-    if (n_pad % 256 || P.dp % (fp8 ? 128 : 64)) return set_error(EJOIN_EINTERNAL, "gram: bad padding");
-    if (n_pad > 0x7fffff00ull) return set_error(EJOIN_EUNSUPPORTED, "gram16: too many rows");
+    if (A.n_pad % 128 || B.n_pad % 256 || P.dp % (fp8 ? 128 : 64))
+        return set_error(EJOIN_EINTERNAL, "gram: bad padding");
+    if (A.n_pad > 0x7fffff00ull || B.n_pad > 0x7fffff00ull)
+        return set_error(EJOIN_EUNSUPPORTED, "gram16: too many rows");
     CUtensorMap ma, mb, maa, mab;
     const CUtensorMapDataType adt =
         P.fmt == Fmt::FP16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
     if (fp8) {
-        EJ_TRY(make_tmap_2d(&ma, Q, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, P.width, n_pad, 128, 128));
-        EJ_TRY(make_tmap_2d(&mb, Q, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, P.width, n_pad, 128, 256));
+        EJ_TRY(make_tmap_2d(&ma, A.Q, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, P.width, A.n_pad, 128, 128));
+        EJ_TRY(make_tmap_2d(&mb, B.Q, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, P.width, B.n_pad, 128, 256));
     } else {
-        EJ_TRY(make_tmap_2d(&ma, Q, adt, 2, P.width, n_pad, 64, 128));
-        EJ_TRY(make_tmap_2d(&mb, Q, adt, 2, P.width, n_pad, 64, 256));
+        EJ_TRY(make_tmap_2d(&ma, A.Q, adt, 2, P.width, A.n_pad, 64, 128));
+        EJ_TRY(make_tmap_2d(&mb, B.Q, adt, 2, P.width, B.n_pad, 64, 256));
     }
-    EJ_TRY(make_tmap_2d(&maa, aug, adt, 2, 32, n_pad, 16, 128));
-    EJ_TRY(make_tmap_2d(&mab, aug, adt, 2, 32, n_pad, 16, 256));
+    EJ_TRY(make_tmap_2d(&maa, A.aug, adt, 2, 32, A.n_pad, 16, 128));
+    EJ_TRY(make_tmap_2d(&mab, B.aug, adt, 2, 32, B.n_pad, 16, 256));
     GramArgs a;
     a.work = work;
     a.nwork = nwork;
@@ -591,6 +592,7 @@ int launch_gram16(const void* Q, const void* aug, uint64_t n_pad, const ScreenPa
     a.tsig = fp8 ? tsig : nullptr;
     a.sig = fp8 ? sig : nullptr;
     a.em = em ? *em : Emit{nullptr, 0, nullptr, 0, nullptr};
+    a.cross = cross ? 1u : 0u;
     if (!tmax || !beta || (fp8 && (!tsig || !sig))) return set_error(EJOIN_EINTERNAL, "gram: margins missing");
     a.counts = counts;
     a.band = band;
