@@ -712,14 +712,18 @@ int learned_order(const float* Y32, const float* Yerr, const uint8_t* bad, uint6
                                                            rng.p + k, keys.p, idx.p);
     EJ_CUDA(cudaGetLastError());
     note_launch();
+    // Lead-coordinate keys live in bits 0..31.  Morton keys use all 64 bits for
+    // the pruning order; the training rounds (no boxes) only need locality for
+    // pair sampling and sort on the coarse top 32 bits (half the passes).
+    const int b0 = lead_only ? 0 : (boxes ? 0 : 32), b1 = lead_only ? 32 : 64;
     size_t tmp_bytes = 0;
     EJ_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, keys.p, keys2.p, idx.p, perm.p,
-                                            (int)n, 0, 64, s));
+                                            (int)n, b0, b1, s));
     DBuf<uint8_t> tmp;
     EJ_TRY(tmp.alloc(tmp_bytes, s, "sort scratch"));
     EJ_CUDA(cub::DeviceRadixSort::SortPairs(tmp.p, tmp_bytes, keys.p, keys2.p, idx.p, perm.p,
-                                            (int)n, 0, 64, s));
-    note_launch(11);  // histogram, scan and one-sweep passes of the library sort
+                                            (int)n, b0, b1, s));
+    note_launch(b1 - b0 == 64 ? 11 : 7);  // histogram, scan and one-sweep passes of the library sort
     if (boxes) {
         const uint64_t nt = n_pad / 128;
         const uint64_t ns = (nt + kSuperTiles - 1) / kSuperTiles;

@@ -440,22 +440,43 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         // accumulator's unit for pair (i, j) being 1 / (sigma_i sigma_j)); the
         // sum is rounded up by the 2^-20 relative margin, division by the
         // power-of-two scales is exact.  0 for an inactive half.
-        auto row_width = [&](uint2 e) -> float {
-            if (e.x == 0xffffffffu || !((e.y >> (30 + h)) & 1u)) return 0.0f;
-            const uint32_t Je = 2u * (e.y & kPairMask) + h;
-            const uint32_t r = e.x * 128u + q * 32u + lane;
-            const float sm = __ldg(&a.beta[r]) + __ldg(&a.tmax[Je]);
+        // Latency: entries are read two blocks ahead and the raw margins one
+        // block ahead, both consumed a block later, so no global-load latency
+        // lands on a block's own path.
+        struct Margins {
+            float b, t, sr, st;
+            bool on;
+        };
+        auto load_margins = [&](uint2 e) -> Margins {
+            Margins m{0.0f, 0.0f, 1.0f, 1.0f, false};
+            if (e.x != 0xffffffffu && ((e.y >> (30 + h)) & 1u)) {
+                const uint32_t Je = 2u * (e.y & kPairMask) + h;
+                const uint32_t r = e.x * 128u + q * 32u + lane;
+                m.b = __ldg(&a.beta[r]);
+                m.t = __ldg(&a.tmax[Je]);
+                if (OPK) {
+                    m.sr = __ldg(&a.sig[r]);
+                    m.st = __ldg(&a.tsig[Je]);
+                }
+                m.on = true;
+            }
+            return m;
+        };
+        auto width = [&](const Margins& m) -> float {
+            if (!m.on) return 0.0f;
+            const float sm = m.b + m.t;
             float Wv = fmaf(fabsf(sm), 9.5367431640625e-07f, sm);
-            if (a.tsig) Wv = Wv / (__ldg(&a.sig[r]) * __ldg(&a.tsig[Je]));
+            if (OPK) Wv = Wv / (m.sr * m.st);
             return Wv;
         };
-        // the next block's entry and band widths are loaded one block ahead
         uint2 w = entry_or_end(a, item_at(0, a.lrun));
-        float W = row_width(w);
+        uint2 wn = entry_or_end(a, item_at(1, a.lrun));
+        float W = width(load_margins(w));
         for (uint64_t idx = 0;; ++idx, ++it) {
             if (item_at(idx, a.lrun) >= a.nwork) break;
             const uint32_t b = it & 1u, use = it >> 1;
-            const uint2 wn = entry_or_end(a, item_at(idx + 1, a.lrun));
+            const uint2 wnn = entry_or_end(a, item_at(idx + 2, a.lrun));
+            const Margins mn = load_margins(wn);
             const uint32_t I = w.x, p = w.y & kPairMask, J = 2u * p + h;
             const bool active = (w.y >> (30 + h)) & 1u;
             const bool diag = a.cross || (I == J);  // credit rows only
@@ -467,7 +488,6 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 ptx::tmem_ld_32x32b_x32(taddr, v0);
                 ptx::tmem_ld_32x32b_x32(taddr + 32u, v1);
             }
-            const float Wn = row_width(wn);
             if (active) ptx::tmem_ld_wait();
             ptx::tc_fence_before();
             __syncwarp();
@@ -497,8 +517,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             }
             __syncwarp();
             if (lane == 0) ptx::mbar_arrive(&S.ebar[b]);
-            W = Wn;
+            W = width(mn);
             w = wn;
+            wn = wnn;
         }
     } else {
         // ------------------------------------------------ count flusher
