@@ -291,6 +291,7 @@ def run_ours(args):
         "band_fraction": stats[-1]["band_fraction"], "band_pairs": stats[-1]["band_pairs"],
         "tile_pairs_run": stats[-1]["tile_pairs_run"],
         "gram_blocks": stats[-1].get("gram_blocks", 0),
+        "exact_rechecks": stats[-1].get("exact_rechecks", 0),
         "tile_pairs_total": stats[-1]["tile_pairs_total"],
         "phase_ms": {k: stats[-1][k] for k in ("ms_prep", "ms_train", "ms_order", "ms_gram",
                                                 "ms_recheck", "ms_total")},

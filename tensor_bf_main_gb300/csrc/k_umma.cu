@@ -162,19 +162,26 @@ __device__ __forceinline__ void col_counts(uint32_t inm, int* cacc, uint32_t lan
     }
 }
 
+__device__ __forceinline__ float max3f(float x, float y, float z) {
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(x), "f"(y), "f"(z));
+    return r;
+}
+
 // In / band bit masks of one 32 x 32 chunk (lane = row, v[c] = column c).
 // Fast path: if max + W < 0 over the chunk, every pair in it is certainly out
 // (rounding of the FP32 add is monotone, so max + W >= 0 whenever any
 // element is >= -W).
 __device__ __forceinline__ bool classify(const uint32_t (&v)[32], float W, uint32_t& inm,
                                          uint32_t& bandm) {
-    float m8[8];
+    float m10[11];
 #pragma unroll
-    for (int j = 0; j < 8; ++j)
-        m8[j] = fmaxf(fmaxf(__uint_as_float(v[j]), __uint_as_float(v[j + 8])),
-                      fmaxf(__uint_as_float(v[j + 16]), __uint_as_float(v[j + 24])));
-    const float mx = fmaxf(fmaxf(fmaxf(m8[0], m8[1]), fmaxf(m8[2], m8[3])),
-                           fmaxf(fmaxf(m8[4], m8[5]), fmaxf(m8[6], m8[7])));
+    for (int j = 0; j < 10; ++j)
+        m10[j] = max3f(__uint_as_float(v[j]), __uint_as_float(v[j + 10]), __uint_as_float(v[j + 20]));
+    m10[10] = fmaxf(__uint_as_float(v[30]), __uint_as_float(v[31]));
+    const float mx = fmaxf(max3f(max3f(m10[0], m10[1], m10[2]), max3f(m10[3], m10[4], m10[5]),
+                                 max3f(m10[6], m10[7], m10[8])),
+                           fmaxf(m10[9], m10[10]));
     inm = bandm = 0;
     if (!__any_sync(FULL, mx + W >= 0.0f)) return false;
     // sign bits, four independent 8-column chains
@@ -482,23 +489,24 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             const bool diag = a.cross || (I == J);  // credit rows only
             if (!ptx::mbar_wait(&S.tfull[b], use & 1u, a.st, 30)) break;
             ptx::tc_fence_after();
-            uint32_t v0[32], v1[32];
+            // the two 32-column chunks one after the other: 32 live values
+            // instead of 64 (measured on c4: 8% faster than loading both at
+            // once); the accumulator is released after the second load
+            uint32_t v[32];
             const uint32_t taddr = tmem + ((q * 32u) << 16) + b * ACC_COLS + cg * 64u;
-            if (active) {
-                ptx::tmem_ld_32x32b_x32(taddr, v0);
-                ptx::tmem_ld_32x32b_x32(taddr + 32u, v1);
-            }
-            if (active) ptx::tmem_ld_wait();
-            ptx::tc_fence_before();
-            __syncwarp();
-            if (lane == 0) ptx::mbar_arrive(&S.tempty[b]);
-
             uint32_t in0 = 0, bd0 = 0, in1 = 0, bd1 = 0;
             bool busy0 = false, busy1 = false;
             if (active) {
-                busy0 = classify(v0, W, in0, bd0);
-                busy1 = classify(v1, W, in1, bd1);
+                ptx::tmem_ld_32x32b_x32(taddr, v);
+                ptx::tmem_ld_wait();
+                busy0 = classify(v, W, in0, bd0);
+                ptx::tmem_ld_32x32b_x32(taddr + 32u, v);
+                ptx::tmem_ld_wait();
             }
+            ptx::tc_fence_before();
+            __syncwarp();
+            if (lane == 0) ptx::mbar_arrive(&S.tempty[b]);
+            if (active) busy1 = classify(v, W, in1, bd1);
             // the counts of buffer b were flushed and cleared for block it - 2
             if (!ptx::mbar_wait(&S.fdone[b], (use & 1u) ^ 1u, a.st, 32)) break;
             if (busy0 || busy1) {
