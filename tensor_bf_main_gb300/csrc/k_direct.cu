@@ -215,8 +215,19 @@ __device__ __forceinline__ void recheck_totals(DevStatus* st, unsigned hits, uns
     }
 }
 
+// 32-byte read-only load (eight floats; p 32-byte aligned).
+__device__ __forceinline__ void ldg8(const float* p, float (&r)[8]) {
+    asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=f"(r[0]), "=f"(r[1]), "=f"(r[2]), "=f"(r[3]), "=f"(r[4]), "=f"(r[5]), "=f"(r[6]),
+          "=f"(r[7])
+        : "l"(p));
+}
+
 // Short rows (d <= 64, 16-byte aligned): a thread per pair streams both rows
-// with 16-byte loads (four partial sums): 32 pairs in flight per warp.
+// with 16-byte loads, or 32-byte loads when V8 (four partial sums): 32 pairs
+// in flight per warp.  The kernel is bound by L1 wavefronts (each lane reads
+// its own row), so wider loads move more bytes per wavefront.
+template <bool V8>
 __global__ void __launch_bounds__(256) band_recheck_thread_kernel(const double* __restrict__ X,
                                                                   uint32_t d,
                                                                   const uint32_t* __restrict__ perm,
@@ -231,17 +242,37 @@ __global__ void __launch_bounds__(256) band_recheck_thread_kernel(const double* 
         const BandPair bp = band[e];
         const uint32_t i = bp.i, j = bp.j & ~kBandBoth;
         if (i >= n || j >= R.nb) continue;
-        const float4* a = reinterpret_cast<const float4*>(R.Xf + (uint64_t)i * d);
-        const float4* b = reinterpret_cast<const float4*>(R.Xfb + (uint64_t)j * d);
         float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f, s3 = 0.0f;
+        if (V8) {
+            const float* a = R.Xf + (uint64_t)i * d;
+            const float* b = R.Xfb + (uint64_t)j * d;
+#pragma unroll 2
+            for (uint32_t c = 0; c < d; c += 8) {
+                float u[8], v[8];
+                ldg8(a + c, u);
+                ldg8(b + c, v);
+#pragma unroll
+                for (int k = 0; k < 8; k += 4) {
+                    const float t0 = u[k] - v[k], t1 = u[k + 1] - v[k + 1];
+                    const float t2 = u[k + 2] - v[k + 2], t3 = u[k + 3] - v[k + 3];
+                    s0 = fmaf(t0, t0, s0);
+                    s1 = fmaf(t1, t1, s1);
+                    s2 = fmaf(t2, t2, s2);
+                    s3 = fmaf(t3, t3, s3);
+                }
+            }
+        } else {
+            const float4* a = reinterpret_cast<const float4*>(R.Xf + (uint64_t)i * d);
+            const float4* b = reinterpret_cast<const float4*>(R.Xfb + (uint64_t)j * d);
 #pragma unroll 4
-        for (uint32_t c = 0; c < d / 4; ++c) {
-            const float4 u = __ldg(&a[c]), v = __ldg(&b[c]);
-            const float t0 = u.x - v.x, t1 = u.y - v.y, t2 = u.z - v.z, t3 = u.w - v.w;
-            s0 = fmaf(t0, t0, s0);
-            s1 = fmaf(t1, t1, s1);
-            s2 = fmaf(t2, t2, s2);
-            s3 = fmaf(t3, t3, s3);
+            for (uint32_t c = 0; c < d / 4; ++c) {
+                const float4 u = __ldg(&a[c]), v = __ldg(&b[c]);
+                const float t0 = u.x - v.x, t1 = u.y - v.y, t2 = u.z - v.z, t3 = u.w - v.w;
+                s0 = fmaf(t0, t0, s0);
+                s1 = fmaf(t1, t1, s1);
+                s2 = fmaf(t2, t2, s2);
+                s3 = fmaf(t3, t3, s3);
+            }
         }
         if (recheck_decide(X, d, perm, T, R, i, j, (s0 + s1) + (s2 + s3), exact_runs)) {
             atomicAdd(&counts[i], 1);
@@ -311,8 +342,13 @@ int launch_band_recheck2(const double* X, uint64_t n, uint32_t d, const uint32_t
     // warp per pair (more pairs in flight per load) for longer rows
     const bool thread = d <= 64 && d % 4 == 0 && (((uintptr_t)R.Xf | (uintptr_t)R.Xfb) & 15) == 0;
     if (thread) {
+        // 32-byte loads when the rows allow them (half the load instructions)
+        const bool v8 = d % 8 == 0 && (((uintptr_t)R.Xf | (uintptr_t)R.Xfb) & 31) == 0;
         const unsigned blocks = (unsigned)std::min<uint64_t>((nband + 255) / 256, 152ull * 32);
-        band_recheck_thread_kernel<<<blocks, 256, 0, s>>>(X, d, perm, T, R, band, nband, n, counts, st, e);
+        if (v8)
+            band_recheck_thread_kernel<true><<<blocks, 256, 0, s>>>(X, d, perm, T, R, band, nband, n, counts, st, e);
+        else
+            band_recheck_thread_kernel<false><<<blocks, 256, 0, s>>>(X, d, perm, T, R, band, nband, n, counts, st, e);
     } else {
         const uint64_t warps = (nband + 31) / 32;
         const unsigned blocks = (unsigned)std::min<uint64_t>((warps + 7) / 8, 152ull * 64);
