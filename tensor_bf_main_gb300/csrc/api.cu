@@ -146,15 +146,31 @@ static bool is_device_ptr(const void* p) {
     return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
-// Compact n x d rows (row stride ld) into device memory.
+// Compact n x d rows (row stride ld) into device memory.  With `defer`, dense
+// rows in pinned host memory (64 MB or more) are not copied here: *defer
+// describes them and the copy is left to the centring pass, which overlaps
+// it with its own work (*deferred = true).
 static int stage_points(const double* points, uint64_t n, uint32_t d, uint64_t ld, DBuf<double>& buf,
-                        const double** Xout, cudaStream_t s) {
+                        const double** Xout, cudaStream_t s, StageCopy* defer = nullptr,
+                        bool* deferred = nullptr) {
+    if (deferred) *deferred = false;
     const bool dev = is_device_ptr(points);
     if (dev && ld == d) {
         *Xout = points;
         return EJOIN_OK;
     }
     EJ_TRY(buf.alloc(n * d, s, "points"));
+    if (defer && !dev && ld == d && n * d * sizeof(double) >= (64ull << 20)) {
+        cudaPointerAttributes a;
+        if (cudaPointerGetAttributes(&a, points) == cudaSuccess && a.type == cudaMemoryTypeHost &&
+            a.devicePointer) {
+            *defer = StageCopy{points, (const double*)a.devicePointer};
+            *deferred = true;
+            *Xout = buf.p;
+            return EJOIN_OK;
+        }
+        cudaGetLastError();
+    }
     if (ld == d) {
         EJ_CUDA(cudaMemcpyAsync(buf.p, points, n * d * sizeof(double),
                                 dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
@@ -182,6 +198,7 @@ struct Join {
     int32_t* counts;         // device, >= n_pad entries, packed-row order
     const uint32_t* perm;    // packed row -> original row (null = identity)
     const Emit* em = nullptr;  // neighbour-list emission (null: counts only)
+    const StageCopy* stage = nullptr;  // X still to be copied (by the centring pass)
 };
 
 static uint64_t round_up(uint64_t v, uint64_t m) { return (v + m - 1) / m * m; }
@@ -454,7 +471,8 @@ static int run_screen16(Join& J, Fmt fmt, bool split, Learned& L) {
     EJ_TRY(Y32.alloc(J.n * J.d, J.s, "FP32 centred points"));
     EJ_TRY(Yerr.alloc(J.n, J.s, "centring error bounds"));
     CenterStats cs;
-    EJ_TRY(launch_center_stats(J.X, J.n, J.d, bad.p, mu.p, Y32.p, Yerr.p, &cs, J.s));
+    EJ_TRY(launch_center_stats(J.X, J.n, J.d, bad.p, mu.p, Y32.p, Yerr.p, &cs, J.s, false, J.stage));
+    J.stage = nullptr;
     tp.stop(J.s);
     const double ms_center = tp.ms();
     // The FP32 copies need the centred coordinates well inside the FP32 range:
@@ -613,10 +631,23 @@ static int self_join_impl(const double* points, uint64_t n, uint32_t d, double e
             default: return set_error(EJOIN_EINVAL, "unknown precision %d", prec);
         }
     };
+    StageCopy sc{};
     if (run) {
-        EJ_TRY(stage_points(points, n, d, ld, xbuf, &J.X, s));
         if (isinf(T)) prec = EJOIN_FP64_DIRECT;  // every non-NaN pair counts: judge only
-        EJ_TRY(run_once());
+        // the 16-bit screens start with the centring pass, which takes over
+        // the host-to-device copy of pinned input
+        const bool screen16 = prec == EJOIN_FP16 || prec == EJOIN_BF16 ||
+                              prec == EJOIN_BF16_SPLIT || prec == EJOIN_FP8_E4M3;
+        bool deferred = false;
+        EJ_TRY(stage_points(points, n, d, ld, xbuf, &J.X, s, screen16 ? &sc : nullptr, &deferred));
+        J.stage = deferred ? &sc : nullptr;
+        const int rc = run_once();
+        if (J.stage) {
+            // not taken over (an early failure): no pass may read X after this
+            J.stage = nullptr;
+            EJ_TRY(rc == EJOIN_OK ? set_error(EJOIN_EINTERNAL, "points were never staged") : rc);
+        }
+        EJ_TRY(rc);
     }
     DBuf<unsigned long long> tot;
     EJ_TRY(tot.alloc(1, s, "total"));

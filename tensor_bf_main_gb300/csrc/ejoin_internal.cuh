@@ -349,10 +349,21 @@ struct CenterStats {
     bool range = false;    // a coordinate beyond 2^120: the FP32 copy is unusable
     bool flushed = false;  // a nonzero coordinate below 2^-126 was replaced by 0
 };
+// A host-to-device copy of the points left to the centring pass: X (device,
+// allocated on the caller's stream) is filled from pinned host rows in
+// chunks on a side stream, and each chunk is centred as soon as it lands, so
+// the copy (bound by the host link) hides the centring.  host_dev is the
+// device-side address of the same pinned rows (the sample for the mean is
+// read from there before the copy completes).
+struct StageCopy {
+    const double* host;
+    const double* host_dev;
+};
 // mu_given: mu holds the mean to use (another point set's, FP32-representable).
+// sc: X is still to be copied from pinned host memory (null: X is in place).
 int launch_center_stats(const double* X, uint64_t n, uint32_t d, uint8_t* bad, double* mu,
                         float* Y32, float* Yerr, CenterStats* out, cudaStream_t s,
-                        bool mu_given = false);
+                        bool mu_given = false, const StageCopy* sc = nullptr);
 // FP64 centred copy Y[n_pad][dp] and per-row thresholds h, g for the DMMA screen.
 int launch_pack_dmma(const double* X, uint64_t n, uint64_t n_pad, const uint32_t* perm,
                      const uint8_t* bad, const double* mu, const DmmaParams& P, double* Y,

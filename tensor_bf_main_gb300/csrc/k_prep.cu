@@ -726,7 +726,8 @@ __global__ void tile_max_kernel(const float* __restrict__ beta, const float4* __
 }  // namespace
 
 int launch_center_stats(const double* X, uint64_t n, uint32_t d, uint8_t* bad, double* mu,
-                        float* Y32, float* Yerr, CenterStats* out, cudaStream_t s, bool mu_given) {
+                        float* Y32, float* Yerr, CenterStats* out, cudaStream_t s, bool mu_given,
+                        const StageCopy* sc) {
     *out = CenterStats{};
     DBuf<float> muf;
     EJ_TRY(muf.alloc(d, s, "FP32 mean"));
@@ -741,7 +742,8 @@ int launch_center_stats(const double* X, uint64_t n, uint32_t d, uint8_t* bad, d
         DBuf<uint32_t> pcnt;
         EJ_TRY(psum.alloc((size_t)nb * d, s, "sample column sums"));
         EJ_TRY(pcnt.alloc((size_t)nb * d, s, "sample column counts"));
-        sample_colsum_kernel<<<nb, 128, 0, s>>>(X, n, d, S, psum.p, pcnt.p);
+        // with a pending copy the sample rows are read from host memory
+        sample_colsum_kernel<<<nb, 128, 0, s>>>(sc ? sc->host_dev : X, n, d, S, psum.p, pcnt.p);
         EJ_CUDA(cudaGetLastError());
         sample_mean_kernel<<<(d + 127) / 128, 128, 0, s>>>(psum.p, pcnt.p, nb, d, mu, muf.p);
         EJ_CUDA(cudaGetLastError());
@@ -762,12 +764,63 @@ int launch_center_stats(const double* X, uint64_t n, uint32_t d, uint8_t* bad, d
         auto fn = vec ? center_kernel<2, 4> : center_kernel<1, 4>;
         int per_sm = 0;
         EJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 256, 0));
-        const uint64_t want = (n + 31) / 32;
-        const unsigned grid = (unsigned)std::max<uint64_t>(
-            1, std::min<uint64_t>(want, (uint64_t)sms * std::max(per_sm, 1)));
-        fn<<<grid, 256, 0, s>>>(X, n, d, muf.p, bad, Y32, Yerr, acc.p);
-        EJ_CUDA(cudaGetLastError());
-        note_launch();
+        auto center = [&](uint64_t r0, uint64_t rows) -> int {
+            const uint64_t want = (rows + 31) / 32;
+            const unsigned grid = (unsigned)std::max<uint64_t>(
+                1, std::min<uint64_t>(want, (uint64_t)sms * std::max(per_sm, 1)));
+            fn<<<grid, 256, 0, s>>>(X + r0 * d, rows, d, muf.p, bad + r0,
+                                    Y32 ? Y32 + r0 * d : nullptr, Yerr ? Yerr + r0 : nullptr,
+                                    acc.p);
+            EJ_CUDA(cudaGetLastError());
+            note_launch();
+            return EJOIN_OK;
+        };
+        if (!sc) {
+            EJ_TRY(center(0, n));
+        } else {
+            // chunked copy on a side stream; s waits for each chunk, then
+            // centres it.  The side stream first waits for s (X was allocated
+            // on s).  Chunk starts stay 16-byte aligned (even row counts).
+            constexpr int kChunks = 8;
+            cudaStream_t cs = nullptr;
+            cudaEvent_t ev[kChunks + 1] = {};
+            int rc = EJOIN_OK;
+            auto fail = [&](cudaError_t e, const char* what) {
+                if (rc == EJOIN_OK) rc = cuda_error(e, what, __FILE__, __LINE__);
+            };
+            cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+            if (e != cudaSuccess) fail(e, "cudaStreamCreateWithFlags");
+            for (int c = 0; c <= kChunks && rc == EJOIN_OK; ++c) {
+                e = cudaEventCreateWithFlags(&ev[c], cudaEventDisableTiming);
+                if (e != cudaSuccess) fail(e, "cudaEventCreateWithFlags");
+            }
+            if (rc == EJOIN_OK) {
+                if ((e = cudaEventRecord(ev[kChunks], s)) != cudaSuccess) fail(e, "cudaEventRecord");
+                else if ((e = cudaStreamWaitEvent(cs, ev[kChunks], 0)) != cudaSuccess)
+                    fail(e, "cudaStreamWaitEvent");
+            }
+            const uint64_t step = ((n + kChunks - 1) / kChunks + 1) & ~1ull;
+            for (uint64_t r0 = 0, c = 0; r0 < n && rc == EJOIN_OK; r0 += step, ++c) {
+                const uint64_t rows = std::min<uint64_t>(step, n - r0);
+                e = cudaMemcpyAsync(const_cast<double*>(X) + r0 * d, sc->host + r0 * d,
+                                    rows * d * sizeof(double), cudaMemcpyHostToDevice, cs);
+                if (e != cudaSuccess) { fail(e, "cudaMemcpyAsync (points)"); break; }
+                if ((e = cudaEventRecord(ev[c], cs)) != cudaSuccess) { fail(e, "cudaEventRecord"); break; }
+                if ((e = cudaStreamWaitEvent(s, ev[c], 0)) != cudaSuccess) {
+                    fail(e, "cudaStreamWaitEvent");
+                    break;
+                }
+                rc = center(r0, rows);
+            }
+            // on success s is ordered after every chunk copy; on failure no copy
+            // may stay in flight into memory the caller frees.  The stream and
+            // events are released once their work completes.
+            if (rc != EJOIN_OK && cs) cudaStreamSynchronize(cs);
+            for (int c = 0; c <= kChunks; ++c)
+                if (ev[c]) cudaEventDestroy(ev[c]);
+            if (cs) cudaStreamDestroy(cs);
+            if (rc != EJOIN_OK) return rc;
+        }
     }
     CenterAcc h;
     EJ_CUDA(cudaMemcpyAsync(&h, acc.p, sizeof h, cudaMemcpyDeviceToHost, s));

@@ -65,3 +65,25 @@ def test_c5_shape_fp8(ej, oracle_mod):
     check(ej, oracle_mod, x, eps, counts, total, nrows_oracle=8, nrows_gpu=128)
     cb, tb, _ = ej.self_join(x, eps, precision="bf16", proj_k=16, train_steps=20)
     assert tb == total and np.array_equal(cb, counts)
+
+
+def test_pinned_host_input_streams_copy(ej, oracle_mod):
+    """Pinned host rows (>= 64 MB) are copied in chunks by the centring pass;
+    counts and lists equal those of pageable and device-resident input."""
+    torch = pytest.importorskip("torch")
+    x = datagen.generate("c4", n=500_000)
+    eps = datagen.EPS["c4"]
+    xp = torch.from_numpy(x).pin_memory()
+    c_pin, t_pin, _ = ej.self_join(xp, eps, precision="bf16_split", proj_k=8)
+    c_np, t_np, _ = ej.self_join(x, eps, precision="bf16_split", proj_k=8)
+    c_dev, t_dev, _ = ej.self_join(torch.from_numpy(x).cuda(), eps, precision="bf16_split",
+                                   proj_k=8)
+    assert t_pin == t_np == t_dev
+    assert np.array_equal(c_pin, c_np) and np.array_equal(c_pin, c_dev)
+    check(ej, oracle_mod, x, eps, c_pin, t_pin, nrows_oracle=8)
+    c16, t16, _ = ej.self_join(xp, eps, precision="fp16")
+    assert t16 == t_pin and np.array_equal(c16, c_pin)
+    off_p, nb_p, _ = ej.neighbor_lists(xp, eps, precision="bf16_split", proj_k=8)
+    off_n, nb_n, _ = ej.neighbor_lists(x, eps, precision="bf16_split", proj_k=8)
+    assert np.array_equal(off_p, off_n) and np.array_equal(nb_p, nb_n)
+    assert int(off_p[-1]) == t_pin
