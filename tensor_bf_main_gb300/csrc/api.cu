@@ -530,6 +530,7 @@ static int run_screen16(Join& J, Fmt fmt, bool split, Learned& L) {
     R.sThi = P.sThi;
     R.c32 = (J.d + 8) * ldexp(1.0, -24) * 1.01;
     R.abs32 = (J.d + 8) * ldexp(1.0, -148);
+    finish_recheck32(R);
     // band records -> pairs, then the FP32 pre-check / exact FP64 recheck
     auto recheck = [&](const BandPair* band, uint64_t nrec, uint64_t npairs, DevStatus* st) {
         if (npairs == 0) return EJOIN_OK;
@@ -885,6 +886,7 @@ static int cross_join(Join& J, const double* Xq, uint64_t nq, int prec, int32_t*
             R.sThi = P.sThi;
             R.c32 = (J.d + 8) * ldexp(1.0, -24) * 1.01;
             R.abs32 = (J.d + 8) * ldexp(1.0, -148);
+            finish_recheck32(R);
             auto recheck = [&](const BandPair* band, uint64_t nrec, uint64_t npairs, DevStatus* st) {
                 if (npairs == 0) return EJOIN_OK;
                 DBuf<BandPair> pairs;

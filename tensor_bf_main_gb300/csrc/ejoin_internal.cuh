@@ -164,7 +164,15 @@ struct Recheck32 {
     double sTlo, sThi; // sqrt of the scaled oracle thresholds (down / up)
     double c32;        // relative bound of the FP32 squared-difference sum
     double abs32;      // absolute bound (FP32 underflow)
+    // the same constants as FP32 values rounded outward (finish_recheck32):
+    // the per-pair decision runs in FP32 with directed rounding (FP64 is slow
+    // on GB300)
+    float f_sTlo, f_sThi;  // sTlo rounded down, sThi rounded up
+    float f_kin, f_kout;   // 1 - c32 rounded down, 1 + c32 rounded up
+    float f_abs;           // abs32 rounded up
 };
+// Fills the FP32 constants of R from its FP64 ones (host).
+void finish_recheck32(Recheck32& R);
 
 // --------------------------------------------------------- device math --
 

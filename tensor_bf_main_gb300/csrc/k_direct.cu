@@ -188,6 +188,12 @@ __global__ void __launch_bounds__(256) band_recheck_kernel(const double* __restr
 //   rad_i + rad_j, and S from |w|^2 by the relative c32 (+ abs32), so
 //   S / (1 - c32) <= (sqrt(Tlo) - rad)^2   => neighbour
 //   S / (1 + c32) >  (sqrt(Thi) + rad)^2   => not a neighbour
+// i.e. S + abs32 <= (sqrt(Tlo) - rad)^2 (1 - c32) and
+//      S - abs32 >  (sqrt(Thi) + rad)^2 (1 + c32).
+// Both tests run in FP32 with every operation rounded in the safe direction
+// (the constants are rounded outward on the host), so they stay rigorous
+// without FP64, whose throughput on GB300 is a small fraction of FP32's.  An
+// infinite radius (bad or padding row) decides nothing.
 // Only the pairs left undecided (a tiny fraction) run the exact FP64 chain of
 // the reference arithmetic on the original rows.  Returns whether (i, j) is a
 // neighbour pair; counts the exact runs.
@@ -195,12 +201,11 @@ __device__ __forceinline__ bool recheck_decide(const double* __restrict__ X, uin
                                                const uint32_t* __restrict__ perm, double T,
                                                const Recheck32& R, uint32_t i, uint32_t j,
                                                float S, unsigned& exact_runs) {
-    const double Sd = (double)S;
-    const double rr = (double)R.rad[i] + (double)R.radb[j];
-    const double lo = R.sTlo - rr;
-    if (lo >= 0.0 && (Sd + R.abs32) / (1.0 - R.c32) <= lo * lo * (1.0 - 8 * kU)) return true;
-    const double hi = R.sThi + rr;
-    if ((Sd - R.abs32) / (1.0 + R.c32) > hi * hi * (1.0 + 8 * kU)) return false;
+    const float rr = __fadd_ru(R.rad[i], R.radb[j]);
+    const float lo = __fsub_rd(R.f_sTlo, rr);
+    if (lo >= 0.0f && __fadd_ru(S, R.f_abs) <= __fmul_rd(__fmul_rd(lo, lo), R.f_kin)) return true;
+    const float hi = __fadd_ru(R.f_sThi, rr);
+    if (__fsub_rd(S, R.f_abs) > __fmul_ru(__fmul_ru(hi, hi), R.f_kout)) return false;
     ++exact_runs;
     const uint64_t oi = perm ? perm[i] : i, oj = R.permb ? R.permb[j] : j;
     return exact_d2(X + oi * (uint64_t)d, R.Xb + oj * (uint64_t)d, d) <= T;
@@ -332,6 +337,26 @@ __global__ void __launch_bounds__(256) band_recheck_warp_kernel(const double* __
 }
 
 }  // namespace
+
+static float f32_down(double v) {
+    float f = (float)v;
+    if ((double)f > v) f = nextafterf(f, -INFINITY);
+    return f;
+}
+static float f32_up(double v) {
+    float f = (float)v;
+    if ((double)f < v) f = nextafterf(f, INFINITY);
+    return f;
+}
+
+void finish_recheck32(Recheck32& R) {
+    R.f_sTlo = f32_down(R.sTlo);
+    R.f_sThi = f32_up(R.sThi);
+    // 4 units of FP64 rounding cover the evaluation of 1 -/+ c32 in FP64
+    R.f_kin = f32_down((1.0 - R.c32) * (1.0 - 4 * kU));
+    R.f_kout = f32_up((1.0 + R.c32) * (1.0 + 4 * kU));
+    R.f_abs = f32_up(R.abs32 * (1.0 + 4 * kU));
+}
 
 int launch_band_recheck2(const double* X, uint64_t n, uint32_t d, const uint32_t* perm, double T,
                          const Recheck32& R, const BandPair* band, uint64_t nband, int32_t* counts,
