@@ -74,8 +74,12 @@ __global__ void __launch_bounds__(PJ_ROWS) project_kernel(
     const float* __restrict__ Y32, const float* __restrict__ Yerr, const uint8_t* __restrict__ bad,
     uint64_t n, uint32_t d, const float* __restrict__ P, uint32_t k, float pmax, float* proj,
     float* err, unsigned int* mn, unsigned int* mx) {
-    __shared__ float sY[PJ_ROWS * (PJ_CH + 1)];
-    __shared__ float sP[K * PJ_CH];
+    // rows at a pitch of PJ_CH + 4 floats (16-byte aligned rows; a quarter-warp
+    // of 16-byte row reads covers all banks once); P transposed [c][a], so
+    // each column's K weights are 16-byte broadcast loads
+    constexpr uint32_t PITCH = PJ_CH + 4;
+    __shared__ __align__(16) float sY[PJ_ROWS * PITCH];
+    __shared__ __align__(16) float sP[PJ_CH * K];
     __shared__ unsigned int smn[4][K], smx[4][K];
     const uint32_t t = threadIdx.x, lane = t & 31, w = t >> 5;
     // every chunk is a whole number of float4s when d % 4 == 0 (cw then too)
@@ -105,31 +109,38 @@ __global__ void __launch_bounds__(PJ_ROWS) project_kernel(
                     float4 v4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
                     if (i0 + r < n && c < cw)
                         v4 = __ldg(reinterpret_cast<const float4*>(Y32 + (i0 + r) * d + c0 + c));
-                    float* dst = sY + r * (PJ_CH + 1) + c;
-                    dst[0] = v4.x;
-                    dst[1] = v4.y;
-                    dst[2] = v4.z;
-                    dst[3] = v4.w;
+                    *reinterpret_cast<float4*>(sY + r * PITCH + c) = v4;
                 }
             } else {
                 for (uint32_t e = t; e < PJ_ROWS * PJ_CH; e += PJ_ROWS) {
                     const uint32_t r = e / PJ_CH, c = e % PJ_CH;
-                    sY[r * (PJ_CH + 1) + c] =
-                        (i0 + r < n && c < cw) ? Y32[(i0 + r) * d + c0 + c] : 0.0f;
+                    sY[r * PITCH + c] = (i0 + r < n && c < cw) ? Y32[(i0 + r) * d + c0 + c] : 0.0f;
                 }
             }
             for (uint32_t e = t; e < K * PJ_CH; e += PJ_ROWS) {
-                const uint32_t a = e / PJ_CH, c = e % PJ_CH;
+                const uint32_t c = e / K, a = e % K;
                 sP[e] = (a < k && c < cw) ? P[a * d + c0 + c] : 0.0f;
             }
             __syncthreads();
-            const float* y = sY + t * (PJ_CH + 1);
-#pragma unroll 4
-            for (uint32_t c = 0; c < cw; ++c) {
-                const float yc = y[c];
-                s2 = __fmaf_ru(yc, yc, s2);
+            // four columns per step (columns past cw hold zeros in sY and sP)
+            const float* y = sY + t * PITCH;
+#pragma unroll 2
+            for (uint32_t c = 0; c < cw; c += 4) {
+                const float4 y4 = *reinterpret_cast<const float4*>(y + c);
+                const float yv[4] = {y4.x, y4.y, y4.z, y4.w};
 #pragma unroll
-                for (int a = 0; a < K; ++a) acc[a] = fmaf(sP[a * PJ_CH + c], yc, acc[a]);
+                for (int u = 0; u < 4; ++u) {
+                    s2 = __fmaf_ru(yv[u], yv[u], s2);
+                    const float4* pp = reinterpret_cast<const float4*>(sP + (c + u) * K);
+#pragma unroll
+                    for (int a4 = 0; a4 < K / 4; ++a4) {
+                        const float4 wv = pp[a4];
+                        acc[4 * a4 + 0] = fmaf(wv.x, yv[u], acc[4 * a4 + 0]);
+                        acc[4 * a4 + 1] = fmaf(wv.y, yv[u], acc[4 * a4 + 1]);
+                        acc[4 * a4 + 2] = fmaf(wv.z, yv[u], acc[4 * a4 + 2]);
+                        acc[4 * a4 + 3] = fmaf(wv.w, yv[u], acc[4 * a4 + 3]);
+                    }
+                }
             }
         }
         if (i < n) {
@@ -296,15 +307,18 @@ __global__ void sample_pairs_kernel(const float* __restrict__ Y32, const uint8_t
         const bool act = e < M;
         uint64_t i = 0, j = 0;
         if (act) {
+            // indices by multiply-high reduction of the hashes (no 64-bit
+            // division, which the GPU emulates in software)
             const uint64_t h1 = splitmix64(seed ^ (e * 0x9E3779B97F4A7C15ull));
             const uint64_t h2 = splitmix64(h1);
             if (e & 1) {
-                i = h1 % n;
-                j = h2 % n;
+                i = __umul64hi(h1, n);
+                j = __umul64hi(h2, n);
             } else {
-                const uint64_t t = h1 % n;
-                uint64_t u = t + 1 + (h2 % window);
-                if (u >= n) u = t >= 1 + (h2 % window) ? t - 1 - (h2 % window) : 0;
+                const uint64_t t = __umul64hi(h1, n);
+                const uint64_t off = 1 + (uint32_t)h2 % window;
+                uint64_t u = t + off;
+                if (u >= n) u = t >= off ? t - off : 0;
                 i = perm ? perm[t] : t;
                 j = perm ? perm[u] : u;
             }

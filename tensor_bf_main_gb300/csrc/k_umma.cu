@@ -162,26 +162,13 @@ __device__ __forceinline__ void col_counts(uint32_t inm, int* cacc, uint32_t lan
     }
 }
 
-__device__ __forceinline__ float max3f(float x, float y, float z) {
-    float r;
-    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(x), "f"(y), "f"(z));
-    return r;
-}
-
-// In / band bit masks of one 32 x 32 chunk (lane = row, v[c] = column c).
+// In / band bit masks of one 32 x 32 chunk (lane = row, v[c] = column c; mx
+// = the lane's maximum, reduced by the tensor-memory load).
 // Fast path: if max + W < 0 over the chunk, every pair in it is certainly out
 // (rounding of the FP32 add is monotone, so max + W >= 0 whenever any
 // element is >= -W).
-__device__ __forceinline__ bool classify(const uint32_t (&v)[32], float W, uint32_t& inm,
-                                         uint32_t& bandm) {
-    float m10[11];
-#pragma unroll
-    for (int j = 0; j < 10; ++j)
-        m10[j] = max3f(__uint_as_float(v[j]), __uint_as_float(v[j + 10]), __uint_as_float(v[j + 20]));
-    m10[10] = fmaxf(__uint_as_float(v[30]), __uint_as_float(v[31]));
-    const float mx = fmaxf(max3f(max3f(m10[0], m10[1], m10[2]), max3f(m10[3], m10[4], m10[5]),
-                                 max3f(m10[6], m10[7], m10[8])),
-                           fmaxf(m10[9], m10[10]));
+__device__ __forceinline__ bool classify(const uint32_t (&v)[32], float mx, float W,
+                                         uint32_t& inm, uint32_t& bandm) {
     inm = bandm = 0;
     if (!__any_sync(FULL, mx + W >= 0.0f)) return false;
     // sign bits, four independent 8-column chains
@@ -496,17 +483,18 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             const uint32_t taddr = tmem + ((q * 32u) << 16) + b * ACC_COLS + cg * 64u;
             uint32_t in0 = 0, bd0 = 0, in1 = 0, bd1 = 0;
             bool busy0 = false, busy1 = false;
+            float mx = 0.0f;
             if (active) {
-                ptx::tmem_ld_32x32b_x32(taddr, v);
+                ptx::tmem_ld_max_32x32b_x32(taddr, v, mx);
                 ptx::tmem_ld_wait();
-                busy0 = classify(v, W, in0, bd0);
-                ptx::tmem_ld_32x32b_x32(taddr + 32u, v);
+                busy0 = classify(v, mx, W, in0, bd0);
+                ptx::tmem_ld_max_32x32b_x32(taddr + 32u, v, mx);
                 ptx::tmem_ld_wait();
             }
             ptx::tc_fence_before();
             __syncwarp();
             if (lane == 0) ptx::mbar_arrive(&S.tempty[b]);
-            if (active) busy1 = classify(v, W, in1, bd1);
+            if (active) busy1 = classify(v, mx, W, in1, bd1);
             // the counts of buffer b were flushed and cleared for block it - 2
             if (!ptx::mbar_wait(&S.fdone[b], (use & 1u) ^ 1u, a.st, 32)) break;
             if (busy0 || busy1) {
