@@ -237,29 +237,68 @@ __global__ void key_kernel(const float* __restrict__ proj, uint64_t n, uint32_t 
 // Per 128-row tile of the sorted order: [lo, hi] of every projected
 // coordinate, widened by each row's error bound (outward rounding);
 // non-finite and padding rows are left out (they are never neighbours).
-__global__ void boxes_kernel(const float* __restrict__ proj, const float* __restrict__ err,
-                             const uint32_t* __restrict__ perm, uint64_t n, uint32_t k,
-                             float* lo, float* hi) {
+// A thread per row reads its row's K projections with 16-byte loads (one
+// gathered row instead of K scattered words), then warps and the block
+// reduce the bounds (min / max are exact in any order).
+template <int K>
+__global__ void __launch_bounds__(128) boxes_kernel(const float* __restrict__ proj,
+                                                    const float* __restrict__ err,
+                                                    const uint32_t* __restrict__ perm, uint64_t n,
+                                                    uint32_t k, float* lo, float* hi) {
+    __shared__ float sl[4][K], sh[4][K];
     const uint64_t t = blockIdx.x;
-    for (uint32_t a = threadIdx.y; a < k; a += blockDim.y) {
-        float l = INFINITY, h = -INFINITY;
-        for (uint32_t r = threadIdx.x; r < 128; r += blockDim.x) {
-            const uint64_t p = t * 128 + r;
-            if (p >= n) continue;
-            const uint64_t i = perm[p];
-            const float v = proj[i * k + a], e = err[i];
-            if (isnan(v) || isnan(e)) continue;
-            l = fminf(l, __fsub_rd(v, e));
-            h = fmaxf(h, __fadd_ru(v, e));
+    const uint32_t r = threadIdx.x, lane = r & 31, w = r >> 5;
+    float l[K], h[K];
+#pragma unroll
+    for (int a = 0; a < K; ++a) {
+        l[a] = INFINITY;
+        h[a] = -INFINITY;
+    }
+    const uint64_t p = t * 128 + r;
+    if (p < n) {
+        const uint64_t i = perm[p];
+        const float e = err[i];
+        float v[K];
+        if (k == (uint32_t)K) {
+            const float4* src = reinterpret_cast<const float4*>(proj + i * K);
+#pragma unroll
+            for (int a4 = 0; a4 < K / 4; ++a4) {
+                const float4 q = __ldg(&src[a4]);
+                v[4 * a4 + 0] = q.x;
+                v[4 * a4 + 1] = q.y;
+                v[4 * a4 + 2] = q.z;
+                v[4 * a4 + 3] = q.w;
+            }
+        } else {
+#pragma unroll
+            for (int a = 0; a < K; ++a) v[a] = a < (int)k ? proj[i * k + a] : 0.0f;
         }
+        if (!isnan(e)) {
+#pragma unroll
+            for (int a = 0; a < K; ++a)
+                if (a < (int)k && !isnan(v[a])) {
+                    l[a] = __fsub_rd(v[a], e);
+                    h[a] = __fadd_ru(v[a], e);
+                }
+        }
+    }
+#pragma unroll
+    for (int a = 0; a < K; ++a)
         for (int o = 16; o; o >>= 1) {
-            l = fminf(l, __shfl_xor_sync(0xffffffffu, l, o));
-            h = fmaxf(h, __shfl_xor_sync(0xffffffffu, h, o));
+            l[a] = fminf(l[a], __shfl_xor_sync(0xffffffffu, l[a], o));
+            h[a] = fmaxf(h[a], __shfl_xor_sync(0xffffffffu, h[a], o));
         }
-        if (threadIdx.x == 0) {
-            lo[t * k + a] = l;
-            hi[t * k + a] = h;
+    if (lane == 0) {
+#pragma unroll
+        for (int a = 0; a < K; ++a) {
+            sl[w][a] = l[a];
+            sh[w][a] = h[a];
         }
+    }
+    __syncthreads();
+    if (r < k) {
+        lo[t * k + r] = fminf(fminf(sl[0][r], sl[1][r]), fminf(sl[2][r], sl[3][r]));
+        hi[t * k + r] = fmaxf(fmaxf(sh[0][r], sh[1][r]), fmaxf(sh[2][r], sh[3][r]));
     }
 }
 
@@ -745,8 +784,12 @@ int learned_order(const float* Y32, const float* Yerr, const uint8_t* bad, uint6
         EJ_TRY(boxes->hi.alloc(nt * k, s, "tile boxes"));
         EJ_TRY(boxes->slo.alloc(ns * k, s, "super-block boxes"));
         EJ_TRY(boxes->shi.alloc(ns * k, s, "super-block boxes"));
-        boxes_kernel<<<(unsigned)nt, dim3(32, 8), 0, s>>>(proj.p, err.p, perm.p, n, k,
-                                                          boxes->lo.p, boxes->hi.p);
+        if (k <= 8)
+            boxes_kernel<8><<<(unsigned)nt, 128, 0, s>>>(proj.p, err.p, perm.p, n, k, boxes->lo.p,
+                                                         boxes->hi.p);
+        else
+            boxes_kernel<16><<<(unsigned)nt, 128, 0, s>>>(proj.p, err.p, perm.p, n, k, boxes->lo.p,
+                                                          boxes->hi.p);
         EJ_CUDA(cudaGetLastError());
         superbox_kernel<<<(unsigned)((ns * k + 255) / 256), 256, 0, s>>>(
             boxes->lo.p, boxes->hi.p, nt, k, kSuperTiles, boxes->slo.p, boxes->shi.p);

@@ -43,7 +43,9 @@ __global__ void sample_colsum_kernel(const double* __restrict__ X, uint64_t n, u
         uint32_t c = 0;
 #pragma unroll 8
         for (uint64_t j = j0; j < j1; ++j) {
-            const uint64_t row = j * n / S;  // evenly spread, increasing
+            // j * n / S, evenly spread and increasing; S is n or the constant
+            // kMeanSample, so no run-time 64-bit division (emulated on the GPU)
+            const uint64_t row = S == n ? j : j * n / kMeanSample;
             const double v = X[row * d + k];
             if (isfinite(v)) {
                 s += v;
