@@ -428,8 +428,14 @@ __host__ __device__ inline uint32_t train_slices(uint32_t d, uint32_t K) {
 // with integer atomics: integer addition is associative, so the result does
 // not depend on the order in which blocks finish (bit-reproducible training).
 constexpr double kFix = 1099511627776.0;  // 2^40
+// v * 2^40 is exact in FP32 as in FP64, so the FP32 conversion gives the same
+// integer (FP64 arithmetic is slow on GB300)
 __device__ __forceinline__ void fix_add(unsigned long long* dst, float v) {
-    atomicAdd(dst, (unsigned long long)__double2ll_rn((double)v * kFix));
+    atomicAdd(dst, (unsigned long long)__float2ll_rn(v * 1099511627776.0f));
+}
+// integer / 2^40 as FP32: one rounding (int64 -> FP32), then an exact scaling
+__device__ __forceinline__ float fix_value(unsigned long long g) {
+    return __ll2float_rn((long long)g) * 9.094947017729282379e-13f;
 }
 
 // Forward + hinge loss + backward for M pairs; G += dL/dP, loss += sum of
@@ -644,7 +650,7 @@ __global__ void adam_renorm_kernel(float* P, unsigned long long* G, float* m1, f
     extern __shared__ float sPa[];  // k * d
     const uint32_t nel = k * d;
     for (uint32_t e = threadIdx.x; e < nel; e += blockDim.x) {
-        const float g = (float)((double)(long long)G[e] / kFix);
+        const float g = fix_value(G[e]);
         G[e] = 0ull;
         const float a = b1 * m1[e] + (1.0f - b1) * g;
         const float b = b2 * m2[e] + (1.0f - b2) * g * g;
