@@ -114,7 +114,9 @@ def cpu_rate(x, eps, seconds, seed=0):
 
 
 class Clocks:
-    """nvidia-smi sampling during the timed region."""
+    """nvidia-smi sampling (every 50 ms) from the warm-up steps through the
+    timed region: the timed region alone is often shorter than one sample
+    period, and the warm-up steps run the same workload."""
 
     def __init__(self):
         self.proc = None
@@ -127,10 +129,10 @@ class Clocks:
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(gpu_index),
-                 "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "--query-gpu=timestamp,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
                  "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
                  "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=self.f, stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
@@ -146,7 +148,7 @@ class Clocks:
         self.f.close()
         rows = []
         for line in open(self.path):
-            parts = [p.strip() for p in line.split(",")]
+            parts = [p.strip() for p in line.split(",")][1:]  # drop the timestamp
             if len(parts) < 8:
                 continue
             try:
@@ -234,12 +236,12 @@ def run_ours(args):
         if dist:
             dist.barrier()
 
+    clocks = Clocks()
+    clocks.start(dev.index)
     for _ in range(args.warmup):
         ej.self_join(xd, eps, **kw)
     barrier()
     torch.cuda.synchronize(dev)
-    clocks = Clocks()
-    clocks.start(dev.index)
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     stats = []
