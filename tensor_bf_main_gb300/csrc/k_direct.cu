@@ -220,12 +220,29 @@ __device__ __forceinline__ void recheck_totals(DevStatus* st, unsigned hits, uns
     }
 }
 
-// 32-byte read-only load (eight floats; p 32-byte aligned).
+// Read-only row loads that do not allocate in L1: the band rows are
+// gathered with little reuse, and allocating them thrashed L1 (measured on
+// c4: the recheck ran 1.4x faster without allocation).  32 bytes (p 32-byte
+// aligned) or 16 bytes (p 16-byte aligned).
 __device__ __forceinline__ void ldg8(const float* p, float (&r)[8]) {
+    asm("ld.global.nc.L1::no_allocate.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=f"(r[0]), "=f"(r[1]), "=f"(r[2]), "=f"(r[3]), "=f"(r[4]), "=f"(r[5]), "=f"(r[6]),
+          "=f"(r[7])
+        : "l"(p));
+}
+// cached forms, for the row a warp reuses across consecutive pairs
+__device__ __forceinline__ void ldg8c(const float* p, float (&r)[8]) {
     asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
         : "=f"(r[0]), "=f"(r[1]), "=f"(r[2]), "=f"(r[3]), "=f"(r[4]), "=f"(r[5]), "=f"(r[6]),
           "=f"(r[7])
         : "l"(p));
+}
+__device__ __forceinline__ float4 ldg4(const float* p) {
+    float4 r;
+    asm("ld.global.nc.L1::no_allocate.v4.f32 {%0,%1,%2,%3}, [%4];"
+        : "=f"(r.x), "=f"(r.y), "=f"(r.z), "=f"(r.w)
+        : "l"(p));
+    return r;
 }
 
 // Short rows (d <= 64, 16-byte aligned): a thread per pair streams both rows
@@ -271,7 +288,8 @@ __global__ void __launch_bounds__(256) band_recheck_thread_kernel(const double* 
             const float4* b = reinterpret_cast<const float4*>(R.Xfb + (uint64_t)j * d);
 #pragma unroll 4
             for (uint32_t c = 0; c < d / 4; ++c) {
-                const float4 u = __ldg(&a[c]), v = __ldg(&b[c]);
+                const float4 u = ldg4(reinterpret_cast<const float*>(a + c));
+                const float4 v = ldg4(reinterpret_cast<const float*>(b + c));
                 const float t0 = u.x - v.x, t1 = u.y - v.y, t2 = u.z - v.z, t3 = u.w - v.w;
                 s0 = fmaf(t0, t0, s0);
                 s1 = fmaf(t1, t1, s1);
@@ -290,8 +308,10 @@ __global__ void __launch_bounds__(256) band_recheck_thread_kernel(const double* 
 }
 
 // Longer rows: a warp takes 32 band pairs; for each pair the lanes stream the
-// two rows (coalesced) and reduce S across the warp, and lane p then decides
-// pair p.
+// two rows (coalesced; with VEC = 8, eight floats per lane and load when d is
+// a multiple of 256 and the rows are 32-byte aligned) and reduce S across the
+// warp, and lane p then decides pair p.
+template <int VEC>
 __global__ void __launch_bounds__(256) band_recheck_warp_kernel(const double* __restrict__ X,
                                                                 uint32_t d,
                                                                 const uint32_t* __restrict__ perm,
@@ -319,9 +339,22 @@ __global__ void __launch_bounds__(256) band_recheck_warp_kernel(const double* __
             const float* a = R.Xf + (uint64_t)i * d;
             const float* b = R.Xfb + (uint64_t)j * d;
             float S = 0.0f;
-            for (uint32_t c = lane; c < d; c += 32) {
-                const float t = a[c] - b[c];
-                S = fmaf(t, t, S);
+            if (VEC == 8) {
+                for (uint32_t c = 8 * lane; c < d; c += 256) {
+                    float u[8], w[8];
+                    ldg8c(a + c, u);
+                    ldg8(b + c, w);
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) {
+                        const float t = u[k] - w[k];
+                        S = fmaf(t, t, S);
+                    }
+                }
+            } else {
+                for (uint32_t c = lane; c < d; c += 32) {
+                    const float t = a[c] - b[c];
+                    S = fmaf(t, t, S);
+                }
             }
             for (int o = 16; o; o >>= 1) S += __shfl_xor_sync(0xffffffffu, S, o);
             if (lane == q) mine = S;
@@ -377,7 +410,13 @@ int launch_band_recheck2(const double* X, uint64_t n, uint32_t d, const uint32_t
     } else {
         const uint64_t warps = (nband + 31) / 32;
         const unsigned blocks = (unsigned)std::min<uint64_t>((warps + 7) / 8, 152ull * 64);
-        band_recheck_warp_kernel<<<blocks, 256, 0, s>>>(X, d, perm, T, R, band, nband, n, counts, st, e);
+        const uintptr_t al = (uintptr_t)R.Xf | (uintptr_t)R.Xfb;
+        // 32-byte loads (the streamed row j not allocated in L1) for d a
+        // multiple of 256; measured no faster than scalar loads at d = 128
+        if (d % 256 == 0 && (al & 31) == 0)
+            band_recheck_warp_kernel<8><<<blocks, 256, 0, s>>>(X, d, perm, T, R, band, nband, n, counts, st, e);
+        else
+            band_recheck_warp_kernel<1><<<blocks, 256, 0, s>>>(X, d, perm, T, R, band, nband, n, counts, st, e);
     }
     EJ_CUDA(cudaGetLastError());
     note_launch();
