@@ -438,6 +438,114 @@ __device__ __forceinline__ float fix_value(unsigned long long g) {
     return __ll2float_rn((long long)g) * 9.094947017729282379e-13f;
 }
 
+// One Adam step on P from G (G is cleared for the next step), then the
+// power-iteration renormalisation P <- P / max(1, 1.02 s): s is the Rayleigh
+// quotient estimate of ||P||_2 from (P P^T)^32 (five normalised squarings, so
+// it converges when the leading eigenvalues are close).  One block; k <= 16;
+// P is kept in shared memory (sPa: k * d floats) between the phases.  Run by
+// one whole block (blockDim.x a multiple of 32): the separate kernel below,
+// or the last block of train_step_kernel.
+__device__ void adam_renorm_block(float* P, unsigned long long* G, float* m1, float* m2,
+                                  uint32_t k, uint32_t d, float lr, float b1, float b2, float c1,
+                                  float c2, int renorm, float* sigma_out, float* sPa) {
+    __shared__ float M[16 * 16], A[16 * 16], B[16 * 16];
+    __shared__ float v[16];
+    __shared__ float lam;
+    const uint32_t nel = k * d;
+    for (uint32_t e = threadIdx.x; e < nel; e += blockDim.x) {
+        const float g = fix_value(__ldcg(&G[e]));  // L2: other blocks added it
+        G[e] = 0ull;
+        const float a = b1 * m1[e] + (1.0f - b1) * g;
+        const float b = b2 * m2[e] + (1.0f - b2) * g * g;
+        m1[e] = a;
+        m2[e] = b;
+        const float pv = P[e] - lr * (a / c1) / (sqrtf(b / c2) + 1e-8f);
+        sPa[e] = pv;
+        if (!renorm) P[e] = pv;
+    }
+    if (!renorm) return;
+    __syncthreads();
+    // M = P P^T: warp per entry
+    const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x / 32, nw = blockDim.x / 32;
+    for (uint32_t e = wid; e < k * k; e += nw) {
+        const uint32_t a = e / k, b = e % k;
+        float s = 0.0f;
+        for (uint32_t c = lane; c < d; c += 32) s = fmaf(sPa[a * d + c], sPa[b * d + c], s);
+        for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) {
+            M[e] = s;
+            A[e] = s;
+        }
+    }
+    // the k x k part runs in warp 0 (warp-level synchronisation only): five
+    // normalised squarings, 8 power-iteration steps, the Rayleigh quotient
+    if (wid == 0) {
+        const uint32_t kk = k * k;
+        for (int sq = 0; sq < 5; ++sq) {
+            float mx = 0.0f;
+            for (uint32_t e = lane; e < kk; e += 32) mx = fmaxf(mx, fabsf(A[e]));
+            for (int o = 16; o; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+            const float inv = mx > 0.0f ? 1.0f / mx : 0.0f;
+            for (uint32_t e = lane; e < kk; e += 32) {
+                const uint32_t a = e / k, b = e % k;
+                float s = 0.0f;
+                for (uint32_t c = 0; c < k; ++c) s = fmaf(A[a * k + c] * inv, A[c * k + b] * inv, s);
+                B[e] = s;
+            }
+            __syncwarp();
+            for (uint32_t e = lane; e < kk; e += 32) A[e] = B[e];
+            __syncwarp();
+        }
+        float vl = lane < k ? 1.0f + 0.01f * lane : 0.0f;  // lane a holds v[a]
+        for (int it = 0; it < 8; ++it) {
+            if (lane < k) v[lane] = vl;
+            __syncwarp();
+            float s = 0.0f;
+            if (lane < k)
+                for (uint32_t b = 0; b < k; ++b) s = fmaf(A[lane * k + b], v[b], s);
+            float nn = s * s;
+            for (int o = 16; o; o >>= 1) nn += __shfl_xor_sync(0xffffffffu, nn, o);
+            vl = nn > 0.0f ? s * rsqrtf(nn) : 0.0f;
+            __syncwarp();
+        }
+        if (lane < k) v[lane] = vl;
+        __syncwarp();
+        float num = 0.0f, den = 0.0f;
+        if (lane < k) {
+            float s = 0.0f;
+            for (uint32_t b = 0; b < k; ++b) s = fmaf(M[lane * k + b], v[b], s);
+            num = vl * s;
+            den = vl * vl;
+        }
+        for (int o = 16; o; o >>= 1) {
+            num += __shfl_xor_sync(0xffffffffu, num, o);
+            den += __shfl_xor_sync(0xffffffffu, den, o);
+        }
+        if (lane == 0) lam = den > 0.0f ? num / den : 0.0f;
+    }
+    __syncthreads();
+    const float sig = sqrtf(fmaxf(lam, 0.0f)) * 1.02f;
+    const float scale = sig > 1.0f ? 1.0f / sig : 1.0f;
+    for (uint32_t e = threadIdx.x; e < nel; e += blockDim.x) P[e] = sPa[e] * scale;
+    if (threadIdx.x == 0 && sigma_out) *sigma_out = sig;
+}
+
+__global__ void adam_renorm_kernel(float* P, unsigned long long* G, float* m1, float* m2,
+                                   uint32_t k, uint32_t d, float lr, float b1, float b2, float c1,
+                                   float c2, int renorm, float* sigma_out) {
+    extern __shared__ float sPa[];  // k * d
+    adam_renorm_block(P, G, m1, m2, k, d, lr, b1, b2, c1, c2, renorm, sigma_out, sPa);
+}
+
+// Adam state of a training step fused into train_step_kernel (done == null:
+// gradient only).
+struct AdamArgs {
+    float* m1;
+    float* m2;
+    float lr, b1, b2, c1, c2;
+    unsigned int* done;  // blocks finished (reset by the last one)
+};
+
 // Forward + hinge loss + backward for M pairs; G += dL/dP, loss += sum of
 // hinge terms / M (fixed-point accumulators).  A tile of TP pairs is staged
 // once in shared memory (row pitch d + 1: conflict-free) and serves
@@ -447,9 +555,9 @@ __device__ __forceinline__ float fix_value(unsigned long long g) {
 //   backward  Q threads per column c, each with K accumulators over every
 //             Q-th pair; the Q partials are then added in a fixed order.
 template <int K>
-__global__ void __launch_bounds__(TRAIN_THREADS) train_step_kernel(const float* __restrict__ P,
-                                                                   uint32_t k, uint32_t d,
-                                                                   PairBatch pb, uint64_t M,
+__global__ void __launch_bounds__(TRAIN_THREADS) train_step_kernel(float* P, uint32_t k,
+                                                                   uint32_t d, PairBatch pb,
+                                                                   uint64_t M, AdamArgs ad,
                                                                    unsigned long long* G,
                                                                    unsigned long long* loss) {
     extern __shared__ float4 sm4[];
@@ -472,14 +580,14 @@ __global__ void __launch_bounds__(TRAIN_THREADS) train_step_kernel(const float* 
         const uint32_t np = (M - base) < TP ? (uint32_t)(M - base) : TP;
         __syncthreads();
         {
-            // 16-byte loads, four in flight per thread (tile starts are 16-byte
+            // 16-byte loads, up to sixteen in flight per thread (tile starts are 16-byte
             // aligned: base is a multiple of TP, itself a multiple of 4 or d is)
             const float* src = pb.V + base * d;
             const uint32_t ne = np * d;
             const bool al = (((uintptr_t)src) & 15) == 0;
             const uint32_t n4 = al ? ne / 4 : 0;
             const float4* src4 = reinterpret_cast<const float4*>(src);
-#pragma unroll 4
+#pragma unroll 16
             for (uint32_t e4 = threadIdx.x; e4 < n4; e4 += blockDim.x) {
                 const float4 v4 = __ldg(&src4[e4]);
                 const float vv[4] = {v4.x, v4.y, v4.z, v4.w};
@@ -634,98 +742,21 @@ __global__ void __launch_bounds__(TRAIN_THREADS) train_step_kernel(const float* 
         if (sG[el] != 0.0f) fix_add(&G[el], sG[el]);
     for (int o = 16; o; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
     if ((threadIdx.x & 31) == 0 && lsum != 0.0f) fix_add(loss, lsum * invM);
+    if (!ad.done) return;
+    // the last block to finish runs the Adam step and the renormalisation
+    // (every block has read P; the gradient atomics are complete once the
+    // counter shows all blocks); sPT (K * d floats) is free for P
+    __shared__ unsigned s_last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = atomicAdd(ad.done, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    adam_renorm_block(P, G, ad.m1, ad.m2, k, d, ad.lr, ad.b1, ad.b2, ad.c1, ad.c2, 1, nullptr, sPT);
+    if (threadIdx.x == 0) *ad.done = 0u;
 }
 
-// One Adam step on P from G (G is cleared for the next step), then the
-// power-iteration renormalisation P <- P / max(1, 1.02 s): s is the Rayleigh
-// quotient estimate of ||P||_2 from (P P^T)^32 (five normalised squarings, so
-// it converges when the leading eigenvalues are close).  One block; k <= 16;
-// P is kept in shared memory (k * d floats, dynamic) between the phases.
-__global__ void adam_renorm_kernel(float* P, unsigned long long* G, float* m1, float* m2,
-                                   uint32_t k, uint32_t d, float lr, float b1, float b2, float c1,
-                                   float c2, int renorm, float* sigma_out) {
-    __shared__ float M[16 * 16], A[16 * 16], B[16 * 16];
-    __shared__ float v[16];
-    __shared__ float lam;
-    extern __shared__ float sPa[];  // k * d
-    const uint32_t nel = k * d;
-    for (uint32_t e = threadIdx.x; e < nel; e += blockDim.x) {
-        const float g = fix_value(G[e]);
-        G[e] = 0ull;
-        const float a = b1 * m1[e] + (1.0f - b1) * g;
-        const float b = b2 * m2[e] + (1.0f - b2) * g * g;
-        m1[e] = a;
-        m2[e] = b;
-        const float pv = P[e] - lr * (a / c1) / (sqrtf(b / c2) + 1e-8f);
-        sPa[e] = pv;
-        if (!renorm) P[e] = pv;
-    }
-    if (!renorm) return;
-    __syncthreads();
-    // M = P P^T: warp per entry
-    const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x / 32, nw = blockDim.x / 32;
-    for (uint32_t e = wid; e < k * k; e += nw) {
-        const uint32_t a = e / k, b = e % k;
-        float s = 0.0f;
-        for (uint32_t c = lane; c < d; c += 32) s = fmaf(sPa[a * d + c], sPa[b * d + c], s);
-        for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-        if (lane == 0) {
-            M[e] = s;
-            A[e] = s;
-        }
-    }
-    // the k x k part runs in warp 0 (warp-level synchronisation only): five
-    // normalised squarings, 8 power-iteration steps, the Rayleigh quotient
-    if (wid == 0) {
-        const uint32_t kk = k * k;
-        for (int sq = 0; sq < 5; ++sq) {
-            float mx = 0.0f;
-            for (uint32_t e = lane; e < kk; e += 32) mx = fmaxf(mx, fabsf(A[e]));
-            for (int o = 16; o; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-            const float inv = mx > 0.0f ? 1.0f / mx : 0.0f;
-            for (uint32_t e = lane; e < kk; e += 32) {
-                const uint32_t a = e / k, b = e % k;
-                float s = 0.0f;
-                for (uint32_t c = 0; c < k; ++c) s = fmaf(A[a * k + c] * inv, A[c * k + b] * inv, s);
-                B[e] = s;
-            }
-            __syncwarp();
-            for (uint32_t e = lane; e < kk; e += 32) A[e] = B[e];
-            __syncwarp();
-        }
-        float vl = lane < k ? 1.0f + 0.01f * lane : 0.0f;  // lane a holds v[a]
-        for (int it = 0; it < 8; ++it) {
-            if (lane < k) v[lane] = vl;
-            __syncwarp();
-            float s = 0.0f;
-            if (lane < k)
-                for (uint32_t b = 0; b < k; ++b) s = fmaf(A[lane * k + b], v[b], s);
-            float nn = s * s;
-            for (int o = 16; o; o >>= 1) nn += __shfl_xor_sync(0xffffffffu, nn, o);
-            vl = nn > 0.0f ? s * rsqrtf(nn) : 0.0f;
-            __syncwarp();
-        }
-        if (lane < k) v[lane] = vl;
-        __syncwarp();
-        float num = 0.0f, den = 0.0f;
-        if (lane < k) {
-            float s = 0.0f;
-            for (uint32_t b = 0; b < k; ++b) s = fmaf(M[lane * k + b], v[b], s);
-            num = vl * s;
-            den = vl * vl;
-        }
-        for (int o = 16; o; o >>= 1) {
-            num += __shfl_xor_sync(0xffffffffu, num, o);
-            den += __shfl_xor_sync(0xffffffffu, den, o);
-        }
-        if (lane == 0) lam = den > 0.0f ? num / den : 0.0f;
-    }
-    __syncthreads();
-    const float sig = sqrtf(fmaxf(lam, 0.0f)) * 1.02f;
-    const float scale = sig > 1.0f ? 1.0f / sig : 1.0f;
-    for (uint32_t e = threadIdx.x; e < nel; e += blockDim.x) P[e] = sPa[e] * scale;
-    if (threadIdx.x == 0 && sigma_out) *sigma_out = sig;
-}
 
 }  // namespace
 
@@ -836,6 +867,9 @@ int train_projection_dev(const float* Y32, const uint8_t* bad, uint64_t n, uint3
     EJ_TRY(m1.zero(s));
     EJ_TRY(m2.zero(s));
     EJ_TRY(loss.zero(s));
+    DBuf<unsigned int> done;  // blocks finished per step (the fused Adam step)
+    EJ_TRY(done.alloc(1, s, "step counter"));
+    EJ_TRY(done.zero(s));
     const uint64_t M = std::max<uint64_t>(pairs ? pairs : (1u << 20), 256);
     const uint64_t B = std::min<uint64_t>(M, 65536);  // minibatch
     DBuf<float> V, tgt;
@@ -846,10 +880,6 @@ int train_projection_dev(const float* Y32, const uint8_t* bad, uint64_t n, uint3
     const float b1 = 0.9f, b2 = 0.999f, lr = 0.02f;
     const size_t shm = train_smem_bytes(k, d);
     if (shm > 220 * 1024) return set_error(EJOIN_EUNSUPPORTED, "projection too large for training");
-    const size_t ashm = (size_t)k * d * sizeof(float);  // adam_renorm_kernel: P in shared memory
-    if (ashm > 220 * 1024) return set_error(EJOIN_EUNSUPPORTED, "projection too large for training");
-    EJ_CUDA(cudaFuncSetAttribute(adam_renorm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)ashm));
     auto step_fn = k <= 8 ? train_step_kernel<8> : train_step_kernel<16>;
     EJ_CUDA(cudaFuncSetAttribute(step_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
     const uint32_t tp = train_tile_pairs(d);
@@ -877,14 +907,12 @@ int train_projection_dev(const float* Y32, const uint8_t* bad, uint64_t n, uint3
             if (cursor + B > M) cursor = 0;
             PairBatch pb{V.p + cursor * d, tgt.p + cursor};
             cursor += B;
-            step_fn<<<grid, TRAIN_THREADS, shm, s>>>(P.p, k, d, pb, B, G.p, loss.p + t_step);
-            EJ_CUDA(cudaGetLastError());
             const float c1 = 1.0f - powf(b1, (float)(t_step + 1));
             const float c2 = 1.0f - powf(b2, (float)(t_step + 1));
-            adam_renorm_kernel<<<1, 256, ashm, s>>>(P.p, G.p, m1.p, m2.p, k, d, lr, b1, b2, c1, c2, 1,
-                                                 nullptr);
+            const AdamArgs ad{m1.p, m2.p, lr, b1, b2, c1, c2, done.p};
+            step_fn<<<grid, TRAIN_THREADS, shm, s>>>(P.p, k, d, pb, B, ad, G.p, loss.p + t_step);
             EJ_CUDA(cudaGetLastError());
-            note_launch(2);
+            note_launch();
         }
     }
     out.P.resize(nel);
@@ -936,7 +964,7 @@ extern "C" int ejoin_testing_projection_grad(const float* V, const float* tgt, u
     auto fn = k <= 8 ? train_step_kernel<8> : train_step_kernel<16>;
     EJ_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
     PairBatch pb{dV.p, dT.p};
-    fn<<<64, TRAIN_THREADS, shm, s>>>(dP.p, k, d, pb, M, dG.p, dL.p);
+    fn<<<64, TRAIN_THREADS, shm, s>>>(dP.p, k, d, pb, M, AdamArgs{}, dG.p, dL.p);
     EJ_CUDA(cudaGetLastError());
     std::vector<unsigned long long> g((size_t)k * d);
     unsigned long long l = 0;
