@@ -33,10 +33,13 @@
 //        otherwise       band: queued for the FP64 recheck
 //    W_iJ = beta_i + max beta over tile J >= beta_i + beta_j (one value per
 //    row and column tile, so the test costs the same as a tile-wide width).
-//  * The epilogue packs sign bits with one funnel shift per element, counts
-//    rows with popc, transposes 32x32 bit blocks across the warp to count
-//    columns (off-diagonal tiles credit both points), and a flusher warp adds
-//    the per-block counts to global memory.  No distance reaches global memory.
+//  * Each epilogue warp reads its two 32x32 chunks one after the other with
+//    tcgen05.ld.red (the load also returns each lane's maximum, which decides
+//    the all-out fast path), packs sign bits with one funnel shift per
+//    element, counts rows with popc, transposes 32x32 bit blocks across the
+//    warp to count columns (off-diagonal tiles credit both points), and a
+//    flusher warp adds the per-block counts to global memory.  No distance
+//    reaches global memory.
 //
 // Every wait is bounded (umma_ptx.cuh); on expiry all roles stop, in-flight
 // copies and MMAs are drained (bounded) and tensor memory is freed.
