@@ -78,7 +78,8 @@ __global__ void __launch_bounds__(PJ_ROWS) project_kernel(
     // of 16-byte row reads covers all banks once); P transposed [c][a], so
     // each column's K weights are 16-byte broadcast loads
     constexpr uint32_t PITCH = PJ_CH + 4;
-    __shared__ __align__(16) float sY[PJ_ROWS * PITCH];
+    extern __shared__ float4 pj_dyn[];  // two row tiles of PJ_ROWS x PITCH floats
+    float* sY = reinterpret_cast<float*>(pj_dyn);
     __shared__ __align__(16) float sP[PJ_CH * K];
     __shared__ unsigned int smn[4][K], smx[4][K];
     const uint32_t t = threadIdx.x, lane = t & 31, w = t >> 5;
@@ -92,7 +93,87 @@ __global__ void __launch_bounds__(PJ_ROWS) project_kernel(
         lo[a] = 0xffffffffu;
         hi[a] = 0u;
     }
-    for (uint64_t i0 = blockIdx.x * (uint64_t)PJ_ROWS; i0 < n; i0 += (uint64_t)gridDim.x * PJ_ROWS) {
+    // one row of outputs (and the box bounds) from the accumulated projection
+    auto finish_row = [&](uint64_t i, const float (&acc)[K], float s2) {
+        if (i >= n) return;
+        if (bad[i]) {
+            for (uint32_t a = 0; a < k; ++a) proj[i * k + a] = NaNf;
+            if (err) err[i] = NaNf;
+            return;
+        }
+#pragma unroll
+        for (int a = 0; a < K; ++a)
+            if (a < (int)k) {
+                proj[i * k + a] = acc[a];
+                const uint32_t b = ordered_bits32(acc[a]);
+                lo[a] = min(lo[a], b);
+                hi[a] = max(hi[a], b);
+            }
+        if (err) {
+            const float inner = __fmaf_ru(c1, __fsqrt_ru(s2), Yerr[i]);
+            err[i] = __fmaf_ru(pmax, inner, (float)d * 3.5873240686715317e-43f);
+        }
+    };
+    const uint64_t stride = (uint64_t)gridDim.x * PJ_ROWS;
+    if (vec4 && d <= PJ_CH) {
+        // rows of at most PJ_CH coordinates: P staged once, row tiles double
+        // buffered with cp.async (the next tile's copies run while this one is
+        // projected; no registers hold them).  Same arithmetic order as below.
+        for (uint32_t e = t; e < K * PJ_CH; e += PJ_ROWS) {
+            const uint32_t c = e / K, a = e % K;
+            sP[e] = (a < k && c < d) ? P[a * d + c] : 0.0f;
+        }
+        auto issue = [&](uint64_t i0b, float* dst) {
+            for (uint32_t e4 = t; e4 < PJ_ROWS * PJ_CH / 4; e4 += PJ_ROWS) {
+                const uint32_t r = e4 / (PJ_CH / 4), c = (e4 % (PJ_CH / 4)) * 4;
+                float* q = dst + r * PITCH + c;
+                if (i0b + r < n && c < d) {
+                    const uint32_t sa = (uint32_t)__cvta_generic_to_shared(q);
+                    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa),
+                                 "l"(Y32 + (i0b + r) * d + c));
+                } else {
+                    *reinterpret_cast<float4*>(q) = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                }
+            }
+            asm volatile("cp.async.commit_group;\n" ::);
+        };
+        uint32_t buf = 0;
+        uint64_t i0 = blockIdx.x * (uint64_t)PJ_ROWS;
+        if (i0 < n) issue(i0, sY);
+        for (; i0 < n; i0 += stride, buf ^= 1u) {
+            const bool more = i0 + stride < n;
+            if (more) issue(i0 + stride, sY + (buf ^ 1u) * PJ_ROWS * PITCH);
+            if (more) asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+            else asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+            __syncthreads();
+            const float* y = sY + buf * PJ_ROWS * PITCH + t * PITCH;
+            float acc[K];
+#pragma unroll
+            for (int a = 0; a < K; ++a) acc[a] = 0.0f;
+            float s2 = 0.0f;
+#pragma unroll 2
+            for (uint32_t c = 0; c < d; c += 4) {
+                const float4 y4 = *reinterpret_cast<const float4*>(y + c);
+                const float yv[4] = {y4.x, y4.y, y4.z, y4.w};
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    s2 = __fmaf_ru(yv[u], yv[u], s2);
+                    const float4* pp = reinterpret_cast<const float4*>(sP + (c + u) * K);
+#pragma unroll
+                    for (int a4 = 0; a4 < K / 4; ++a4) {
+                        const float4 wv = pp[a4];
+                        acc[4 * a4 + 0] = fmaf(wv.x, yv[u], acc[4 * a4 + 0]);
+                        acc[4 * a4 + 1] = fmaf(wv.y, yv[u], acc[4 * a4 + 1]);
+                        acc[4 * a4 + 2] = fmaf(wv.z, yv[u], acc[4 * a4 + 2]);
+                        acc[4 * a4 + 3] = fmaf(wv.w, yv[u], acc[4 * a4 + 3]);
+                    }
+                }
+            }
+            finish_row(i0 + t, acc, s2);
+            __syncthreads();  // this buffer is refilled two tiles later
+        }
+    } else
+    for (uint64_t i0 = blockIdx.x * (uint64_t)PJ_ROWS; i0 < n; i0 += stride) {
         const uint64_t i = i0 + t;
         float acc[K];
 #pragma unroll
@@ -143,25 +224,7 @@ __global__ void __launch_bounds__(PJ_ROWS) project_kernel(
                 }
             }
         }
-        if (i < n) {
-            if (bad[i]) {
-                for (uint32_t a = 0; a < k; ++a) proj[i * k + a] = NaNf;
-                if (err) err[i] = NaNf;
-            } else {
-#pragma unroll
-                for (int a = 0; a < K; ++a)
-                    if (a < (int)k) {
-                        proj[i * k + a] = acc[a];
-                        const uint32_t b = ordered_bits32(acc[a]);
-                        lo[a] = min(lo[a], b);
-                        hi[a] = max(hi[a], b);
-                    }
-                if (err) {
-                    const float inner = __fmaf_ru(c1, __fsqrt_ru(s2), Yerr[i]);
-                    err[i] = __fmaf_ru(pmax, inner, (float)d * 3.5873240686715317e-43f);
-                }
-            }
-        }
+        finish_row(i, acc, s2);
     }
 #pragma unroll
     for (int a = 0; a < K; ++a)
@@ -782,12 +845,14 @@ int learned_order(const float* Y32, const float* Yerr, const uint8_t* bad, uint6
         EJ_CUDA(cudaGetDevice(&dev));
         EJ_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
         auto fn = k <= 8 ? project_kernel<8> : project_kernel<16>;
+        const size_t dsm = 2 * (size_t)PJ_ROWS * (PJ_CH + 4) * sizeof(float);  // two row tiles
+        EJ_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm));
         int per_sm = 0;
-        EJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, PJ_ROWS, 0));
+        EJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, PJ_ROWS, dsm));
         const uint64_t tiles = (n + PJ_ROWS - 1) / PJ_ROWS;
         const unsigned grid = (unsigned)std::max<uint64_t>(
             1, std::min<uint64_t>(tiles, (uint64_t)sms * std::max(per_sm, 1)));
-        fn<<<grid, PJ_ROWS, 0, s>>>(Y32, boxes ? Yerr : nullptr, bad, n, d, P_dev, k, pmax, proj.p,
+        fn<<<grid, PJ_ROWS, dsm, s>>>(Y32, boxes ? Yerr : nullptr, bad, n, d, P_dev, k, pmax, proj.p,
                                     boxes ? err.p : nullptr, rng.p, rng.p + k);
         EJ_CUDA(cudaGetLastError());
         note_launch();
