@@ -46,7 +46,7 @@ extern "C" {
  * INPUT_DATA_PREC / COMPUTE_PREC / ACCUM_PREC, params.h:10-12 and
  * params.h:175-203; here it is a runtime option). */
 typedef enum ejoin_precision {
-    EJOIN_FP64_DIRECT = 0, /* CUDA-core direct differences: the exact judge
+    EJOIN_FP64_DIRECT = 0, /* CUDA-core direct differences: the exact arbiter
                               (reference searchMode 1, kernel_join.cu:168-200) */
     EJOIN_FP64_DMMA = 1,   /* FP64 DMMA Gram tiles + FP64 band recheck
                               (reference kernel_join.cu:530-677 re-designed) */

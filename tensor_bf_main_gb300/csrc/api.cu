@@ -7,7 +7,7 @@
 // device memory and exiting on an unknown mode.  Here the driver
 //   1. places the points in device memory (host or device input),
 //   2. runs the chosen exact pipeline:
-//        FP64_DIRECT  exact FP64 tiles (the judge)
+//        FP64_DIRECT  exact FP64 tiles (the arbiter)
 //        FP64_DMMA    FP64 Gram screen + band recheck
 //        BF16/FP16    centre, scale, pack; tcgen05 Gram screen + band recheck
 //      optionally behind the learned tile-pair pruning (k_learn.cu),
@@ -275,7 +275,7 @@ static int run_direct(Join& J) {
 }
 
 static int run_dmma(Join& J) {
-    // pair emission runs on the exact judge (the DMMA epilogue only counts)
+    // pair emission runs on the exact arbiter (the DMMA epilogue only counts)
     if (J.em) return run_direct(J);
     EventTimer tp, tg, tr;
     tp.start(J.s);
@@ -634,7 +634,7 @@ static int self_join_impl(const double* points, uint64_t n, uint32_t d, double e
     };
     StageCopy sc{};
     if (run) {
-        if (isinf(T)) prec = EJOIN_FP64_DIRECT;  // every non-NaN pair counts: judge only
+        if (isinf(T)) prec = EJOIN_FP64_DIRECT;  // every non-NaN pair counts: arbiter only
         // the 16-bit screens start with the centring pass, which takes over
         // the host-to-device copy of pinned input
         const bool screen16 = prec == EJOIN_FP16 || prec == EJOIN_BF16 ||
@@ -822,7 +822,7 @@ int ejoin_query_counts(const double* points, uint64_t n, uint32_t d, double eps,
 // Join of two point sets on the tensor-core screen: queries are the A side
 // (rows, counted), points the B side; both centred with the points' mean and
 // packed with one scale.  Data outside the FP32 path's range, FP64 modes and
-// eps = inf take the exact FP64 judge.
+// eps = inf take the exact FP64 arbiter.
 static int cross_join(Join& J, const double* Xq, uint64_t nq, int prec, int32_t* qcounts) {
     const bool fp64 = prec == EJOIN_FP64_DIRECT || prec == EJOIN_FP64_DMMA || isinf(J.T);
     if (!fp64) {

@@ -3,7 +3,7 @@
 // Same positional arguments as the reference's main (main.cu:17-26, ids in
 // params.h:160-171):
 //     ejoin_main <dataset> <epsilon> <searchMode> [device] [--dim D] [--binary] [--precision P]
-// searchMode 1/2 = exact FP64 judge, 3/4 = exact tensor-core join, 5 = with
+// searchMode 1/2 = exact FP64 arbiter, 3/4 = exact tensor-core join, 5 = with
 // learned pruning.  The reference fixed the dimension at compile time
 // (INPUT_DATA_DIM, params.h:4); here it is --dim (default: the number of
 // values on the first line of the file).  The result is appended to

@@ -123,7 +123,7 @@ struct BandRec {
 
 // Pair emission for neighbour lists (null when only counts are wanted):
 // in-records of the tensor-core screen and single pairs (band hits, direct
-// judge hits), appended through the counters cnt[0] / cnt[1]; entries beyond
+// arbiter hits), appended through the counters cnt[0] / cnt[1]; entries beyond
 // a capacity are dropped and detected by the caller from the counters.
 struct Emit {
     BandRec* inq;

@@ -1,6 +1,6 @@
 // k_direct.cu -- FP64 CUDA-core kernels with the reference's exact arithmetic.
 //
-//  * direct_selfjoin_kernel: the exact judge (EJOIN_FP64_DIRECT, reference
+//  * direct_selfjoin_kernel: the exact arbiter (EJOIN_FP64_DIRECT, reference
 //    searchMode 1, kernel_join.cu:168-200).  The reference runs one thread
 //    per query over all N candidates and bumps one global 64-bit counter per
 //    hit; here a CTA takes one 64x64 tile pair of the upper triangle (I <= J),

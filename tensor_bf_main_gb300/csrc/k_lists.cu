@@ -4,7 +4,7 @@
 // kernels (kernel_join.cu:139-162) are dead code.  Here the lists come from a
 // second pass of the same exact join that emits its neighbour pairs: the
 // tensor-core screen appends one in-record per row and 32-column chunk with
-// certain neighbours, the band recheck and the FP64 judge append single
+// certain neighbours, the band recheck and the FP64 arbiter append single
 // pairs.  Every neighbour pair is emitted exactly once (the screens visit
 // each unordered pair once; kBandBoth marks pairs that credit both points),
 // so the per-point counts of the counting pass give the CSR offsets, and a

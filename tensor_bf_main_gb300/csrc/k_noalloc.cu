@@ -135,7 +135,7 @@ int run(const double* X, uint64_t n, uint32_t d, double eps, cudaStream_t s, int
         return EJOIN_OK;
     }
     if (isinf(T)) {
-        // every non-NaN pair counts: the exact direct judge needs no scratch
+        // every non-NaN pair counts: the exact direct arbiter needs no scratch
         EJ_TRY(launch_direct_selfjoin(X, n, d, T, counts, nullptr, s));
     } else {
         na_rowflags_kernel<<<(unsigned)((n * 32 + 255) / 256), 256, 0, s>>>(X, n, d, bad);
