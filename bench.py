@@ -173,6 +173,64 @@ def peaks():
         return None
 
 
+def gram_roofline(stats, d, prec, pk, args, proj_k):
+    """Roofline of the dominant kernel, the tcgen05 Gram screen.
+
+    achieved = MMA flops of the data products over the 128 x 128 tile pairs
+    that the screen actually needs (the active halves, `tile_pairs_run`: upper
+    triangle, not pruned), x3 with the hi+lo split (hi*hi, hi*lo, lo*hi), the
+    16-wide aug product excluded; divided by the kernel's CUDA-event time
+    (`ms_gram`, event pair on the launching stream around the one launch).
+    peak = the burst dense BF16 rate of MEASURED_PEAKS.json (the kernel runs
+    for milliseconds inside a step of about 25 ms, under the burst clock);
+    FP8 operands run kind::f8f6f4 at twice the BF16 rate, so their peak is 2x
+    that figure.  Two more fractions against the same peak:
+      frac_executed  every MMA the kernel issued: all 128 x 256 blocks
+                     (`gram_blocks`, both halves, inactive ones included),
+                     aug products included;
+      frac_useful    the hi*hi products of the active halves only (the part
+                     of the split that decides the answer alone).
+    l2_operand_bytes: bytes the TMA engine moves from L2 into shared memory
+    per launch (per block: the A slab of 128 rows and the B slab of 256 rows
+    of every K step, plus the 128 + 256 aug rows of 32 bytes).
+    """
+    gram_ms = statistics.mean(s["ms_gram"] for s in stats)
+    t = gram_ms / 1e3
+    fp8 = prec == "fp8_e4m3"
+    split = prec == "bf16_split"
+    dp = -(-d // (128 if fp8 else 64)) * (128 if fp8 else 64)
+    tiles = statistics.mean(s["tile_pairs_run"] for s in stats)
+    blocks = statistics.mean(s["gram_blocks"] for s in stats)
+    kdata = (3 if split else 1) * dp
+    f_needed = tiles * 2.0 * 128 * 128 * kdata
+    f_useful = tiles * 2.0 * 128 * 128 * dp
+    f_exec = blocks * 2.0 * 128 * 256 * (kdata + 16)
+    burst = (pk or {}).get("bf16_tflops")
+    peak = (burst or 1900.0) * (2.0 if fp8 else 1.0)
+    src = ("MEASURED_PEAKS.json bf16_tflops (burst)" if burst else "fallback 1.9 PFLOP/s") + \
+          (" x2 (FP8 kind::f8f6f4)" if fp8 else "")
+    achieved = f_needed / t / 1e12
+    elem = 1 if fp8 else 2
+    steps = (dp * elem // 128) * (2 if split else 1)  # K slabs of 128-byte rows
+    l2_bytes = blocks * (steps * (128 + 256) * 128 + (128 + 256) * 32)
+    traffic = None
+    try:
+        prof = json.load(open(PROFILE_SUMMARY))
+        key = f"{args.config}:{prec}:k{proj_k}"
+        if key in prof:
+            traffic = prof[key]["traffic_bytes_per_launch"]
+    except (OSError, ValueError, KeyError):
+        pass
+    return {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+            "frac": achieved / peak, "traffic": traffic, "peak_source": src,
+            "kernel": "gram_kernel (tcgen05)",
+            "flops_per_launch": f_needed, "ms_per_launch": gram_ms,
+            "frac_executed": f_exec / t / 1e12 / peak, "flops_executed_per_launch": f_exec,
+            "frac_useful": f_useful / t / 1e12 / peak,
+            "active_tile_pairs": tiles, "blocks": blocks,
+            "l2_operand_bytes": l2_bytes, "l2_operand_gbs": l2_bytes / t / 1e9}
+
+
 def run_reference(args):
     world, rank, _ = dist_env()
     if rank != 0:
@@ -255,31 +313,10 @@ def run_ours(args):
     ck = clocks.stop()
     ms, value = replica_rate(e0.elapsed_time(e1) / args.steps, n, world, dist, dev)
 
-    # roofline of the dominant kernel (the Gram screen): executed MMA flops per
-    # launch over its CUDA-event duration, against the measured sustained
-    # dense BF16 rate (the kernel runs inside a long step)
     pk = peaks()
-    gram_ms = statistics.mean(s["ms_gram"] for s in stats)
-    gram_flops = statistics.mean(s["gram_flops"] for s in stats)
-    achieved = gram_flops / (gram_ms / 1e3) / 1e12
     prec = stats[0]["precision"]
-    if prec in ("fp64_dmma", "fp64_direct"):
-        roof = None
-    else:
-        peak = (pk or {}).get("bf16_tflops_sustained") or 1700.0
-        traffic = None
-        try:
-            prof = json.load(open(PROFILE_SUMMARY))
-            key = f"{args.config}:{prec}:k{proj_k}"
-            if key in prof:
-                traffic = prof[key]["traffic_bytes_per_launch"]
-        except (OSError, ValueError, KeyError):
-            pass
-        roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                "frac": achieved / peak, "traffic": traffic,
-                "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained" if pk else "fallback",
-                "kernel": "gram_kernel (tcgen05)", "flops_per_launch": gram_flops,
-                "ms_per_launch": gram_ms}
+    roof = None if prec in ("fp64_dmma", "fp64_direct") else gram_roofline(stats, d, prec, pk,
+                                                                         args, proj_k)
 
     line = {
         "metric": "pair-distances/s at FP64-exact counts", "value": value, "unit": "pairs/s",

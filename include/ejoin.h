@@ -54,7 +54,7 @@ typedef enum ejoin_precision {
     EJOIN_BF16 = 3,        /* tcgen05 kind::f16, BF16 operands, FP32 accumulate */
     EJOIN_BF16_SPLIT = 4,  /* BF16 hi+lo split products (hi*hi + hi*lo + lo*hi) */
     EJOIN_FP8_E4M3 = 5,    /* tcgen05 kind::f8f6f4, E4M3 with per-row scales */
-    EJOIN_AUTO = 6         /* library picks (BF16_SPLIT for d <= 512, else FP8) */
+    EJOIN_AUTO = 6         /* library picks (FP16 for d <= 128, else BF16) */
 } ejoin_precision;
 
 /* Point ordering used by the learned pruning (proj_k > 0). */
@@ -85,6 +85,12 @@ typedef struct ejoin_options {
 } ejoin_options;
 
 #define EJOIN_FLAG_NO_RECHECK_STATS 0x1u /* reserved */
+/* Keep the device scratch cached in the library's memory pool after the call,
+ * so that repeated joins skip the cost of mapping fresh device memory.
+ * Without it every call returns its scratch to the device before it returns
+ * (the library never touches the device's default pool).  The cached memory
+ * is released by ejoin_release_scratch or at exit. */
+#define EJOIN_FLAG_KEEP_SCRATCH 0x2u
 
 typedef struct ejoin_stats {
     uint64_t n;
@@ -108,6 +114,7 @@ typedef struct ejoin_stats {
     /* reserved[0]: band pairs the FP32 pre-check left to the exact FP64 chain;
        reserved[1]: 128 x 256 blocks the tensor-core Gram kernel computed
        (each covers up to two of the tile_pairs_run 128 x 128 tile pairs);
+       reserved[2]: peak device scratch the call reserved (bytes);
        ejoin_train_projection: reserved[0] / [1] = first / last hinge loss. */
     double reserved[5];
 } ejoin_stats;
@@ -172,6 +179,11 @@ int ejoin_train_projection(const double* points, uint64_t n, uint32_t d, double 
  * (host arithmetic, rigorous). */
 int ejoin_certify_spectral_norm(const float* P, uint32_t k, uint32_t d, double* bound_out);
 
+/* Return the device scratch cached by calls made with EJOIN_FLAG_KEEP_SCRATCH
+ * on `device` to the device.  No reference counterpart (the reference never
+ * freed its device memory, gpu_join.cu:210-322). */
+int ejoin_release_scratch(int device);
+
 /* Largest double T with sqrt(T) <= eps: the join counts pairs with d2 <= T. */
 double ejoin_threshold(double eps);
 
@@ -222,8 +234,11 @@ int ejoin_gpu_join_main_brute_force(unsigned int searchMode, unsigned int device
  * static 32 MiB device array that every GPU loading the library holds until
  * exit.  Limits: n <= 16384, d <= 128 (else EJOIN_EINVAL); a boundary band
  * larger than the array's queue returns EJOIN_ENOMEM.  `points` (n x d,
- * contiguous) and `counts` (n int32) must be device memory; *total_out is
- * host memory (may be NULL); `stream` may be NULL.  The first call on a
+ * contiguous) and `counts` (n int32) must be device memory of `device` (or
+ * managed memory), else EJOIN_EINVAL before any launch; *total_out is host
+ * memory (may be NULL); `stream` may be NULL.  Every call waits for its own
+ * work on `stream` before returning (the status and total are read back to
+ * the host).  On a non-zero return the counts are zero.  The first call on a
  * device resolves the array's address and should come before any stream
  * capture on that device.  All calls share the array: calls that overlap on
  * the GPU race. */

@@ -25,6 +25,23 @@ int ejoin_testing_projection_grad(const float* V, const float* tgt, uint64_t M, 
  * *sigma_est_out receives the inflated estimate the kernel used. */
 int ejoin_testing_renormalise(float* P, uint32_t k, uint32_t d, float* sigma_est_out);
 
+/* Failure injection for the tests of the error paths.  The reference
+ * printed CUDA errors and carried on (utils.cu:7-13) or exited
+ * (gpu_join.cu:313-314, dataset.cu:16-20); here every failure returns a
+ * status, and these hooks make the failures happen on purpose, on the host
+ * side of the library, so that the tests can check the status, that every
+ * buffer is released and that the next call succeeds.
+ *   EJOIN_TESTING_FAIL_ALLOC    value = k: the k-th device allocation from
+ *                               now fails (EJOIN_ENOMEM); 0 cancels
+ *   EJOIN_TESTING_GRAM_TIMEOUT  value = ns: the next tensor-core screen runs
+ *                               with that wait deadline and a producer that
+ *                               never issues its first stage, so its bounded
+ *                               waits expire (EJOIN_ETIMEOUT); 0 cancels
+ * Process-wide; each injection is used once. */
+#define EJOIN_TESTING_FAIL_ALLOC 1
+#define EJOIN_TESTING_GRAM_TIMEOUT 2
+int ejoin_testing_inject(int what, uint64_t value);
+
 #ifdef __cplusplus
 }
 #endif

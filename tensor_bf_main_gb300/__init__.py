@@ -96,6 +96,7 @@ class Stats(ctypes.Structure):
         d["precision"] = Precision.NAMES.get(d["precision"], d["precision"])
         d["exact_rechecks"] = int(self.reserved[0])
         d["gram_blocks"] = int(self.reserved[1])
+        d["scratch_peak_bytes"] = int(self.reserved[2])
         return d
 
 
@@ -105,11 +106,17 @@ EXPORTED = [
     "ejoin_certify_spectral_norm", "ejoin_threshold", "ejoin_import_dataset",
     "ejoin_import_binary", "ejoin_free", "ejoin_last_error", "ejoin_version",
     "ejoin_gpu_join_main_brute_force", "ejoin_self_join_noalloc", "ejoin_neighbor_lists",
-    "ejoin_join_counts",
+    "ejoin_join_counts", "ejoin_release_scratch",
 ]
 
 # Test hooks declared in include/ejoin_testing.h.
-TESTING = ["ejoin_testing_projection_grad", "ejoin_testing_renormalise"]
+TESTING = ["ejoin_testing_projection_grad", "ejoin_testing_renormalise", "ejoin_testing_inject"]
+
+# option flags (include/ejoin.h)
+FLAG_KEEP_SCRATCH = 0x2
+# failure injection (include/ejoin_testing.h)
+TESTING_FAIL_ALLOC = 1
+TESTING_GRAM_TIMEOUT = 2
 
 _lib = None
 
@@ -148,6 +155,9 @@ def load_library(path: str = LIB_PATH):
     L.ejoin_testing_renormalise.argtypes = [vp, u32, u32, vp]
     L.ejoin_testing_renormalise.restype = ctypes.c_int
     L.ejoin_self_join_noalloc.argtypes = [vp, u64, u32, dbl, ctypes.c_int, vp, vp, ctypes.POINTER(u64)]
+    L.ejoin_release_scratch.argtypes = [ctypes.c_int]
+    L.ejoin_testing_inject.argtypes = [ctypes.c_int, u64]
+    L.ejoin_testing_inject.restype = ctypes.c_int
     for name in EXPORTED:
         if name not in ("ejoin_threshold", "ejoin_free"):
             getattr(L, name).restype = ctypes.c_int
@@ -165,7 +175,7 @@ def _check(rc: int):
 
 def _options(device=0, precision=Precision.AUTO, proj_k=0, ld=0, projection=None,
              train_pairs=1 << 20, train_steps=50, order=Order.MORTON, seed=0x5EED5EED,
-             stream=None, band_capacity=0, acc_bound_scale=1.0):
+             stream=None, band_capacity=0, acc_bound_scale=1.0, keep_scratch=False):
     o = Options()
     _check(load_library().ejoin_default_options(ctypes.byref(o)))
     o.device = int(device)
@@ -178,6 +188,8 @@ def _options(device=0, precision=Precision.AUTO, proj_k=0, ld=0, projection=None
     o.seed = int(seed)
     o.band_capacity = int(band_capacity)
     o.acc_bound_scale = float(acc_bound_scale)
+    if keep_scratch:
+        o.flags |= FLAG_KEEP_SCRATCH
     if projection is not None:
         p = np.ascontiguousarray(projection, dtype=np.float32)
         o._proj_keepalive = p
@@ -292,6 +304,16 @@ def train_projection(points, eps: float, k: int = 8, device: int = 0, **kw):
     info = st.as_dict()
     info["loss_first"], info["loss_last"] = st.reserved[0], st.reserved[1]
     return P, sig.value, info
+
+
+def release_scratch(device: int = 0) -> None:
+    """Return the scratch cached by keep_scratch=True calls to the device."""
+    _check(load_library().ejoin_release_scratch(int(device)))
+
+
+def testing_inject(what: int, value: int) -> None:
+    """Failure injection for the error-path tests (include/ejoin_testing.h)."""
+    _check(load_library().ejoin_testing_inject(int(what), int(value)))
 
 
 def certify_spectral_norm(P) -> float:

@@ -21,9 +21,12 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
+#include <mutex>
 #include <vector>
 
 #include "ejoin_internal.cuh"
+#include "ejoin_testing.h"
 
 namespace ejoin {
 
@@ -55,6 +58,80 @@ void clear_error() {
     t_status = 0;
     t_msg[0] = 0;
 }
+
+// ------------------------------------------------------- scratch pool --
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_pool_mu;
+cudaMemPool_t g_pools[kMaxDevices] = {};
+thread_local cudaMemPool_t t_pool = nullptr;
+std::atomic<uint64_t> g_fail_at{0};
+std::atomic<uint64_t> g_gram_timeout{0};
+
+// The library's pool on device dev: device-local memory, freed blocks kept
+// for the rest of a call (release threshold: unlimited; CallScope trims it).
+int library_pool(int dev, cudaMemPool_t* out) {
+    if (dev < 0 || dev >= kMaxDevices) return set_error(EJOIN_EINVAL, "device ordinal %d unsupported", dev);
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    if (!g_pools[dev]) {
+        cudaMemPoolProps props;
+        memset(&props, 0, sizeof props);
+        props.allocType = cudaMemAllocationTypePinned;
+        props.handleTypes = cudaMemHandleTypeNone;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = dev;
+        cudaMemPool_t p = nullptr;
+        EJ_CUDA(cudaMemPoolCreate(&p, &props));
+        uint64_t thr = UINT64_MAX;
+        EJ_CUDA(cudaMemPoolSetAttribute(p, cudaMemPoolAttrReleaseThreshold, &thr));
+        g_pools[dev] = p;
+    }
+    *out = g_pools[dev];
+    return EJOIN_OK;
+}
+}  // namespace
+
+cudaMemPool_t current_pool() { return t_pool; }
+
+int CallScope::enter(int dev, cudaStream_t stream, bool keep_scratch) {
+    EJ_TRY(library_pool(dev, &pool));
+    prev = t_pool;
+    t_pool = pool;
+    s = stream;
+    keep = keep_scratch;
+    uint64_t zero = 0;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReservedMemHigh, &zero);
+    return EJOIN_OK;
+}
+
+uint64_t CallScope::peak_reserved() const {
+    uint64_t v = 0;
+    if (pool) cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemHigh, &v);
+    return v;
+}
+
+CallScope::~CallScope() {
+    if (!pool) return;
+    // every buffer of the call was freed on s (stream order) before this
+    // runs; once s is idle the pool holds no live allocation of this call
+    if (cudaStreamSynchronize(s) != cudaSuccess) cudaGetLastError();
+    if (!keep) cudaMemPoolTrimTo(pool, 0);
+    t_pool = prev;
+}
+
+void inject_alloc_failure(uint64_t k) { g_fail_at.store(k); }
+
+bool alloc_should_fail() {
+    uint64_t v = g_fail_at.load();
+    while (v) {
+        if (g_fail_at.compare_exchange_weak(v, v - 1)) return v == 1;
+    }
+    return false;
+}
+
+void inject_gram_timeout(uint64_t ns) { g_gram_timeout.store(ns); }
+uint64_t take_gram_timeout() { return g_gram_timeout.exchange(0); }
 
 // ---------------------------------------------------------- threshold --
 
@@ -123,16 +200,6 @@ static int check_device(int dev, int* sms) {
                          "device %d is sm_%d%d; libejoin.so is built for sm_103a (GB300) only", dev,
                          p.major, p.minor);
     *sms = p.multiProcessorCount;
-    static bool pool_done[64] = {};
-    if (dev < 64 && !pool_done[dev]) {
-        cudaMemPool_t pool;
-        if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
-            uint64_t thr = UINT64_MAX;
-            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
-        }
-        cudaGetLastError();
-        pool_done[dev] = true;
-    }
     return EJOIN_OK;
 }
 
@@ -228,6 +295,13 @@ static int screen_and_recheck(Join& J, uint64_t cap0, Screen&& screen, Recheck&&
     for (int attempt = 0;; ++attempt) {
         EJ_TRY(band.alloc(cap, J.s, "band queue"));
         EJ_TRY(dst.zero(J.s));
+        if (const uint64_t ns = unit == 2 ? take_gram_timeout() : 0) {
+            // test hook: short deadline, producer withholds its first stage
+            const uint32_t one = 1;
+            EJ_CUDA(cudaMemcpyAsync(&dst.p->wait_ns, &ns, sizeof ns, cudaMemcpyHostToDevice, J.s));
+            EJ_CUDA(cudaMemcpyAsync(&dst.p->withhold, &one, sizeof one, cudaMemcpyHostToDevice, J.s));
+            EJ_CUDA(cudaStreamSynchronize(J.s));
+        }
         EJ_CUDA(cudaMemsetAsync(J.counts, 0, n_pad * sizeof(int32_t), J.s));
         tg.start(J.s);
         EJ_TRY(screen(band.p, cap / unit, dst.p));
@@ -541,10 +615,35 @@ static int run_screen16(Join& J, Fmt fmt, bool split, Learned& L) {
         return launch_band_recheck2(J.X, J.n, J.d, J.perm, J.T, R, pairs.p, npairs, J.counts, st,
                                     J.em, J.s);
     };
-    // generous first queue (capped at a quarter of free memory by
-    // band_budget): an overflow re-runs the whole screen
-    const uint64_t cap0 = std::max<uint64_t>(1u << 22, 512 * J.n);
-    return screen_and_recheck(J, cap0, screen, recheck, n_pad, tg, tr, 2);
+    // First queue: sized from a systematic sample of the blocks (every 64th,
+    // counting records only) when the list could produce more records than
+    // the minimum queue; an overflow re-runs the whole screen with the exact
+    // size.  (A block produces at most 128 rows x 8 chunks = 1024 records.)
+    uint64_t cap_rec = 1u << 22;
+    if (!J.opt.band_capacity && nwork * 1024 > cap_rec) {
+        EventTimer te;
+        te.start(J.s);
+        DBuf<uint2> sw;
+        DBuf<DevStatus> est;
+        uint64_t ns = 0;
+        const uint64_t stride = 64;
+        EJ_TRY(sample_worklist(work.p, nwork, stride, sw, &ns, J.s));
+        EJ_TRY(est.alloc(1, J.s, "band estimate"));
+        EJ_TRY(est.zero(J.s));
+        const GramSide gs{Qp, side.Aug.p, n_pad};
+        EJ_TRY(launch_gram16(gs, gs, P, sw.p, ns, side.tmax.p, side.beta.p, side.tsig.p,
+                             side.sig.p, false, J.counts, nullptr, 0, est.p, nullptr, J.sms, J.s));
+        DevStatus h;
+        EJ_CUDA(cudaMemcpyAsync(&h, est.p, sizeof h, cudaMemcpyDeviceToHost, J.s));
+        EJ_CUDA(cudaStreamSynchronize(J.s));
+        te.stop(J.s);
+        J.st->ms_order += te.ms();
+        if (h.timeout)
+            return set_error(EJOIN_ETIMEOUT, "Gram kernel: a bounded device wait expired (site %u)", h.where);
+        const double scaled = (double)h.band_count * (double)nwork / (double)std::max<uint64_t>(ns, 1);
+        cap_rec = std::max<uint64_t>(cap_rec, (uint64_t)(1.3 * scaled) + (1u << 20));
+    }
+    return screen_and_recheck(J, 2 * cap_rec, screen, recheck, n_pad, tg, tr, 2);
 }
 
 // AUTO (measured on GB300 over the benchmark shapes): FP16's 11-bit
@@ -595,6 +694,8 @@ static int self_join_impl(const double* points, uint64_t n, uint32_t d, double e
     EJ_TRY(check_device(opt.device, &sms));
     EJ_TRY(ds.enter(opt.device));
     cudaStream_t s = opt.stream ? (cudaStream_t)opt.stream : cudaStreamPerThread;
+    CallScope scope;  // before every device buffer of the call
+    EJ_TRY(scope.enter(opt.device, s, (opt.flags & EJOIN_FLAG_KEEP_SCRATCH) != 0));
     const bool out_dev = is_device_ptr(counts_out);
     const double T = threshold(eps);
     const uint64_t launches0 = launches_so_far();
@@ -730,6 +831,7 @@ static int self_join_impl(const double* points, uint64_t n, uint32_t d, double e
     EJ_CUDA(cudaStreamSynchronize(s));
     stats.ms_total = tt.ms();
     stats.kernel_launches = launches_so_far() - launches0;
+    stats.reserved[2] = (double)scope.peak_reserved();
     const double computed = (double)n * (double)n;
     stats.band_fraction = computed > 0 ? (double)stats.band_pairs / computed : 0.0;
     if (total_out) *total_out = total;
@@ -794,6 +896,8 @@ int ejoin_query_counts(const double* points, uint64_t n, uint32_t d, double eps,
     EJ_TRY(check_device(opt.device, &sms));
     EJ_TRY(ds.enter(opt.device));
     cudaStream_t s = opt.stream ? (cudaStream_t)opt.stream : cudaStreamPerThread;
+    CallScope scope;  // before every device buffer of the call
+    EJ_TRY(scope.enter(opt.device, s, (opt.flags & EJOIN_FLAG_KEEP_SCRATCH) != 0));
     const double T = threshold(eps);
     const bool out_dev = is_device_ptr(counts_out);
     DBuf<double> xbuf;
@@ -896,7 +1000,7 @@ static int cross_join(Join& J, const double* Xq, uint64_t nq, int prec, int32_t*
                 return launch_band_recheck2(Xq, nq, J.d, nullptr, J.T, R, pairs.p, npairs, qcounts,
                                             st, nullptr, J.s);
             };
-            const uint64_t cap0 = std::max<uint64_t>(1u << 22, 256 * (nq + J.n));
+            const uint64_t cap0 = std::max<uint64_t>(1u << 22, 16 * (nq + J.n));
             return screen_and_recheck(Jq, cap0, screen, recheck, npq, tg, tr, 2);
         }
     }
@@ -940,6 +1044,8 @@ int ejoin_join_counts(const double* queries, uint64_t nq, const double* points, 
     EJ_TRY(check_device(opt.device, &sms));
     EJ_TRY(ds.enter(opt.device));
     cudaStream_t s = opt.stream ? (cudaStream_t)opt.stream : cudaStreamPerThread;
+    CallScope scope;  // before every device buffer of the call
+    EJ_TRY(scope.enter(opt.device, s, (opt.flags & EJOIN_FLAG_KEEP_SCRATCH) != 0));
     const double T = threshold(eps);
     const uint64_t launches0 = launches_so_far();
     EventTimer tt;
@@ -981,6 +1087,7 @@ int ejoin_join_counts(const double* queries, uint64_t nq, const double* points, 
     EJ_CUDA(cudaStreamSynchronize(s));
     stats.ms_total = tt.ms();
     stats.kernel_launches = launches_so_far() - launches0;
+    stats.reserved[2] = (double)scope.peak_reserved();
     const double computed = (double)n * (double)nq;
     stats.band_fraction = computed > 0 ? (double)stats.band_pairs / computed : 0.0;
     if (total_out) *total_out = total;
@@ -1008,6 +1115,8 @@ int ejoin_train_projection(const double* points, uint64_t n, uint32_t d, double 
     EJ_TRY(check_device(opt.device, &sms));
     EJ_TRY(ds.enter(opt.device));
     cudaStream_t s = opt.stream ? (cudaStream_t)opt.stream : cudaStreamPerThread;
+    CallScope scope;  // before every device buffer of the call
+    EJ_TRY(scope.enter(opt.device, s, (opt.flags & EJOIN_FLAG_KEEP_SCRATCH) != 0));
     DBuf<double> xbuf;
     const double* X = nullptr;
     EJ_TRY(stage_points(points, n, d, ld, xbuf, &X, s));
@@ -1037,6 +1146,27 @@ int ejoin_train_projection(const double* points, uint64_t n, uint32_t d, double 
         stats_out->reserved[1] = tr.loss_last;
     }
     return EJOIN_OK;
+}
+
+int ejoin_release_scratch(int device) {
+    clear_error();
+    if (device < 0 || device >= kMaxDevices) return set_error(EJOIN_EINVAL, "device %d out of range", device);
+    cudaMemPool_t p = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(g_pool_mu);
+        p = g_pools[device];
+    }
+    if (p) EJ_CUDA(cudaMemPoolTrimTo(p, 0));
+    return EJOIN_OK;
+}
+
+int ejoin_testing_inject(int what, uint64_t value) {
+    clear_error();
+    switch (what) {
+        case EJOIN_TESTING_FAIL_ALLOC: inject_alloc_failure(value); return EJOIN_OK;
+        case EJOIN_TESTING_GRAM_TIMEOUT: inject_gram_timeout(value); return EJOIN_OK;
+        default: return set_error(EJOIN_EINVAL, "unknown injection %d", what);
+    }
 }
 
 double ejoin_threshold(double eps) { return threshold(eps); }

@@ -117,9 +117,28 @@ int main(int argc, char** argv) {
     std::cout << "[Main | Result] ~ Time to join: " << timeJoin << '\n';
     std::cout << "[Main | Result] ~ Total result set size: " << total << '\n';
 
-    // CSV line of the reference (main.cu:115-127); compute dim / block / warps
-    // / precision columns describe the run actually made
+    // CSV line of the reference (main.cu:115-127).  The reference wrote its
+    // compile-time COMPUTE_DIM, BLOCKSIZE, WARP_PER_BLOCK and precisions; here
+    // the columns describe the main kernel of the mode actually run (the
+    // library reports it in st.precision):
+    //   FP64 direct   d coordinates, 256-thread blocks (8 warps)
+    //   FP64 DMMA     d padded to 32, 128-thread CTAs (4 warps)
+    //   16-bit Gram   d padded to 64, 608-thread CTAs (19 warps)
+    //   FP8 Gram      d padded to 128, 608-thread CTAs (19 warps)
     const char* precs[] = {"64", "64", "16", "16", "16", "8", "16"};
+    const int pm = st.precision >= 0 && st.precision <= 6 ? st.precision : 6;
+    unsigned computeDim = (dim + 63) / 64 * 64, blockSize = 608, warps = 19;
+    if (pm == EJOIN_FP64_DIRECT) {
+        computeDim = dim;
+        blockSize = 256;
+        warps = 8;
+    } else if (pm == EJOIN_FP64_DMMA) {
+        computeDim = (dim + 31) / 32 * 32;
+        blockSize = 128;
+        warps = 4;
+    } else if (pm == EJOIN_FP8_E4M3) {
+        computeDim = (dim + 127) / 128 * 128;
+    }
     std::ofstream out;
     std::ifstream in("tensor_brute-force.txt");
     const bool empty = !in.good() || in.peek() == std::ifstream::traits_type::eof();
@@ -127,10 +146,8 @@ int main(int argc, char** argv) {
     if (empty)
         out << "Dataset, epsilon, searchMode, executionTime, totalNeighbors, inputDim, computeDim, "
                "blockSize, warpPerBlock, computePrec, accumPrec\n";
-    const unsigned computeDim = (dim + 63) / 64 * 64;
     out << filename << ", " << epsilon << ", " << searchMode << ", " << timeJoin << ", " << total
-        << ", " << dim << ", " << computeDim << ", " << 608 << ", " << 19 << ", "
-        << precs[st.precision >= 0 && st.precision <= 6 ? st.precision : 6] << ", "
-        << (st.precision <= 1 ? 64 : 32) << std::endl;
+        << ", " << dim << ", " << computeDim << ", " << blockSize << ", " << warps << ", "
+        << precs[pm] << ", " << (pm <= 1 ? 64 : 32) << std::endl;
     return 0;
 }

@@ -38,9 +38,31 @@ void clear_error();
 
 // ------------------------------------------------------- device buffers --
 
-// Stream-ordered device allocation from the device's default memory pool
-// (the pool keeps freed blocks cached, so repeated joins do not pay for
-// cudaMalloc).  Freed on the same stream when the buffer goes out of scope.
+// Device scratch comes from a memory pool the library owns, one per device
+// (never the device's default pool, which belongs to the host program).
+// CallScope, constructed by every entry point before its first buffer,
+// selects the pool for the calling thread; when the entry point returns (its
+// buffers freed, its stream synchronised) the pool gives its memory back to
+// the device unless the caller asked to keep it (EJOIN_FLAG_KEEP_SCRATCH).
+cudaMemPool_t current_pool();
+struct CallScope {
+    cudaMemPool_t pool = nullptr, prev = nullptr;
+    cudaStream_t s = nullptr;
+    bool keep = false;
+    // Selects the library pool of device dev for this thread (creating it
+    // on first use).
+    int enter(int dev, cudaStream_t stream, bool keep_scratch);
+    // Largest device memory the pool reserved since enter() (bytes).
+    uint64_t peak_reserved() const;
+    ~CallScope();
+};
+// Test hook: make the k-th device allocation from now fail (0 = none).
+void inject_alloc_failure(uint64_t k);
+bool alloc_should_fail();
+
+// Stream-ordered device allocation from the library pool of the current
+// call (freed blocks stay cached in the pool for the rest of the call).
+// Freed on the same stream when the buffer goes out of scope.
 template <typename T>
 struct DBuf {
     T* p = nullptr;
@@ -60,7 +82,11 @@ struct DBuf {
         s = stream;
         count = n;
         if (n == 0) return EJOIN_OK;
-        cudaError_t e = cudaMallocAsync((void**)&p, n * sizeof(T), stream);
+        cudaMemPool_t pool = current_pool();
+        cudaError_t e = alloc_should_fail()
+                            ? cudaErrorMemoryAllocation
+                            : (pool ? cudaMallocFromPoolAsync((void**)&p, n * sizeof(T), pool, stream)
+                                    : cudaMallocAsync((void**)&p, n * sizeof(T), stream));
         if (e != cudaSuccess) {
             p = nullptr;
             cudaGetLastError();
@@ -148,7 +174,17 @@ struct DevStatus {
     unsigned long long band_pairs;  // pairs in those entries (record queues)
     unsigned long long band_hits;
     unsigned long long exact_rechecks;  // band pairs the FP32 pre-check left to FP64
+    // test hooks (zero in normal runs): the deadline of the bounded waits in
+    // ns (0 = the default), and, in the tensor-core Gram kernel, a producer
+    // that never issues the copies of its first stage
+    unsigned long long wait_ns;
+    unsigned int withhold;
+    unsigned int pad_;
 };
+// Test hook: the next tensor-core screen runs with wait deadline `ns` and a
+// producer that withholds its first stage (the waits then expire).
+void inject_gram_timeout(uint64_t ns);
+uint64_t take_gram_timeout();
 
 // Constants of the FP32 band pre-check (scaled space of the 16-bit screen).
 // Pairs (i, j) take row i from side A and row j from side B; for a self join
@@ -309,6 +345,9 @@ int build_worklist(uint64_t nT, uint64_t nTa, const LearnedBoxes* boxes, float t
 // nTb column tiles (with data; B padded to whole 256-row pairs).
 int build_worklist_cross(uint64_t nTa, uint64_t nTb, DBuf<uint2>& work, uint64_t* nwork_out,
                          uint64_t* ntiles_out, cudaStream_t s);
+// out = work[0], work[stride], work[2 stride], ... (*nsample_out entries).
+int sample_worklist(const uint2* work, uint64_t nwork, uint64_t stride, DBuf<uint2>& out,
+                    uint64_t* nsample_out, cudaStream_t s);
 int sum_counts(const int32_t* counts, uint64_t n, unsigned long long* dev_total, cudaStream_t s);
 int scatter_counts(const int32_t* src, const uint32_t* perm, uint64_t n, int32_t* dst,
                    cudaStream_t s);

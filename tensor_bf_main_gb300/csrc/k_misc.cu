@@ -252,6 +252,25 @@ int build_worklist_cross(uint64_t nTa, uint64_t nTb, DBuf<uint2>& work, uint64_t
     return EJOIN_OK;
 }
 
+// Every stride-th entry of a work list (a systematic sample of its blocks).
+__global__ void sample_work_kernel(const uint2* __restrict__ work, uint64_t nsample,
+                                   uint64_t stride, uint2* __restrict__ out) {
+    const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i < nsample) out[i] = work[i * stride];
+}
+
+int sample_worklist(const uint2* work, uint64_t nwork, uint64_t stride, DBuf<uint2>& out,
+                    uint64_t* nsample_out, cudaStream_t s) {
+    const uint64_t ns = stride ? (nwork + stride - 1) / stride : 0;
+    *nsample_out = ns;
+    if (ns == 0) return EJOIN_OK;
+    EJ_TRY(out.alloc(ns, s, "sampled work list"));
+    sample_work_kernel<<<(unsigned)((ns + 255) / 256), 256, 0, s>>>(work, ns, stride, out.p);
+    EJ_CUDA(cudaGetLastError());
+    note_launch();
+    return EJOIN_OK;
+}
+
 int sum_counts(const int32_t* counts, uint64_t n, unsigned long long* dev_total, cudaStream_t s) {
     if (n == 0) return EJOIN_OK;
     uint64_t blocks = (n + 255) / 256;

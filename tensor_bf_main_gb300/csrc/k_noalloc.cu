@@ -20,6 +20,11 @@
 //  * the first call on a device resolves the array's device address with
 //    cudaGetSymbolAddress (the host-side name is only a stand-in); make that
 //    first call before any stream capture on that device;
+//  * points and counts must be memory of that device (or managed memory);
+//    anything else is rejected with EJOIN_EINVAL before any launch;
+//  * every call waits for its own work on `stream` before it returns (it
+//    reads the status and the total back to the host);
+//  * on a non-zero return the counts are zero, not partial sums;
 //  * all calls share the one array: calls whose work overlaps on the GPU (two
 //    streams, two threads) race and corrupt each other's results.  Each call
 //    clears what must start at zero (status, counts, total).
@@ -68,28 +73,47 @@ __global__ void na_rowflags_kernel(const double* __restrict__ X, uint64_t n, uin
     if (row < n && lane == 0) bad[row] = ok ? 0 : 1;
 }
 
-// One thread per column: mean over the finite rows, rows in index order.
-__global__ void na_mean_kernel(const double* __restrict__ X, uint64_t n, uint32_t d,
-                               const uint8_t* __restrict__ bad, double* mu) {
-    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= d) return;
+// Mean over the finite rows, one block per 32 columns: warp w sums rows w,
+// w + 32, w + 64, ... of its 32 columns (lane = column, coalesced 256-byte
+// rows), then the 32 partial sums of each column are added in a fixed tree
+// order, so the mean is the same on every run.
+constexpr int kMeanWarps = 32;
+__global__ void __launch_bounds__(kMeanWarps * 32)
+    na_mean_kernel(const double* __restrict__ X, uint64_t n, uint32_t d,
+                   const uint8_t* __restrict__ bad, double* mu) {
+    __shared__ double part[kMeanWarps][33];
+    __shared__ uint32_t good[kMeanWarps];
+    const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const uint32_t k = blockIdx.x * 32u + lane;
     double s = 0.0;
-    uint64_t good = 0;
-    for (uint64_t r = 0; r < n; ++r)
-        if (!bad[r]) {
-            s += X[r * d + k];
-            ++good;
+    uint32_t g = 0;
+    for (uint64_t r = w; r < n; r += kMeanWarps) {
+        if (bad[r]) continue;
+        ++g;
+        if (k < d) s += X[r * d + k];
+    }
+    part[w][lane] = s;
+    if (lane == 0) good[w] = g;
+    __syncthreads();
+    for (int h = kMeanWarps / 2; h > 0; h >>= 1) {
+        if ((int)w < h) {
+            part[w][lane] += part[w + h][lane];
+            if (lane == 0) good[w] += good[w + h];
         }
-    mu[k] = good ? s / (double)good : 0.0;
+        __syncthreads();
+    }
+    if (w == 0 && k < d) mu[k] = good[0] ? part[0][lane] / (double)good[0] : 0.0;
 }
 
-bool is_device_pointer(const void* p) {
+// Memory the kernels on `dev` can read and write without peer access:
+// device memory of `dev` itself, or managed memory.
+bool is_device_pointer(const void* p, int dev) {
     cudaPointerAttributes a;
     if (!p || cudaPointerGetAttributes(&a, p) != cudaSuccess) {
         cudaGetLastError();
         return false;
     }
-    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+    return (a.type == cudaMemoryTypeDevice && a.device == dev) || a.type == cudaMemoryTypeManaged;
 }
 
 size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
@@ -141,7 +165,7 @@ int run(const double* X, uint64_t n, uint32_t d, double eps, cudaStream_t s, int
         na_rowflags_kernel<<<(unsigned)((n * 32 + 255) / 256), 256, 0, s>>>(X, n, d, bad);
         EJ_CUDA(cudaGetLastError());
         note_launch();
-        na_mean_kernel<<<(d + 127) / 128, 128, 0, s>>>(X, n, d, bad, mu);
+        na_mean_kernel<<<(d + 31) / 32, kMeanWarps * 32, 0, s>>>(X, n, d, bad, mu);
         EJ_CUDA(cudaGetLastError());
         note_launch();
         EJ_TRY(launch_pack_dmma(X, n, n_pad, nullptr, bad, mu, P, Y, h, g, s));
@@ -149,12 +173,21 @@ int run(const double* X, uint64_t n, uint32_t d, double eps, cudaStream_t s, int
         DevStatus hs;
         EJ_CUDA(cudaMemcpyAsync(&hs, st, sizeof hs, cudaMemcpyDeviceToHost, s));
         EJ_CUDA(cudaStreamSynchronize(s));
-        if (hs.timeout) return set_error(EJOIN_ETIMEOUT, "a bounded device wait expired");
-        if (hs.band_count > cap)
+        // on either failure the screen's partial counts are cleared, so a
+        // caller that ignores the status reads zeros, not plausible counts
+        if (hs.timeout) {
+            EJ_CUDA(cudaMemsetAsync(counts, 0, n * sizeof(int32_t), s));
+            EJ_CUDA(cudaStreamSynchronize(s));
+            return set_error(EJOIN_ETIMEOUT, "a bounded device wait expired");
+        }
+        if (hs.band_count > cap) {
+            EJ_CUDA(cudaMemsetAsync(counts, 0, n * sizeof(int32_t), s));
+            EJ_CUDA(cudaStreamSynchronize(s));
             return set_error(EJOIN_ENOMEM,
                              "boundary band of %llu pairs exceeds the %llu-entry queue of the "
                              "static scratch; use ejoin_self_join",
                              (unsigned long long)hs.band_count, (unsigned long long)cap);
+        }
         EJ_TRY(launch_band_recheck(X, n, d, nullptr, T, band, hs.band_count, counts, st, s));
     }
     EJ_TRY(sum_counts(counts, n, tot, s));
@@ -199,9 +232,10 @@ extern "C" int ejoin_self_join_noalloc(const double* points, uint64_t n, uint32_
     }
     EJ_CUDA(cudaSetDevice(device));
     int rc = EJOIN_OK;
-    if (n && (!is_device_pointer(points) || !is_device_pointer(counts)))
+    if (n && (!is_device_pointer(points, device) || !is_device_pointer(counts, device)))
         rc = set_error(EJOIN_EINVAL,
-                       "ejoin_self_join_noalloc: points and counts must be device memory");
+                       "ejoin_self_join_noalloc: points and counts must be device memory of "
+                       "device %d", device);
     else
         rc = run(points, n, d, eps, stream ? (cudaStream_t)stream : cudaStreamPerThread, device,
                  counts, total_out);

@@ -304,6 +304,11 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             uint32_t aug_ph[NAUG] = {0, 0};
             uint64_t aug_issued = 0;
             bool ok = true;
+            // test hook (DevStatus::withhold): the first stage is never
+            // issued, so the waits on it expire; it is not counted in
+            // `issued` and the producer stops before stage 0 comes round
+            // again, so the drain below never waits for it
+            bool withhold = *(volatile unsigned*)&a.st->withhold != 0u;
             // entries are read one block ahead (their latency hides behind a block)
             uint2 wnext = entry_or_end(a, item_at(0, a.lrun));
             for (uint64_t idx = 0; ok; ++idx) {
@@ -331,11 +336,15 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                     }
                     uint8_t* sa = stages + (size_t)st * STAGE_BYTES;
                     const int32_t x = (int32_t)slab_x<OPK>(step, a.nhi, a.split);
-                    ptx::mbar_arrive_expect_tx(&S.full[st], DATA_TX);
-                    ptx::tma_load_2d(sa, &tqa, x, ya, &S.full[st]);
-                    ptx::tma_load_2d(sa + SLAB_A, &tqb, x, yb, &S.full[st]);
-                    issued_ph[st] = ph;
-                    ++issued;
+                    if (withhold) {
+                        withhold = false;
+                    } else {
+                        ptx::mbar_arrive_expect_tx(&S.full[st], DATA_TX);
+                        ptx::tma_load_2d(sa, &tqa, x, ya, &S.full[st]);
+                        ptx::tma_load_2d(sa + SLAB_A, &tqb, x, yb, &S.full[st]);
+                        issued_ph[st] = ph;
+                        ++issued;
+                    }
                     if (++st == NST) {
                         st = 0;
                         ph ^= 1u;

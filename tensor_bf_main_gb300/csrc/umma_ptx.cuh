@@ -70,11 +70,12 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, DevSta
                                           unsigned where) {
     if (mbar_try_wait(bar, parity)) return true;
     const uint64_t t0 = globaltimer();
+    const uint64_t lim = st->wait_ns ? st->wait_ns : kWaitLimitNs;
     for (uint32_t it = 1;; ++it) {
         if (mbar_try_wait(bar, parity)) return true;
         if ((it & 255u) == 0) {
             if (*(volatile unsigned*)&st->timeout) return false;
-            if (globaltimer() - t0 > kWaitLimitNs) {
+            if (globaltimer() - t0 > lim) {
                 if (atomicCAS(&st->timeout, 0u, 1u) == 0u) st->where = where;
                 return false;
             }

@@ -1,7 +1,7 @@
 """Generate the committed golden fixtures under tests/golden/.
 
 Run in the container that has the reference mounted:
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <reference-root>
 
 Fixtures written (all small):
   test100.f64, test128.f64  -- the reference's shipped sample inputs
@@ -24,6 +24,7 @@ Fixtures written (all small):
 import json
 import os
 import subprocess
+import tempfile
 import sys
 
 import numpy as np
@@ -80,17 +81,20 @@ def main(ref):
         "loader_oneline.txt": " ".join(f"{v:.17g}" for v in vals.ravel()[:180]) + " ",
     }
     golden = {"dim": 90, "files": {}}
-    for fname, text in layouts.items():
-        p = os.path.join(HERE, fname)
-        with open(p, "w") as f:
-            f.write(text)
-        rows = oracle.reference_import_dataset(p, os.path.join("/tmp", fname + ".bin"))
-        golden["files"][fname] = {"rows": int(rows.shape[0]),
-                                  "values": [float(v) for v in rows.ravel()]}
+    with tempfile.TemporaryDirectory(dir=HERE) as tmp:
+        for fname, text in layouts.items():
+            p = os.path.join(HERE, fname)
+            with open(p, "w") as f:
+                f.write(text)
+            rows = oracle.reference_import_dataset(p, os.path.join(tmp, fname + ".bin"))
+            golden["files"][fname] = {"rows": int(rows.shape[0]),
+                                      "values": [float(v) for v in rows.ravel()]}
     with open(os.path.join(HERE, "loader_golden.json"), "w") as f:
         json.dump(golden, f)
     print("golden fixtures written to", HERE)
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py <reference-root>")
+    main(sys.argv[1])

@@ -54,6 +54,18 @@ def test_golden_ties(ej, mode):
 
 
 @pytest.mark.parametrize("mode", MODES)
+def test_golden_contraction(ej, mode):
+    """Pairs within ulps of the radius whose d2 depends on whether the
+    reference's accumulation is contracted into an fma: every mode follows the
+    fma reading (the oracle's, and nvcc's default for kernel_join.cu:186-189)."""
+    g = json.load(open(os.path.join(GOLDEN, "contraction.json")))
+    x = load_f64("contraction.f64", g["d"])
+    counts, total, st = ej.self_join(x, g["eps"], precision=mode)
+    assert total == g["fma"]["total"], (mode, st)
+    assert counts.tolist() == g["fma"]["counts"], mode
+
+
+@pytest.mark.parametrize("mode", MODES)
 @pytest.mark.parametrize("n,d", [(1, 3), (2, 1), (15, 18), (16, 3), (17, 64), (127, 128),
                                  (128, 18), (129, 64), (1000, 18), (3000, 128), (2500, 1)])
 def test_random_sizes(ej, oracle_mod, mode, n, d):
@@ -162,6 +174,10 @@ def test_cli_reference_argv_and_csv(ej, tmp_path):
     lines = open(tmp_path / "tensor_brute-force.txt").read().splitlines()
     assert lines[0].startswith("Dataset, epsilon, searchMode, executionTime, totalNeighbors")
     assert len(lines) == 4 and lines[1].split(", ")[4] == "11100"
+    # inputDim, computeDim, blockSize, warpPerBlock, computePrec, accumPrec of
+    # the kernel each mode ran: FP16 Gram screen (AUTO at d = 18), FP64 direct
+    assert lines[1].split(", ")[5:] == ["18", "64", "608", "19", "16", "32"]
+    assert lines[2].split(", ")[5:] == ["18", "18", "256", "8", "64", "64"]
 
 
 @pytest.mark.parametrize("mode", ["bf16_split", "fp16", "fp8_e4m3", "fp64_dmma"])

@@ -33,6 +33,20 @@ def test_oracle_ties_against_rational_restatement(oracle_mod):
         assert counts.tolist() == case["counts"]
 
 
+def test_oracle_follows_the_contracted_reading(oracle_mod):
+    """contraction.f64 holds pairs within ulps of the radius whose d2 differs
+    between acc = fma(t, t, acc) and acc = acc + fl(t * t); the oracle takes
+    the fma reading (nvcc's default contraction of kernel_join.cu:186-189)."""
+    g = json.load(open(os.path.join(GOLDEN, "contraction.json")))
+    x = load_f64("contraction.f64", g["d"])
+    counts, total = oracle_mod.self_join(x, g["eps"])
+    assert total == g["fma"]["total"] != g["mul_add"]["total"]
+    assert counts.tolist() == g["fma"]["counts"]
+    assert oracle_mod.threshold(g["eps"]) == g["threshold"]
+    c2, t2 = oracle_mod.py_self_join(x, g["eps"])
+    assert t2 == total and c2.tolist() == g["fma"]["counts"]
+
+
 def test_oracle_matches_python_loops_random(oracle_mod):
     rng = np.random.default_rng(3)
     x = rng.random((40, 5))
