@@ -58,6 +58,8 @@ def parse():
     p.add_argument("--no-fp64", action="store_true")
     p.add_argument("--fp64-rows", type=int, default=65536)
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-ref-gpu", action="store_true",
+                   help="skip timing the reference's own GPU kernels")
     return p.parse_args()
 
 
@@ -231,6 +233,42 @@ def gram_roofline(stats, d, prec, pk, args, proj_k):
             "l2_operand_bytes": l2_bytes, "l2_operand_gbs": l2_bytes / t / 1e9}
 
 
+def reference_gpu(ej, x, eps, stream, dev, n16=262144, n64=32768):
+    """The reference's own tensor-core join kernels on this GPU, built from its
+    kernel_join.cu by oracle/build_ref.sh and launched as its driver does
+    (oracle/ref_gpu.cu): distanceCalculationBruteForceTensorHalf (FP16 MQ,
+    kernel_join.cu:328-524) on the first n16 rows and ...TensorDouble (FP64
+    MQ, kernel_join.cu:530-677) on the first n64 rows of the workload.  Both
+    visit all N^2 ordered pairs, so their pairs/s does not depend on N.
+    Their totals are not exact (FP16 rounding; races in the reference's
+    shared-memory use); the exact total of the same rows is given beside
+    them.  None if the kernels were not built (no reference checkout where
+    build() ran) or d has no built variant."""
+    try:
+        from oracle import refgpu
+    except ImportError:
+        return None
+    n, d = x.shape
+    if d not in (64, 128) or not refgpu.available(f"fp16_d{d}", f"fp64_d{d}"):
+        return None
+    out = {}
+    for key, variant, kind, rows in (("fp16_mq", f"fp16_d{d}", "mq16", n16),
+                                     ("fp64_mq", f"fp64_d{d}", "mq64", n64)):
+        m = min(n, rows)
+        xs = np.ascontiguousarray(x[:m])
+        r = refgpu.run(variant, kind, xs, eps, d, reps=1)
+        _, exact, _ = ej.self_join(xs, eps, precision="bf16_split", stream=stream,
+                                   device=dev.index)
+        out[key] = {"kernel": ("distanceCalculationBruteForceTensorHalf" if kind == "mq16"
+                               else "distanceCalculationBruteForceTensorDouble"),
+                    "rows": m, "pairs_per_s": m * m / (r["kernel_ms_best"] / 1e3),
+                    "kernel_ms": r["kernel_ms_best"], "driver_ms": r["driver_ms_best"],
+                    "driver_pairs_per_s": m * m / (r["driver_ms_best"] / 1e3),
+                    "total": r["total"], "exact_total": exact,
+                    "sample": f"first {m} rows of the workload"}
+    return out
+
+
 def run_reference(args):
     world, rank, _ = dist_env()
     if rank != 0:
@@ -288,7 +326,10 @@ def run_ours(args):
     stream = torch.cuda.current_stream(dev)
     xd = torch.from_numpy(x).to(dev)
     cd = torch.empty(n, dtype=torch.int32, device=dev)
-    kw = dict(precision=args.precision, proj_k=proj_k, counts=cd, stream=stream, device=dev.index)
+    # repeated joins keep the library's scratch cached between calls (what a
+    # caller that joins again and again does); the first warm-up call maps it
+    kw = dict(precision=args.precision, proj_k=proj_k, counts=cd, stream=stream, device=dev.index,
+              keep_scratch=True)
 
     def barrier():
         if dist:
@@ -361,20 +402,28 @@ def run_ours(args):
                                   "extrapolated_ms_full": n * n / rate * 1e3,
                                   "speedup": value / world / rate}
 
+    if rank == 0 and not args.no_ref_gpu:
+        rg = reference_gpu(ej, x, eps, stream, dev)
+        if rg:
+            line["reference_gpu"] = rg
+
     if rank == 0 and not args.no_e2e:
         xh = torch.from_numpy(x).pin_memory()
         ch = np.empty(n, dtype=np.int32)
-        ej.self_join(xh, eps, precision=args.precision, proj_k=proj_k, counts=ch, stream=stream)
+        ej.self_join(xh, eps, precision=args.precision, proj_k=proj_k, counts=ch, stream=stream,
+                     keep_scratch=True)
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
         for _ in range(args.steps):
             ej.self_join(xh, eps, precision=args.precision, proj_k=proj_k, counts=ch,
-                         stream=stream)
+                         stream=stream, keep_scratch=True)
         torch.cuda.synchronize(dev)
         e2e_s = (time.perf_counter() - t0) / args.steps
         line["e2e"] = {"value": float(n) * n / e2e_s, "unit": "pairs/s",
                        "h2d_bytes_per_step": int(n * d * 8), "d2h_bytes_per_step": int(n * 4 + 8),
                        "ms_per_step": e2e_s * 1e3}
+
+    ej.release_scratch(dev.index)
 
     if rank == 0 and not args.no_cpu_baseline:
         rate, nq, dt, cores = cpu_rate(x, eps, args.cpu_seconds)

@@ -189,17 +189,38 @@ double ejoin_threshold(double eps);
 
 /* Text loader with the reference's semantics (dataset.cu:10-39): numbers
  * separated by commas and/or whitespace, a row closes every `dim` values, a
- * trailing partial row is dropped.  *points_out is malloc'd (free with
- * ejoin_free).  Returns EJOIN_EIO if the file cannot be opened (the
- * reference printed and exited, dataset.cu:16-20). */
+ * trailing partial row is dropped.  *points_out is allocated by the library
+ * -- page-locked host memory where a CUDA device is present, so that a join
+ * from it copies in chunks overlapped with its first passes -- and freed with
+ * ejoin_free.  Returns EJOIN_EIO if the file cannot be opened (the reference
+ * printed and exited, dataset.cu:16-20). */
 int ejoin_import_dataset(const char* filename, uint32_t dim, double** points_out,
                          uint64_t* n_out);
 
-/* Binary loader: raw little-endian float64, row-major, `dim` columns. */
+/* Binary loader: raw little-endian float64, row-major, `dim` columns, read
+ * in 64 MiB pieces straight into the result (allocated as for
+ * ejoin_import_dataset).  The fast path for the 1-8 GB inputs whose text form
+ * the reference's fscanf loop (dataset.cu:25-36) takes minutes to parse. */
 int ejoin_import_binary(const char* filename, uint32_t dim, double** points_out,
                         uint64_t* n_out);
 
+/* Free a buffer returned by the loaders. */
 void ejoin_free(void* p);
+
+/* Save a learned projection (k x d FP32, row-major, 1 <= k <= 16) with its
+ * certified spectral-norm bound to a small binary file (magic, version, k, d,
+ * bound, the values, a checksum), for reuse by later joins through
+ * ejoin_options.projection.  No reference counterpart (the projection is
+ * new; the reference keeps no state between runs). */
+int ejoin_save_projection(const char* filename, const float* P, uint32_t k, uint32_t d,
+                          double sigma_cert);
+
+/* Load a projection saved by ejoin_save_projection.  With P_out NULL only the
+ * shape (and bound) is returned; else P_out must hold capacity >= k * d
+ * floats.  A file that is not a projection file, has another version, the
+ * wrong size or a bad checksum returns EJOIN_EIO. */
+int ejoin_load_projection(const char* filename, float* P_out, uint64_t capacity, uint32_t* k_out,
+                          uint32_t* d_out, double* sigma_cert_out);
 
 /* Copy the calling thread's last error message into buf (NUL-terminated);
  * returns the status of that error (0 if none). */

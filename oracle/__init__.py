@@ -221,10 +221,13 @@ def py_fma(a: float, b: float, c: float) -> float:
 
 
 def py_pair_d2(a, b) -> float:
-    acc = 0.0
-    for ak, bk in zip(a, b):
-        t = float(ak) - float(bk)
-        acc = py_fma(t, t, acc)
+    """The reference's compiled arithmetic (oracle.c pair_d2): with t_j the
+    rounded differences, fma(t0, t0, fl(t1 * t1)), then fma(t_j, t_j, acc)."""
+    t = [float(ak) - float(bk) for ak, bk in zip(a, b)]
+    t1 = t[1] if len(t) > 1 else 0.0
+    acc = py_fma(t[0], t[0], t1 * t1)
+    for v in t[2:]:
+        acc = py_fma(v, v, acc)
     return acc
 
 

@@ -53,7 +53,7 @@ variant() {
                -e '/^#if COMPUTE_PREC == 64/i #endif' "$src/kernel_join.cu"
     fi
     # the reference's makefile flags (makefile:6), C++17 for CUDA 13's headers
-    "$NVCC" -cubin -gencode arch=compute_103a,code=sm_103a -std=c++17 -O3 -lineinfo "$@" \
+    "$NVCC" -cubin -gencode arch=compute_103a,code=sm_103a -std=c++17 -O3 -lineinfo -w "$@" \
         -I"$src" "$src/kernel_join.cu" -o "$OUT/ref_$name.cubin"
     rm -rf "$src"
     echo "built $OUT/ref_$name.cubin"

@@ -10,12 +10,20 @@
  *  - kernel_join.cu:168-200 `distanceCalculationBruteForceCuda` (searchMode 1,
  *    the FP64 CUDA-core kernel): for a query p and candidate c,
  *        acc = 0; for j in 0..d-1: acc += (p_j - c_j) * (p_j - c_j)
- *    in double, index order (kernel_join.cu:185-189), where nvcc contracts the
- *    multiply-add into one fused multiply-add; then a pair is a neighbour iff
- *    sqrt(acc) <= eps (kernel_join.cu:194).  Every ordered pair (i, j) is
- *    tested, the self pair included (the loop at :184 runs over all points).
- *    This file writes the contraction explicitly as fma() and is compiled
- *    with -ffp-contract=off so no other contraction can happen.
+ *    in double, index order (kernel_join.cu:185-189); then a pair is a
+ *    neighbour iff sqrt(acc) <= eps (kernel_join.cu:194).  Every ordered pair
+ *    (i, j) is tested, the self pair included (the loop at :184 runs over all
+ *    points).  How the products are rounded is the compiler's choice; the
+ *    reference's kernel compiled by nvcc for sm_103a computes, with
+ *    t_j = fl(p_j - c_j),
+ *        acc = fma(t_0, t_0, fl(t_1 * t_1));  acc = fma(t_j, t_j, acc), j >= 2
+ *    (`0 + t_0 * t_0` folds into the bare product, which is then fused into
+ *    the second step).  That form was pinned by running the reference's own
+ *    compiled kernel (built from its sources by oracle/build_ref.sh) on
+ *    pairs within ulps of the radius that the plain fma chain, this form and
+ *    the uncontracted sum count differently (tests/golden/contraction*.json),
+ *    at d = 18, 64 and 128.  This file writes every fma explicitly and is
+ *    compiled with -ffp-contract=off so no other contraction can happen.
  *
  *  - The predicate sqrt(acc) <= eps is evaluated as acc <= T where T is the
  *    largest double whose correctly rounded square root is <= eps
@@ -64,11 +72,14 @@ double oracle_threshold(double eps)
     return t;
 }
 
-/* Squared distance exactly as the reference's FP64 kernel forms it. */
+/* Squared distance exactly as the reference's FP64 kernel computes it once
+ * compiled (see the header): fma(t0, t0, fl(t1 * t1)), then fma(t, t, acc). */
 static inline double pair_d2(const double* a, const double* b, uint32_t d)
 {
-    double acc = 0.0;
-    for (uint32_t k = 0; k < d; ++k) {
+    double t0 = a[0] - b[0];
+    double t1 = d > 1 ? a[1] - b[1] : 0.0;
+    double acc = fma(t0, t0, t1 * t1);
+    for (uint32_t k = 2; k < d; ++k) {
         double t = a[k] - b[k];
         acc = fma(t, t, acc);
     }
@@ -81,8 +92,18 @@ static inline void pair_d2_x4(const double* a, const double* b0, const double* b
                               const double* b2, const double* b3, uint32_t d,
                               double out[4])
 {
-    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
-    for (uint32_t k = 0; k < d; ++k) {
+    double s0, s1, s2, s3;
+    {
+        double a0 = a[0], a1 = d > 1 ? a[1] : 0.0;
+        double u0 = a0 - b0[0], u1 = a0 - b1[0], u2 = a0 - b2[0], u3 = a0 - b3[0];
+        double v0 = d > 1 ? a1 - b0[1] : 0.0, v1 = d > 1 ? a1 - b1[1] : 0.0;
+        double v2 = d > 1 ? a1 - b2[1] : 0.0, v3 = d > 1 ? a1 - b3[1] : 0.0;
+        s0 = fma(u0, u0, v0 * v0);
+        s1 = fma(u1, u1, v1 * v1);
+        s2 = fma(u2, u2, v2 * v2);
+        s3 = fma(u3, u3, v3 * v3);
+    }
+    for (uint32_t k = 2; k < d; ++k) {
         double ak = a[k];
         double t0 = ak - b0[k], t1 = ak - b1[k], t2 = ak - b2[k], t3 = ak - b3[k];
         s0 = fma(t0, t0, s0);

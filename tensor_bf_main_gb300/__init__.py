@@ -106,7 +106,8 @@ EXPORTED = [
     "ejoin_certify_spectral_norm", "ejoin_threshold", "ejoin_import_dataset",
     "ejoin_import_binary", "ejoin_free", "ejoin_last_error", "ejoin_version",
     "ejoin_gpu_join_main_brute_force", "ejoin_self_join_noalloc", "ejoin_neighbor_lists",
-    "ejoin_join_counts", "ejoin_release_scratch",
+    "ejoin_join_counts", "ejoin_release_scratch", "ejoin_save_projection",
+    "ejoin_load_projection",
 ]
 
 # Test hooks declared in include/ejoin_testing.h.
@@ -156,6 +157,9 @@ def load_library(path: str = LIB_PATH):
     L.ejoin_testing_renormalise.restype = ctypes.c_int
     L.ejoin_self_join_noalloc.argtypes = [vp, u64, u32, dbl, ctypes.c_int, vp, vp, ctypes.POINTER(u64)]
     L.ejoin_release_scratch.argtypes = [ctypes.c_int]
+    L.ejoin_save_projection.argtypes = [ctypes.c_char_p, vp, u32, u32, dbl]
+    L.ejoin_load_projection.argtypes = [ctypes.c_char_p, vp, u64, ctypes.POINTER(u32),
+                                        ctypes.POINTER(u32), ctypes.POINTER(dbl)]
     L.ejoin_testing_inject.argtypes = [ctypes.c_int, u64]
     L.ejoin_testing_inject.restype = ctypes.c_int
     for name in EXPORTED:
@@ -304,6 +308,27 @@ def train_projection(points, eps: float, k: int = 8, device: int = 0, **kw):
     info = st.as_dict()
     info["loss_first"], info["loss_last"] = st.reserved[0], st.reserved[1]
     return P, sig.value, info
+
+
+def save_projection(filename: str, P, sigma_cert: float) -> None:
+    """Write a learned projection (k x d) and its certified bound to a file."""
+    P = np.ascontiguousarray(P, dtype=np.float32)
+    if P.ndim != 2:
+        raise ValueError("P must be k x d")
+    _check(load_library().ejoin_save_projection(filename.encode(), P.ctypes.data, P.shape[0],
+                                                P.shape[1], float(sigma_cert)))
+
+
+def load_projection(filename: str):
+    """Read a projection file: returns (P (k x d float32), sigma_cert)."""
+    L = load_library()
+    k, d, sig = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_double()
+    _check(L.ejoin_load_projection(filename.encode(), None, 0, ctypes.byref(k), ctypes.byref(d),
+                                   ctypes.byref(sig)))
+    P = np.zeros((k.value, d.value), dtype=np.float32)
+    _check(L.ejoin_load_projection(filename.encode(), P.ctypes.data, P.size, ctypes.byref(k),
+                                   ctypes.byref(d), ctypes.byref(sig)))
+    return P, sig.value
 
 
 def release_scratch(device: int = 0) -> None:

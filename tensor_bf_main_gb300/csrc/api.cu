@@ -23,7 +23,10 @@
 #include <algorithm>
 #include <atomic>
 #include <mutex>
+#include <set>
 #include <vector>
+
+#include <nvtx3/nvToolsExt.h>
 
 #include "ejoin_internal.cuh"
 #include "ejoin_testing.h"
@@ -133,6 +136,41 @@ bool alloc_should_fail() {
 void inject_gram_timeout(uint64_t ns) { g_gram_timeout.store(ns); }
 uint64_t take_gram_timeout() { return g_gram_timeout.exchange(0); }
 
+// ------------------------------------------------------- host buffers --
+
+namespace {
+std::mutex g_host_mu;
+std::set<void*> g_pinned;
+}  // namespace
+
+void* host_alloc(size_t bytes) {
+    int count = 0;
+    if (cudaGetDeviceCount(&count) == cudaSuccess && count > 0) {
+        void* p = nullptr;
+        if (cudaHostAlloc(&p, bytes, cudaHostAllocPortable) == cudaSuccess && p) {
+            std::lock_guard<std::mutex> lk(g_host_mu);
+            g_pinned.insert(p);
+            return p;
+        }
+    }
+    cudaGetLastError();
+    return malloc(bytes);
+}
+
+void host_free(void* p) {
+    if (!p) return;
+    {
+        std::lock_guard<std::mutex> lk(g_host_mu);
+        auto it = g_pinned.find(p);
+        if (it != g_pinned.end()) {
+            g_pinned.erase(it);
+            cudaFreeHost(p);
+            return;
+        }
+    }
+    free(p);
+}
+
 // ---------------------------------------------------------- threshold --
 
 // Largest double T with sqrt(T) <= eps.  Correctly rounded sqrt is monotone,
@@ -166,6 +204,18 @@ void oracle_band(double T, uint32_t d, double* Tlo, double* Thi) {
     *Tlo = lo > 0.0 ? lo : 0.0;
     *Thi = hi;
 }
+
+// ------------------------------------------------------------- tracing --
+
+// NVTX range over one phase of a join (prep, train, order, pack, gram,
+// recheck), visible in Nsight Systems / Compute timelines; a no-op unless a
+// tool is attached.  The phases' GPU times are also in ejoin_stats.
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 // ------------------------------------------------------------ devices --
 
@@ -304,7 +354,10 @@ static int screen_and_recheck(Join& J, uint64_t cap0, Screen&& screen, Recheck&&
         }
         EJ_CUDA(cudaMemsetAsync(J.counts, 0, n_pad * sizeof(int32_t), J.s));
         tg.start(J.s);
-        EJ_TRY(screen(band.p, cap / unit, dst.p));
+        {
+            NvtxRange nr("ejoin:gram");
+            EJ_TRY(screen(band.p, cap / unit, dst.p));
+        }
         tg.stop(J.s);
         DevStatus h;
         EJ_CUDA(cudaMemcpyAsync(&h, dst.p, sizeof h, cudaMemcpyDeviceToHost, J.s));
@@ -314,7 +367,10 @@ static int screen_and_recheck(Join& J, uint64_t cap0, Screen&& screen, Recheck&&
         if (h.band_count <= cap / unit) {
             const uint64_t pairs = unit == 1 ? h.band_count : h.band_pairs;
             tr.start(J.s);
-            EJ_TRY(recheck(band.p, h.band_count, pairs, dst.p));
+            {
+                NvtxRange nr("ejoin:recheck");
+                EJ_TRY(recheck(band.p, h.band_count, pairs, dst.p));
+            }
             tr.stop(J.s);
             EJ_CUDA(cudaMemcpyAsync(&h, dst.p, sizeof h, cudaMemcpyDeviceToHost, J.s));
             EJ_CUDA(cudaStreamSynchronize(J.s));
@@ -401,7 +457,8 @@ struct Learned {
 };
 
 static int prepare_learned(Join& J, const float* Y32, const float* Yerr, const uint8_t* bad,
-                           uint64_t n_pad, Learned& L) {
+                           uint64_t n_pad, Learned& L, TrainResult* trained = nullptr,
+                           double ms_trained = 0.0) {
     const uint32_t k = J.opt.proj_k;
     if (k == 0 || k > 16) return set_error(EJOIN_EINVAL, "proj_k must be in 0..16 (got %u)", k);
     EventTimer tt, to;
@@ -411,9 +468,13 @@ static int prepare_learned(Join& J, const float* Y32, const float* Yerr, const u
     if (J.opt.projection) {
         P.assign(J.opt.projection, J.opt.projection + (size_t)k * J.d);
         EJ_TRY(cert_spectral_norm(P.data(), k, J.d, &sigma));
+    } else if (trained) {
+        // trained already, overlapping the centring pass (run_screen16)
+        P.swap(trained->P);
+        sigma = trained->sigma_cert;
     } else {
         TrainResult tr;
-        EJ_TRY(train_projection_dev(Y32, bad, J.n, J.d, J.eps, k, J.opt.train_pairs,
+        EJ_TRY(train_projection_dev(Y32, bad, training_rows(J.n), J.d, J.eps, k, J.opt.train_pairs,
                                     J.opt.train_steps, J.opt.seed, J.opt.order == EJOIN_ORDER_LEAD,
                                     J.s, tr));
         P.swap(tr.P);
@@ -449,7 +510,7 @@ static int prepare_learned(Join& J, const float* Y32, const float* Yerr, const u
     L.k = k;
     J.perm = L.perm.p;
     J.st->sigma_cert = sigma;
-    J.st->ms_train = tt.ms();
+    J.st->ms_train = trained ? ms_trained : tt.ms();
     J.st->ms_order = to.ms();
     return EJOIN_OK;
 }
@@ -545,10 +606,58 @@ static int run_screen16(Join& J, Fmt fmt, bool split, Learned& L) {
     EJ_TRY(Y32.alloc(J.n * J.d, J.s, "FP32 centred points"));
     EJ_TRY(Yerr.alloc(J.n, J.s, "centring error bounds"));
     CenterStats cs;
-    EJ_TRY(launch_center_stats(J.X, J.n, J.d, bad.p, mu.p, Y32.p, Yerr.p, &cs, J.s, false, J.stage));
+    // Projection training samples the first training_rows(n) rows; it starts
+    // on a stream of its own as soon as those rows are centred, so with a
+    // staged (pinned host) input it runs while the rest is still copied.
+    const bool train = J.opt.proj_k && L.k == 0 && !J.opt.projection;
+    TrainResult trained;
+    bool have_trained = false;
+    double ms_train = 0.0;
+    const uint64_t nt = training_rows(J.n);
+    // end of the centring pass on J.s (recorded when the hook starts: every
+    // centring launch is enqueued by then), so that ms_prep leaves the
+    // overlapped training out
+    EventTimer tc;
+    bool centred_marked = false;
+    PrefixHook hook = [&](cudaEvent_t ready) -> int {
+        if (J.opt.proj_k == 0 || J.opt.proj_k > 16)
+            return set_error(EJOIN_EINVAL, "proj_k must be in 0..16 (got %u)", J.opt.proj_k);
+        tc.stop(J.s);
+        centred_marked = true;
+        cudaStream_t ts = nullptr;
+        EJ_CUDA(cudaStreamCreateWithFlags(&ts, cudaStreamNonBlocking));
+        struct StreamGuard {
+            cudaStream_t s;
+            ~StreamGuard() {
+                cudaStreamSynchronize(s);
+                cudaStreamDestroy(s);
+            }
+        } guard{ts};
+        EJ_CUDA(cudaStreamWaitEvent(ts, ready, 0));
+        NvtxRange nr("ejoin:train");
+        EventTimer tt;
+        tt.start(ts);
+        EJ_TRY(train_projection_dev(Y32.p, bad.p, nt, J.d, J.eps, J.opt.proj_k, J.opt.train_pairs,
+                                    J.opt.train_steps, J.opt.seed, J.opt.order == EJOIN_ORDER_LEAD,
+                                    ts, trained));
+        tt.stop(ts);
+        ms_train = tt.ms();
+        have_trained = true;
+        return EJOIN_OK;
+    };
+    {
+        NvtxRange nr("ejoin:prep");
+        EJ_TRY(launch_center_stats(J.X, J.n, J.d, bad.p, mu.p, Y32.p, Yerr.p, &cs, J.s, false,
+                                   J.stage, nt, train && J.n >= 2 ? &hook : nullptr));
+    }
     J.stage = nullptr;
     tp.stop(J.s);
-    const double ms_center = tp.ms();
+    double ms_center = tp.ms();
+    if (centred_marked) {
+        float v = 0.f;
+        cudaEventElapsedTime(&v, tp.a, tc.b);
+        ms_center = v;
+    }
     // The FP32 copies need the centred coordinates well inside the FP32 range:
     // squared norms of up to 2^27 coordinates must not overflow, and the
     // absolute error terms (2^-126 per flushed coordinate, underflow of FP32
@@ -561,13 +670,20 @@ static int run_screen16(Join& J, Fmt fmt, bool split, Learned& L) {
     // rows padded to whole 128 x 256 blocks of the Gram kernel
     const uint64_t n_pad = round_up(J.n, 256);
     // a second pass of the same join (pair emission) reuses the ordering
-    if (J.opt.proj_k && L.k == 0) EJ_TRY(prepare_learned(J, Y32.p, Yerr.p, bad.p, n_pad, L));
+    if (J.opt.proj_k && L.k == 0) {
+        NvtxRange nr("ejoin:order");
+        EJ_TRY(prepare_learned(J, Y32.p, Yerr.p, bad.p, n_pad, L, have_trained ? &trained : nullptr,
+                               ms_train));
+    }
     tp.start(J.s);
     const bool fp8 = (fmt == Fmt::E4M3);
     double kprod = 0;
     const ScreenParams P = screen_params(fmt, split, J.d, maxabs, J.T, J.opt.acc_bound_scale, &kprod);
     PackedSide side;
-    EJ_TRY(pack_side(Y32.p, Yerr.p, bad.p, J.n, n_pad, J.perm, P, side, J.s));
+    {
+        NvtxRange nr("ejoin:pack");
+        EJ_TRY(pack_side(Y32.p, Yerr.p, bad.p, J.n, n_pad, J.perm, P, side, J.s));
+    }
     tp.stop(J.s);
     J.st->ms_prep = ms_center + tp.ms();
     const uint64_t nT = n_pad / 128;
@@ -640,7 +756,7 @@ static int run_screen16(Join& J, Fmt fmt, bool split, Learned& L) {
         J.st->ms_order += te.ms();
         if (h.timeout)
             return set_error(EJOIN_ETIMEOUT, "Gram kernel: a bounded device wait expired (site %u)", h.where);
-        const double scaled = (double)h.band_count * (double)nwork / (double)std::max<uint64_t>(ns, 1);
+        const double scaled = (double)h.band_records * (double)nwork / (double)std::max<uint64_t>(ns, 1);
         cap_rec = std::max<uint64_t>(cap_rec, (uint64_t)(1.3 * scaled) + (1u << 20));
     }
     return screen_and_recheck(J, 2 * cap_rec, screen, recheck, n_pad, tg, tr, 2);
@@ -864,6 +980,7 @@ int ejoin_self_join(const double* points, uint64_t n, uint32_t d, double eps,
                     const ejoin_options* opt, int32_t* counts_out, uint64_t* total_out,
                     ejoin_stats* stats_out) {
     clear_error();
+    NvtxRange nr("ejoin_self_join");
     return self_join_impl(points, n, d, eps, opt, counts_out, total_out, stats_out);
 }
 
@@ -1131,8 +1248,9 @@ int ejoin_train_projection(const double* points, uint64_t n, uint32_t d, double 
     CenterStats cs;
     EJ_TRY(launch_center_stats(X, n, d, bad.p, mu.p, Y32.p, nullptr, &cs, s));
     TrainResult tr;
-    EJ_TRY(train_projection_dev(Y32.p, bad.p, n, d, eps, opt.proj_k, opt.train_pairs,
-                                opt.train_steps, opt.seed, opt.order == EJOIN_ORDER_LEAD, s, tr));
+    EJ_TRY(train_projection_dev(Y32.p, bad.p, training_rows(n), d, eps, opt.proj_k,
+                                opt.train_pairs, opt.train_steps, opt.seed,
+                                opt.order == EJOIN_ORDER_LEAD, s, tr));
     t.stop(s);
     memcpy(P_out, tr.P.data(), tr.P.size() * sizeof(float));
     if (sigma_cert_out) *sigma_cert_out = tr.sigma_cert;
@@ -1181,7 +1299,7 @@ int ejoin_last_error(char* buf, size_t len) {
 
 int ejoin_version(void) { return EJOIN_VERSION_MAJOR * 100 + EJOIN_VERSION_MINOR; }
 
-void ejoin_free(void* p) { free(p); }
+void ejoin_free(void* p) { host_free(p); }
 
 int ejoin_gpu_join_main_brute_force(unsigned int searchMode, unsigned int device, double* dataset,
                                     unsigned int* nbQueryPoints, double* epsilon,

@@ -8,6 +8,8 @@
 #include <stdint.h>
 #include <stdio.h>
 
+#include <algorithm>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -56,6 +58,11 @@ struct CallScope {
     uint64_t peak_reserved() const;
     ~CallScope();
 };
+// Host result buffers of the loaders: page-locked where a CUDA device is
+// present (else malloc); host_free releases either kind.
+void* host_alloc(size_t bytes);
+void host_free(void* p);
+
 // Test hook: make the k-th device allocation from now fail (0 = none).
 void inject_alloc_failure(uint64_t k);
 bool alloc_should_fail();
@@ -180,6 +187,9 @@ struct DevStatus {
     unsigned long long wait_ns;
     unsigned int withhold;
     unsigned int pad_;
+    // record queues: records actually produced (band_count counts the queue
+    // space reserved, which may include empty records, mask 0)
+    unsigned long long band_records;
 };
 // Test hook: the next tensor-core screen runs with wait deadline `ns` and a
 // producer that withholds its first stage (the waits then expire).
@@ -212,14 +222,21 @@ void finish_recheck32(Recheck32& R);
 
 // --------------------------------------------------------- device math --
 
-// Squared distance exactly as the reference's FP64 kernel forms it
-// (kernel_join.cu:185-189 compiled with nvcc's default contraction): per
-// coordinate t = a - b rounded once, acc = fma(t, t, acc), index order.
+// Squared distance exactly as the reference's FP64 kernel computes it
+// (kernel_join.cu:184-189 as nvcc compiles it for sm_103a): per coordinate
+// t_k = a_k - b_k rounded once; the first two terms as fma(t0, t0, fl(t1*t1))
+// (the compiler folds `0 + t0*t0` into the bare product and fuses that one
+// into the second step), then acc = fma(t_k, t_k, acc) for k >= 2 in index
+// order.  Running the reference's own compiled kernel on pairs built to tell
+// the readings apart pinned this form at d = 18, 64 and 128.  d = 1 gives
+// fl(t0*t0).
 __device__ __forceinline__ double exact_d2(const double* __restrict__ a,
                                            const double* __restrict__ b, uint32_t d) {
-    double acc = 0.0;
-    for (uint32_t k = 0; k < d; ++k) {
-        double t = __dsub_rn(a[k], b[k]);
+    const double t0 = __dsub_rn(a[0], b[0]);
+    const double t1 = d > 1 ? __dsub_rn(a[1], b[1]) : 0.0;
+    double acc = __fma_rn(t0, t0, __dmul_rn(t1, t1));
+    for (uint32_t k = 2; k < d; ++k) {
+        const double t = __dsub_rn(a[k], b[k]);
         acc = __fma_rn(t, t, acc);
     }
     return acc;
@@ -358,6 +375,12 @@ struct TrainResult {
     double loss_first = 0, loss_last = 0;
     double sigma_cert = 0;
 };
+// Rows the projection training samples from: the first training_rows(n)
+// rows (all rows up to 2^21, else half of them, at least 2^21), so that the
+// training can start while the rest of a staged input is still copied.
+inline uint64_t training_rows(uint64_t n) {
+    return n <= (1ull << 21) ? n : std::max<uint64_t>(1ull << 21, n / 2);
+}
 // Y32: FP32 centred copy of the points (launch_center_stats); bad: row flags.
 int train_projection_dev(const float* Y32, const uint8_t* bad, uint64_t n, uint32_t d, double eps,
                          uint32_t k, uint64_t pairs, uint32_t steps, uint64_t seed, int lead_only,
@@ -408,9 +431,15 @@ struct StageCopy {
 };
 // mu_given: mu holds the mean to use (another point set's, FP32-representable).
 // sc: X is still to be copied from pinned host memory (null: X is in place).
+// on_prefix (optional) is called once every copy and centring pass is
+// enqueued, with an event on s that completes when the first prefix_rows rows
+// are centred; it may run work on its own stream that waits for that event
+// (the projection training), overlapping the rest of the copy.
+using PrefixHook = std::function<int(cudaEvent_t)>;
 int launch_center_stats(const double* X, uint64_t n, uint32_t d, uint8_t* bad, double* mu,
                         float* Y32, float* Yerr, CenterStats* out, cudaStream_t s,
-                        bool mu_given = false, const StageCopy* sc = nullptr);
+                        bool mu_given = false, const StageCopy* sc = nullptr,
+                        uint64_t prefix_rows = 0, const PrefixHook* on_prefix = nullptr);
 // FP64 centred copy Y[n_pad][dp] and per-row thresholds h, g for the DMMA screen.
 int launch_pack_dmma(const double* X, uint64_t n, uint64_t n_pad, const uint32_t* perm,
                      const uint8_t* bad, const double* mu, const DmmaParams& P, double* Y,

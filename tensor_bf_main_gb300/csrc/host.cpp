@@ -7,6 +7,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
 #include <vector>
 
 #include "ejoin.h"
@@ -15,6 +16,9 @@ namespace ejoin {
 int set_error(int status, const char* fmt, ...);
 void clear_error();
 int cert_spectral_norm(const float* P, uint32_t k, uint32_t d, double* bound_out);
+// api.cu: host buffers of the loaders, page-locked where a CUDA device is
+// present (so that a join from them takes the chunked, overlapped copy)
+void* host_alloc(size_t bytes);
 }  // namespace ejoin
 
 using ejoin::set_error;
@@ -87,7 +91,7 @@ int ejoin_import_dataset(const char* filename, uint32_t dim, double** points_out
         }
     }
     const uint64_t rows = vals.size() / dim;
-    double* out = (double*)malloc((rows ? rows : 1) * dim * sizeof(double));
+    double* out = (double*)ejoin::host_alloc((rows ? rows : 1) * dim * sizeof(double));
     if (!out) return set_error(EJOIN_ENOMEM, "host allocation failed");
     if (rows) memcpy(out, vals.data(), rows * dim * sizeof(double));
     *points_out = out;
@@ -107,15 +111,23 @@ int ejoin_import_binary(const char* filename, uint32_t dim, double** points_out,
     const long sz = ftell(f);
     fseek(f, 0, SEEK_SET);
     const uint64_t rows = sz > 0 ? (uint64_t)sz / (8ull * dim) : 0;
-    double* out = (double*)malloc((rows ? rows : 1) * dim * sizeof(double));
+    double* out = (double*)ejoin::host_alloc((rows ? rows : 1) * dim * sizeof(double));
     if (!out) {
         fclose(f);
         return set_error(EJOIN_ENOMEM, "host allocation failed");
     }
-    const size_t got = rows ? fread(out, sizeof(double), rows * dim, f) : 0;
+    // straight into the (page-locked) result, 64 MiB at a time
+    const uint64_t total = rows * dim;
+    uint64_t got = 0;
+    while (got < total) {
+        const size_t want = (size_t)std::min<uint64_t>(total - got, 8ull << 20);
+        const size_t r = fread(out + got, sizeof(double), want, f);
+        got += r;
+        if (r != want) break;
+    }
     fclose(f);
-    if (got != rows * dim) {
-        free(out);
+    if (got != total) {
+        ejoin_free(out);
         return set_error(EJOIN_EIO, "short read on %s", filename);
     }
     *points_out = out;
@@ -207,3 +219,108 @@ int cert_spectral_norm(const float* P, uint32_t k, uint32_t d, double* bound_out
 }
 
 }  // namespace ejoin
+
+// ------------------------------------------------ projection files --
+//
+// A learned projection P (k x d FP32) with its certified spectral-norm bound,
+// so that a trained P can be reused by later joins (ejoin_options.projection
+// re-certifies it).  Little-endian layout:
+//   0   8  magic "EJOINPRJ"
+//   8   4  format version (1)
+//   12  4  k
+//   16  4  d
+//   20  4  zero
+//   24  8  sigma_cert (double)
+//   32  4 k d  P, row-major FP32
+//   ..  8  FNV-1a 64 of every byte before it
+namespace {
+constexpr char kProjMagic[8] = {'E', 'J', 'O', 'I', 'N', 'P', 'R', 'J'};
+constexpr uint32_t kProjVersion = 1;
+
+uint64_t fnv1a(const unsigned char* p, size_t n, uint64_t h = 1469598103934665603ull) {
+    for (size_t i = 0; i < n; ++i) {
+        h ^= p[i];
+        h *= 1099511628211ull;
+    }
+    return h;
+}
+void put_u32(std::vector<unsigned char>& b, uint32_t v) {
+    for (int i = 0; i < 4; ++i) b.push_back((unsigned char)(v >> (8 * i)));
+}
+void put_u64(std::vector<unsigned char>& b, uint64_t v) {
+    for (int i = 0; i < 8; ++i) b.push_back((unsigned char)(v >> (8 * i)));
+}
+uint32_t get_u32(const unsigned char* p) {
+    uint32_t v = 0;
+    for (int i = 0; i < 4; ++i) v |= (uint32_t)p[i] << (8 * i);
+    return v;
+}
+uint64_t get_u64(const unsigned char* p) {
+    uint64_t v = 0;
+    for (int i = 0; i < 8; ++i) v |= (uint64_t)p[i] << (8 * i);
+    return v;
+}
+}  // namespace
+
+int ejoin_save_projection(const char* filename, const float* P, uint32_t k, uint32_t d,
+                          double sigma_cert) {
+    ejoin::clear_error();
+    if (!filename || !P || k == 0 || k > 16 || d == 0)
+        return set_error(EJOIN_EINVAL, "bad arguments (k must be 1..16, d >= 1)");
+    std::vector<unsigned char> b;
+    b.insert(b.end(), kProjMagic, kProjMagic + 8);
+    put_u32(b, kProjVersion);
+    put_u32(b, k);
+    put_u32(b, d);
+    put_u32(b, 0);
+    uint64_t sbits;
+    memcpy(&sbits, &sigma_cert, 8);
+    put_u64(b, sbits);
+    for (uint64_t e = 0; e < (uint64_t)k * d; ++e) {
+        uint32_t v;
+        memcpy(&v, &P[e], 4);
+        put_u32(b, v);
+    }
+    put_u64(b, fnv1a(b.data(), b.size()));
+    FILE* f = fopen(filename, "wb");
+    if (!f) return set_error(EJOIN_EIO, "could not open %s for writing", filename);
+    const size_t w = fwrite(b.data(), 1, b.size(), f);
+    const int c = fclose(f);
+    if (w != b.size() || c != 0) return set_error(EJOIN_EIO, "short write on %s", filename);
+    return EJOIN_OK;
+}
+
+int ejoin_load_projection(const char* filename, float* P_out, uint64_t capacity, uint32_t* k_out,
+                          uint32_t* d_out, double* sigma_cert_out) {
+    ejoin::clear_error();
+    if (!filename) return set_error(EJOIN_EINVAL, "filename is NULL");
+    std::vector<char> raw;
+    if (!read_file(filename, raw)) return set_error(EJOIN_EIO, "could not open %s", filename);
+    raw.pop_back();  // read_file's terminating NUL
+    const unsigned char* p = reinterpret_cast<const unsigned char*>(raw.data());
+    const size_t n = raw.size();
+    if (n < 40 || memcmp(p, kProjMagic, 8) != 0)
+        return set_error(EJOIN_EIO, "%s is not a projection file", filename);
+    const uint32_t ver = get_u32(p + 8), k = get_u32(p + 12), d = get_u32(p + 16);
+    if (ver != kProjVersion) return set_error(EJOIN_EIO, "%s: format version %u unsupported", filename, ver);
+    if (k == 0 || k > 16 || d == 0 || n != 40 + 4ull * k * d)
+        return set_error(EJOIN_EIO, "%s: bad header or size", filename);
+    if (get_u64(p + n - 8) != fnv1a(p, n - 8))
+        return set_error(EJOIN_EIO, "%s: checksum mismatch", filename);
+    if (k_out) *k_out = k;
+    if (d_out) *d_out = d;
+    if (sigma_cert_out) {
+        const uint64_t sbits = get_u64(p + 24);
+        memcpy(sigma_cert_out, &sbits, 8);
+    }
+    if (P_out) {
+        if (capacity < (uint64_t)k * d)
+            return set_error(EJOIN_EINVAL, "P_out holds %llu of %u floats",
+                             (unsigned long long)capacity, k * d);
+        for (uint64_t e = 0; e < (uint64_t)k * d; ++e) {
+            const uint32_t v = get_u32(p + 32 + 4 * e);
+            memcpy(&P_out[e], &v, 4);
+        }
+    }
+    return EJOIN_OK;
+}

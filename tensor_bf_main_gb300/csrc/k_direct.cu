@@ -12,7 +12,9 @@
 //  * direct_query_kernel: the same tile over (query rows) x (all points).
 //  * band_recheck_kernel: one thread per band pair, the same chain.
 //
-// Zero padding of the k loop is exact: fma(0, 0, acc) == acc for acc >= +0.
+// Every chain follows the reference's compiled arithmetic (exact_d2:
+// fma(t0, t0, fl(t1*t1)), then fma(t, t, acc) in index order).  Zero padding
+// of the k loop is exact: fma(0, 0, acc) == acc for acc >= +0.
 #include <algorithm>
 
 #include "ejoin_internal.cuh"
@@ -44,11 +46,36 @@ __device__ __forceinline__ void stage_tile(double (*S)[PADK], const double* __re
 }
 
 // One 64x64 tile of exact squared distances.  Thread (ty, tx) owns rows
-// ty + 16*rr and columns tx + 16*cc.
+// ty + 16*rr and columns tx + 16*cc.  The first chunk (first) starts every
+// chain with fma(t0, t0, fl(t1*t1)), the reference's compiled form of its
+// first two terms (exact_d2); zero-padded coordinates give t = 0 there too.
 __device__ __forceinline__ void tile_chains(double acc[4][4], double (*SA)[PADK],
-                                            double (*SB)[PADK], int ty, int tx) {
+                                            double (*SB)[PADK], int ty, int tx, bool first) {
+    int k0 = 0;
+    if (first) {
+        double a0[4], a1[4], b0[4], b1[4];
+#pragma unroll
+        for (int rr = 0; rr < 4; ++rr) {
+            a0[rr] = SA[0][ty + 16 * rr];
+            a1[rr] = SA[1][ty + 16 * rr];
+        }
+#pragma unroll
+        for (int cc = 0; cc < 4; ++cc) {
+            b0[cc] = SB[0][tx + 16 * cc];
+            b1[cc] = SB[1][tx + 16 * cc];
+        }
+#pragma unroll
+        for (int rr = 0; rr < 4; ++rr)
+#pragma unroll
+            for (int cc = 0; cc < 4; ++cc) {
+                const double t0 = __dsub_rn(a0[rr], b0[cc]);
+                const double t1 = __dsub_rn(a1[rr], b1[cc]);
+                acc[rr][cc] = __fma_rn(t0, t0, __dmul_rn(t1, t1));
+            }
+        k0 = 2;
+    }
 #pragma unroll 4
-    for (int k = 0; k < KC; ++k) {
+    for (int k = k0; k < KC; ++k) {
         double a[4], b[4];
 #pragma unroll
         for (int rr = 0; rr < 4; ++rr) a[rr] = SA[k][ty + 16 * rr];
@@ -90,7 +117,7 @@ __global__ void __launch_bounds__(256) direct_selfjoin_kernel(const double* __re
         stage_tile(SA, X, n, d, I * TB, k0, nullptr, 0);
         stage_tile(SB, X, n, d, J * TB, k0, nullptr, 0);
         __syncthreads();
-        tile_chains(acc, SA, SB, ty, tx);
+        tile_chains(acc, SA, SB, ty, tx, k0 == 0);
     }
     const bool diag = (I == J);
 #pragma unroll
@@ -137,7 +164,7 @@ __global__ void __launch_bounds__(256) direct_query_kernel(const double* __restr
         else stage_tile(SA, X, n, d, Q * TB, k0, rows, nq);
         stage_tile(SB, X, n, d, J * TB, k0, nullptr, 0);
         __syncthreads();
-        tile_chains(acc, SA, SB, ty, tx);
+        tile_chains(acc, SA, SB, ty, tx, k0 == 0);
     }
 #pragma unroll
     for (int rr = 0; rr < 4; ++rr) {

@@ -729,7 +729,7 @@ __global__ void tile_max_kernel(const float* __restrict__ beta, const float4* __
 
 int launch_center_stats(const double* X, uint64_t n, uint32_t d, uint8_t* bad, double* mu,
                         float* Y32, float* Yerr, CenterStats* out, cudaStream_t s, bool mu_given,
-                        const StageCopy* sc) {
+                        const StageCopy* sc, uint64_t prefix_rows, const PrefixHook* on_prefix) {
     *out = CenterStats{};
     DBuf<float> muf;
     EJ_TRY(muf.alloc(d, s, "FP32 mean"));
@@ -777,8 +777,27 @@ int launch_center_stats(const double* X, uint64_t n, uint32_t d, uint8_t* bad, d
             note_launch();
             return EJOIN_OK;
         };
+        // event on s after the centring of the first prefix_rows rows, handed
+        // to on_prefix once every chunk is enqueued
+        cudaEvent_t pev = nullptr;
+        if (on_prefix) EJ_CUDA(cudaEventCreateWithFlags(&pev, cudaEventDisableTiming));
+        struct EventGuard {
+            cudaEvent_t& e;
+            ~EventGuard() {
+                if (e) cudaEventDestroy(e);
+            }
+        } pev_guard{pev};
+        bool pev_recorded = false;
+        auto mark_prefix = [&](uint64_t rows_done) -> int {
+            if (pev && !pev_recorded && rows_done >= std::min(prefix_rows, n)) {
+                EJ_CUDA(cudaEventRecord(pev, s));
+                pev_recorded = true;
+            }
+            return EJOIN_OK;
+        };
         if (!sc) {
             EJ_TRY(center(0, n));
+            EJ_TRY(mark_prefix(n));
         } else {
             // chunked copy on a side stream; s waits for each chunk, then
             // centres it.  The side stream first waits for s (X was allocated
@@ -813,6 +832,7 @@ int launch_center_stats(const double* X, uint64_t n, uint32_t d, uint8_t* bad, d
                     break;
                 }
                 rc = center(r0, rows);
+                if (rc == EJOIN_OK) rc = mark_prefix(r0 + rows);
             }
             // on success s is ordered after every chunk copy; on failure no copy
             // may stay in flight into memory the caller frees.  The stream and
@@ -822,6 +842,15 @@ int launch_center_stats(const double* X, uint64_t n, uint32_t d, uint8_t* bad, d
                 if (ev[c]) cudaEventDestroy(ev[c]);
             if (cs) cudaStreamDestroy(cs);
             if (rc != EJOIN_OK) return rc;
+        }
+        // every copy and centring pass is enqueued: the prefix hook (projection
+        // training on the first rows) runs while the rest still streams in
+        if (pev_recorded) {
+            const int hrc = (*on_prefix)(pev);
+            if (hrc != EJOIN_OK) {
+                cudaStreamSynchronize(s);
+                return hrc;
+            }
         }
     }
     CenterAcc h;

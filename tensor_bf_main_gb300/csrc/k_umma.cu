@@ -216,6 +216,7 @@ __device__ __forceinline__ void stage_band(const GramArgs& a, Ctl& S, uint32_t b
         } else {
             const unsigned long long g = atomicAdd(&a.st->band_count, 1ull);
             atomicAdd(&a.st->band_pairs, (unsigned long long)__popc(m));
+            atomicAdd(&a.st->band_records, 1ull);
             if (g < a.band_cap) a.band[g] = r;
         }
     }
@@ -478,35 +479,52 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         uint2 w = entry_or_end(a, item_at(0, a.lrun));
         uint2 wn = entry_or_end(a, item_at(1, a.lrun));
         float W = width(load_margins(w));
-        for (uint64_t idx = 0;; ++idx, ++it) {
-            if (item_at(idx, a.lrun) >= a.nwork) break;
+        auto is_active = [&](uint2 e) { return e.x != 0xffffffffu && ((e.y >> (30 + h)) & 1u); };
+        // Software pipeline: the first 32-column chunk of block idx + 1 is
+        // loaded from tensor memory before the counting work of block idx, so
+        // the load's latency hides behind that work.  v holds the chunk in
+        // flight; nothing reads it before tmem_ld_wait_regs.
+        uint32_t v[32];
+        float mx = 0.0f;
+        const uint32_t tq = tmem + ((q * 32u) << 16) + cg * 64u;
+        bool run = item_at(0, a.lrun) < a.nwork;
+        if (run) {
+            run = ptx::mbar_wait(&S.tfull[0], 0u, a.st, 30);
+            if (run) {
+                ptx::tc_fence_after();
+                if (is_active(w)) ptx::tmem_ld_max_32x32b_x32(tq, v, mx);
+            }
+        }
+        for (uint64_t idx = 0; run; ++idx, ++it) {
             const uint32_t b = it & 1u, use = it >> 1;
             const uint2 wnn = entry_or_end(a, item_at(idx + 2, a.lrun));
             const Margins mn = load_margins(wn);
             const uint32_t I = w.x, p = w.y & kPairMask, J = 2u * p + h;
-            const bool active = (w.y >> (30 + h)) & 1u;
+            const bool active = is_active(w);
             const bool diag = a.cross || (I == J);  // credit rows only
-            if (!ptx::mbar_wait(&S.tfull[b], use & 1u, a.st, 30)) break;
-            ptx::tc_fence_after();
-            // the two 32-column chunks one after the other: 32 live values
-            // instead of 64 (measured on c4: 8% faster than loading both at
-            // once); the accumulator is released after the second load
-            uint32_t v[32];
-            const uint32_t taddr = tmem + ((q * 32u) << 16) + b * ACC_COLS + cg * 64u;
+            // the two 32-column chunks one after the other (32 live values);
+            // the accumulator is released after the second load
+            const uint32_t taddr = tq + b * ACC_COLS;
             uint32_t in0 = 0, bd0 = 0, in1 = 0, bd1 = 0;
             bool busy0 = false, busy1 = false;
-            float mx = 0.0f;
             if (active) {
-                ptx::tmem_ld_max_32x32b_x32(taddr, v, mx);
-                ptx::tmem_ld_wait();
+                ptx::tmem_ld_wait_regs(v, mx);
                 busy0 = classify(v, mx, W, in0, bd0);
                 ptx::tmem_ld_max_32x32b_x32(taddr + 32u, v, mx);
-                ptx::tmem_ld_wait();
+                ptx::tmem_ld_wait_regs(v, mx);
             }
             ptx::tc_fence_before();
             __syncwarp();
             if (lane == 0) ptx::mbar_arrive(&S.tempty[b]);
             if (active) busy1 = classify(v, mx, W, in1, bd1);
+            // next block: wait for its accumulator, start its first load
+            const bool more = item_at(idx + 1, a.lrun) < a.nwork;
+            if (more) {
+                const uint32_t bn = (it + 1) & 1u, usen = (it + 1) >> 1;
+                if (!ptx::mbar_wait(&S.tfull[bn], usen & 1u, a.st, 31)) break;
+                ptx::tc_fence_after();
+                if (is_active(wn)) ptx::tmem_ld_max_32x32b_x32(tq + bn * ACC_COLS, v, mx);
+            }
             // the counts of buffer b were flushed and cleared for block it - 2
             if (!ptx::mbar_wait(&S.fdone[b], (use & 1u) ^ 1u, a.st, 32)) break;
             if (busy0 || busy1) {
@@ -528,11 +546,24 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             W = width(mn);
             w = wn;
             wn = wnn;
+            run = more;
         }
+        // a load still in flight (a wait that gave up) completes before the
+        // tensor memory is freed
+        ptx::tmem_ld_wait_regs(v, mx);
     } else {
         // ------------------------------------------------ count flusher
         // adds the per-block row / column counts to global memory and clears
-        // them, off the epilogue warps' critical path
+        // them, off the epilogue warps' critical path.  Band records go to
+        // queue space the CTA reserves kResChunk records at a time: one
+        // returning global atomic per chunk instead of one per block (its
+        // round trip on every block made this warp the kernel's limit); the
+        // unused tail of the last chunk is filled with empty records (mask 0,
+        // no pairs), and band_records counts the real ones.
+        constexpr uint32_t kResChunk = 4096;
+        static_assert(kResChunk >= BAND_SMEM, "a block's records fit one new chunk");
+        unsigned long long rbase = 0;
+        uint32_t rleft = 0;
         uint32_t it = 0;
         uint2 wnext = entry_or_end(a, item_at(0, a.lrun));
         for (uint64_t idx = 0;; ++idx, ++it) {
@@ -562,23 +593,42 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             // copy, and their pair count
             const uint32_t nst = min(S.band_n[b], BAND_SMEM);
             if (nst) {
-                unsigned long long gbase = 0;
-                if (lane == 0) gbase = atomicAdd(&a.st->band_count, (unsigned long long)nst);
-                gbase = __shfl_sync(FULL, gbase, 0);
+                // the first rleft records fill the current chunk, the rest
+                // start a new one
+                const bool grow = rleft < nst;
+                unsigned long long nbase = 0;
+                if (grow) {
+                    if (lane == 0) nbase = atomicAdd(&a.st->band_count, (unsigned long long)kResChunk);
+                    nbase = __shfl_sync(FULL, nbase, 0);
+                }
                 uint32_t np = 0;
                 for (uint32_t e = lane; e < nst; e += 32) {
                     const BandRec r = S.band_buf[b][e];
                     np += __popc(r.mask);
-                    if (gbase + e < a.band_cap) a.band[gbase + e] = r;
+                    const unsigned long long g = e < rleft ? rbase + e : nbase + (e - rleft);
+                    if (g < a.band_cap) a.band[g] = r;
                 }
                 np = __reduce_add_sync(FULL, np);
-                if (lane == 0) atomicAdd(&a.st->band_pairs, (unsigned long long)np);
+                if (lane == 0) {
+                    atomicAdd(&a.st->band_pairs, (unsigned long long)np);
+                    atomicAdd(&a.st->band_records, (unsigned long long)nst);
+                }
+                if (grow) {
+                    rbase = nbase + (nst - rleft);
+                    rleft = kResChunk - (nst - rleft);
+                } else {
+                    rbase += nst;
+                    rleft -= nst;
+                }
             }
             __syncwarp();
             if (lane == 0) S.band_n[b] = 0;
             __syncwarp();
             if (lane == 0) ptx::mbar_arrive(&S.fdone[b]);
         }
+        // empty records in the unused tail of the last reserved chunk
+        for (uint32_t e = lane; e < rleft; e += 32)
+            if (rbase + e < a.band_cap) a.band[rbase + e] = BandRec{0u, 0u, 0u, 0u};
     }
 
     ptx::tc_fence_before();

@@ -233,6 +233,20 @@ __device__ __forceinline__ void tmem_ld_max_32x32b_x32(uint32_t taddr, uint32_t 
 __device__ __forceinline__ void tmem_ld_wait() {
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
+// The same wait, naming the load's destination registers as read and written
+// by it, so that the compiler keeps every use of them after the wait (for a
+// load left in flight while other work runs).
+__device__ __forceinline__ void tmem_ld_wait_regs(uint32_t (&r)[32], float& mx) {
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]),
+                   "+r"(r[6]), "+r"(r[7]), "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]),
+                   "+r"(r[12]), "+r"(r[13]), "+r"(r[14]), "+r"(r[15]), "+r"(r[16]), "+r"(r[17]),
+                   "+r"(r[18]), "+r"(r[19]), "+r"(r[20]), "+r"(r[21]), "+r"(r[22]), "+r"(r[23]),
+                   "+r"(r[24]), "+r"(r[25]), "+r"(r[26]), "+r"(r[27]), "+r"(r[28]), "+r"(r[29]),
+                   "+r"(r[30]), "+r"(r[31]), "+f"(mx)
+                 :
+                 : "memory");
+}
 
 }  // namespace ptx
 }  // namespace ejoin

@@ -1,25 +1,34 @@
-"""Generate tests/golden/contraction.f64 / contraction.json.
+"""Generate the contraction fixtures: tests/golden/contraction[_d<D>].f64/.json.
 
 The reference's FP64 kernel (kernel_join.cu:186-189) accumulates
-`acc += (p - c) * (p - c)` per coordinate.  Compiled by nvcc with its default
-floating-point contraction, that is acc = fma(t, t, acc); without contraction
-it is acc = acc + fl(t * t).  The two readings give different d2 in the last
-bits, so they can disagree on `sqrt(d2) <= eps` for pairs that lie within a
-few ulps of the radius.  Every other fixture here is built on exactly
-representable sums, where both readings agree; this one is built from such
-disagreeing pairs, so it tells the readings apart.
+`acc += (p - c) * (p - c)` per coordinate, from acc = 0.  The compiler decides
+how the products are rounded, and three readings are plausible:
 
-Construction (seeded, pure Python, no reference code): 64 pairs (a, b) in 18
-dimensions, pair k at a = B_k + U[0,1)^18 with B_k = 8 x (the 7 low bits of k)
-on the first 7 coordinates, and b = a + r u for a random unit vector u and r
-within a few ulps of eps = 1 (threshold T = the largest double whose square
-root is <= 1).  For each candidate both readings are evaluated exactly
-(rational arithmetic, rounded once per operation as the hardware does); a
-candidate is kept when its readings fall on different sides of T: the first
-40 pairs are counted by the fma reading only, the other 24 by the mul-add
-reading only.  Points of different pairs differ by more than 5 in some
-coordinate, so no point has a neighbour besides its partner.  The JSON holds the per-point counts and
-totals of both readings.
+  fma      acc = fma(t_j, t_j, acc) for every j (contraction of every step)
+  first    acc = fma(t_0, t_0, fl(t_1 * t_1)), then fma(t_j, t_j, acc) for
+           j >= 2 (`0 + t_0 * t_0` folded into the bare product, which is then
+           fused into the second step instead of the second product)
+  mul_add  acc = acc + fl(t_j * t_j) (no contraction)
+
+They give different d2 in the last bits, so they can disagree on
+`sqrt(d2) <= eps` for pairs that lie within a few ulps of the radius.  Every
+other fixture here is built on exactly representable sums, where all readings
+agree; these are built from disagreeing pairs, so they tell the readings
+apart (the GPU tests run the reference's own compiled kernel on them).
+
+Construction (seeded, pure Python, no reference code), for each dimension D:
+pairs (a, b) in D dimensions, pair k at a = B_k + U[0,1)^D with
+B_k = 8 x (the 7 low bits of k) on the first 7 coordinates, and b = a + r u
+for a random unit vector u and r within a few ulps of eps = 1 (threshold
+T = the largest double whose square root is <= 1).  Each candidate is
+evaluated exactly in every reading (rational arithmetic, rounded once per
+operation as the hardware does) and kept when its readings do not all agree:
+for each ordered pair of readings (X, Y), WANT[(X, Y)] pairs that X counts and
+Y does not -- unequal numbers, so that the three readings also give three
+different totals (the reference's kernel reports only a total).  Points of
+different pairs differ by more than 5 in some coordinate, so no point has a
+neighbour besides its partner.  The JSON holds the per-point counts and totals
+of every reading.
 
     python tests/golden/make_contraction.py
 """
@@ -32,9 +41,9 @@ from fractions import Fraction
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-D = 18
 EPS = 1.0
-N_FMA_ONLY, N_MUL_ONLY = 40, 24
+WANT = {("fma", "first"): 12, ("first", "fma"): 3, ("fma", "mul_add"): 9, ("mul_add", "fma"): 2,
+        ("first", "mul_add"): 6, ("mul_add", "first"): 1}
 
 
 def threshold(eps):
@@ -46,11 +55,25 @@ def threshold(eps):
     return t
 
 
+def _fma(x, y, z):
+    return float(Fraction(x) * Fraction(y) + Fraction(z))
+
+
 def fma_reading(a, b):
     acc = 0.0
     for x, y in zip(a, b):
         t = x - y
-        acc = float(Fraction(t) * Fraction(t) + Fraction(acc))
+        acc = _fma(t, t, acc)
+    return acc
+
+
+def first_reading(a, b):
+    t = [x - y for x, y in zip(a, b)]
+    if len(t) == 1:
+        return t[0] * t[0]
+    acc = _fma(t[0], t[0], t[1] * t[1])
+    for v in t[2:]:
+        acc = _fma(v, v, acc)
     return acc
 
 
@@ -62,48 +85,60 @@ def mul_add_reading(a, b):
     return acc
 
 
-def main():
+READINGS = {"fma": fma_reading, "first": first_reading, "mul_add": mul_add_reading}
+
+
+def make(d, name, seed):
     T = threshold(EPS)
-    rng = np.random.default_rng(20260101)
-    fma_only, mul_only = [], []
+    rng = np.random.default_rng(seed)
+    want = dict(WANT)
+    pairs = []
     tries = 0
-    for k in range(N_FMA_ONLY + N_MUL_ONLY):
-        want_fma = k < N_FMA_ONLY
-        base = np.zeros(D)
+    while any(want.values()):
+        tries += 1
+        if tries > 20_000_000:
+            sys.exit(f"d={d}: not enough discriminating pairs ({want})")
+        k = len(pairs)
+        base = np.zeros(d)
         base[:7] = 8.0 * ((k >> np.arange(7)) & 1)
-        while True:
-            tries += 1
-            if tries > 5_000_000:
-                sys.exit("not enough discriminating pairs found")
-            a = base + rng.random(D)
-            u = rng.standard_normal(D)
-            u /= np.linalg.norm(u)
-            r = 1.0 + rng.uniform(-4, 4) * 2.0 ** -53
-            b = a + r * u
-            af, bf = [float(v) for v in a], [float(v) for v in b]
-            f, m = fma_reading(af, bf) <= T, mul_add_reading(af, bf) <= T
-            if want_fma and f and not m:
-                fma_only.append((af, bf))
+        a = base + rng.random(d)
+        u = rng.standard_normal(d)
+        u /= np.linalg.norm(u)
+        b = a + (1.0 + rng.uniform(-4, 4) * 2.0 ** -53) * u
+        af, bf = [float(v) for v in a], [float(v) for v in b]
+        if abs(mul_add_reading(af, bf) - T) > 2.0 ** -46:
+            continue  # farther than 64 ulps from T: every reading agrees
+        inside = {r: fn(af, bf) <= T for r, fn in READINGS.items()}
+        for (x, y), left in want.items():
+            if left and inside[x] and not inside[y]:
+                want[(x, y)] -= 1
+                pairs.append((af, bf))
                 break
-            if not want_fma and m and not f:
-                mul_only.append((af, bf))
-                break
-    pairs = fma_only + mul_only
     x = np.array([p for pair in pairs for p in pair], dtype="<f8")
     n = x.shape[0]
-    x.tofile(os.path.join(HERE, "contraction.f64"))
-    out = {"n": n, "d": D, "eps": EPS, "threshold": T}
-    for name, fn in (("fma", fma_reading), ("mul_add", mul_add_reading)):
+    totals = set()
+    x.tofile(os.path.join(HERE, name + ".f64"))
+    out = {"n": n, "d": d, "eps": EPS, "threshold": T}
+    for r, fn in READINGS.items():
         counts = [1] * n
         for i in range(0, n, 2):
             if fn(list(x[i]), list(x[i + 1])) <= T:
                 counts[i] += 1
                 counts[i + 1] += 1
-        out[name] = {"total": sum(counts), "counts": counts}
-    with open(os.path.join(HERE, "contraction.json"), "w") as f:
+        out[r] = {"total": sum(counts), "counts": counts}
+        totals.add(sum(counts))
+    if len(totals) != len(READINGS):
+        sys.exit(f"{name}: totals do not tell the readings apart; change the seed")
+    with open(os.path.join(HERE, name + ".json"), "w") as f:
         json.dump(out, f)
-    print(f"{n} points, totals: fma {out['fma']['total']}, mul_add {out['mul_add']['total']} "
-          f"({tries} candidate pairs)")
+    print(f"{name}: {n} points, totals " +
+          ", ".join(f"{r} {out[r]['total']}" for r in READINGS) + f" ({tries} candidates)")
+
+
+def main():
+    make(18, "contraction", 20260101)
+    make(64, "contraction_d64", 20260164)
+    make(128, "contraction_d128", 20260228)
 
 
 if __name__ == "__main__":

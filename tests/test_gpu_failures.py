@@ -32,10 +32,16 @@ def clustered(n, d, rng, k=8, sigma=0.05):
 
 @pytest.fixture(scope="module")
 def case(oracle_mod):
+    """Clusters plus two far-off groups of 40 identical points exactly eps
+    apart: 1,600 pairs on the boundary itself, which every screen (the FP64
+    one included) must send to the exact recheck."""
     rng = np.random.default_rng(99)
     x = clustered(4000, 32, rng)
     i, j = rng.integers(0, 4000, 4000), rng.integers(0, 4000, 4000)
     eps = float(np.quantile(np.sqrt(((x[i] - x[j]) ** 2).sum(1)), 60 / 4000))
+    g = np.full((80, 32), 50.0)
+    g[40:, 0] += eps
+    x = np.concatenate([x, g])
     exp, tot = oracle_mod.self_join(x, eps)
     return x, eps, exp, tot
 

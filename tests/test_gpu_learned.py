@@ -96,6 +96,23 @@ def test_lead_order_and_reused_projection(ej):
     assert abs(s1["sigma_cert"] - sigma) <= 1e-12 * sigma
 
 
+def test_saved_projection_reused_from_file(ej, tmp_path):
+    """A trained P saved to a projection file and loaded back prunes exactly
+    the same tile pairs and gives the same exact counts."""
+    x = latent_data(50000, 7)
+    eps = eps_for_mean(x, 30)
+    P, sigma, _ = ej.train_projection(x, eps, k=8, train_steps=40)
+    path = str(tmp_path / "c.ejp")
+    ej.save_projection(path, P, sigma)
+    Q, sig2 = ej.load_projection(path)
+    assert sig2 == sigma and np.array_equal(P, Q)
+    c1, t1, s1 = ej.self_join(x, eps, precision="fp16", proj_k=8, projection=P)
+    c2, t2, s2 = ej.self_join(x, eps, precision="fp16", proj_k=8, projection=Q)
+    plain, tp, _ = ej.self_join(x, eps, precision="fp64_dmma")
+    assert t1 == t2 == tp and np.array_equal(c1, c2) and np.array_equal(c1, plain)
+    assert s1["tile_pairs_run"] == s2["tile_pairs_run"] < s1["tile_pairs_total"]
+
+
 def test_training_gains_over_untrained_projection(ej):
     """What the trained network buys: tile pairs reaching the GEMM and time,
     trained P vs an untrained random contractive P vs no projection."""

@@ -54,15 +54,17 @@ def test_golden_ties(ej, mode):
 
 
 @pytest.mark.parametrize("mode", MODES)
-def test_golden_contraction(ej, mode):
-    """Pairs within ulps of the radius whose d2 depends on whether the
-    reference's accumulation is contracted into an fma: every mode follows the
-    fma reading (the oracle's, and nvcc's default for kernel_join.cu:186-189)."""
-    g = json.load(open(os.path.join(GOLDEN, "contraction.json")))
-    x = load_f64("contraction.f64", g["d"])
+@pytest.mark.parametrize("name", ["contraction", "contraction_d64", "contraction_d128"])
+def test_golden_contraction(ej, mode, name):
+    """Pairs within ulps of the radius whose count depends on how the
+    reference's accumulation is rounded: every mode counts what the
+    reference's own compiled kernel counts (fma(t0, t0, fl(t1 * t1)), then
+    the fma chain; kernel_join.cu:186-189)."""
+    g = json.load(open(os.path.join(GOLDEN, name + ".json")))
+    x = load_f64(name + ".f64", g["d"])
     counts, total, st = ej.self_join(x, g["eps"], precision=mode)
-    assert total == g["fma"]["total"], (mode, st)
-    assert counts.tolist() == g["fma"]["counts"], mode
+    assert total == g["first"]["total"], (mode, st)
+    assert counts.tolist() == g["first"]["counts"], mode
 
 
 @pytest.mark.parametrize("mode", MODES)

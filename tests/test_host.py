@@ -87,3 +87,50 @@ def test_no_gpu_raises_instead_of_falling_back(ej):
     with pytest.raises(ej.EjoinError) as e:
         ej.self_join(np.zeros((4, 3)), 0.1)
     assert e.value.status == -4
+
+
+def test_projection_file_round_trip(ej, tmp_path):
+    rng = np.random.default_rng(5)
+    P = rng.standard_normal((8, 64)).astype(np.float32)
+    path = str(tmp_path / "p.ejp")
+    ej.save_projection(path, P, 0.987654321)
+    Q, sig = ej.load_projection(path)
+    assert Q.dtype == np.float32 and Q.shape == (8, 64)
+    assert np.array_equal(Q.view(np.uint32), P.view(np.uint32))
+    assert sig == 0.987654321
+    assert os.path.getsize(path) == 40 + 4 * 8 * 64
+
+
+def test_projection_file_rejects_damage(ej, tmp_path):
+    P = np.ones((2, 3), dtype=np.float32)
+    path = tmp_path / "p.ejp"
+    ej.save_projection(str(path), P, 1.0)
+    raw = bytearray(path.read_bytes())
+    for pos in (0, 9, 13, 30, len(raw) - 20):
+        bad = bytearray(raw)
+        bad[pos] ^= 0x40
+        path.write_bytes(bytes(bad))
+        with pytest.raises(ej.EjoinError) as e:
+            ej.load_projection(str(path))
+        assert e.value.status == -7
+    path.write_bytes(bytes(raw[:-1]))
+    with pytest.raises(ej.EjoinError):
+        ej.load_projection(str(path))
+    with pytest.raises(ej.EjoinError) as e:
+        ej.load_projection(str(tmp_path / "missing.ejp"))
+    assert e.value.status == -7
+    with pytest.raises(ej.EjoinError) as e:
+        ej.save_projection(str(tmp_path / "k17.ejp"), np.ones((17, 3), np.float32), 1.0)
+    assert e.value.status == -1
+
+
+def test_binary_loader_reads_in_pieces(ej, tmp_path):
+    rng = np.random.default_rng(6)
+    x = rng.standard_normal((3001, 7))
+    path = tmp_path / "x.f64"
+    x.astype("<f8").tofile(path)
+    assert np.array_equal(ej.import_binary(str(path), 7), x)
+    # a trailing partial row is dropped
+    with open(path, "ab") as f:
+        f.write(b"\0" * 16)
+    assert np.array_equal(ej.import_binary(str(path), 7), x)
