@@ -15,8 +15,11 @@ extrapolated as N^2 / rate) and the CPU baseline (the oracle restatement of
 the reference's FP64 kernel on all host cores, bounded sample).
 
 --impl reference times the reference's CPU algorithm (the oracle port; the
-reference has no CPU join of its own and its GPU code cannot be built on the
-box) on the same workload, one bounded sample of query rows per step.
+reference has no CPU join of its own) on the same workload, one bounded
+sample of query rows per step.  The reference's own GPU kernels, built from
+its sources where the reference checkout is present (oracle/build_ref.sh),
+are timed on the same GPU by the default arm and reported in its line under
+"reference_gpu".
 
 With --gpus N under torchrun every rank runs an independent replica
 (replicas only: the spec path is single-GPU) and rank 0 reports the
@@ -419,9 +422,21 @@ def run_ours(args):
                          stream=stream, keep_scratch=True)
         torch.cuda.synchronize(dev)
         e2e_s = (time.perf_counter() - t0) / args.steps
+        # the host link on its own: a plain copy of the same pinned rows (the
+        # staged join cannot beat it; it varies between boxes with where the
+        # pinned pages sit)
+        xd2 = torch.empty_like(xd)
+        xd2.copy_(xh, non_blocking=True)
+        torch.cuda.synchronize(dev)
+        c0 = time.perf_counter()
+        xd2.copy_(xh, non_blocking=True)
+        torch.cuda.synchronize(dev)
+        copy_ms = (time.perf_counter() - c0) * 1e3
+        del xd2
         line["e2e"] = {"value": float(n) * n / e2e_s, "unit": "pairs/s",
                        "h2d_bytes_per_step": int(n * d * 8), "d2h_bytes_per_step": int(n * 4 + 8),
-                       "ms_per_step": e2e_s * 1e3}
+                       "ms_per_step": e2e_s * 1e3, "plain_h2d_copy_ms": copy_ms,
+                       "plain_h2d_gbs": n * d * 8 / copy_ms / 1e6}
 
     ej.release_scratch(dev.index)
 
