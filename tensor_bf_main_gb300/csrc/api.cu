@@ -563,7 +563,7 @@ struct PackedSide {
     uint64_t n_pad = 0;
     DBuf<uint16_t> Q, Aug;
     DBuf<uint8_t> Q8;
-    DBuf<float> beta, tmax, Xf, rad, sig, tsig;
+    DBuf<float> beta, cmax, Xf, rad, sig, tsig;
     const void* operands(const ScreenParams& P) const {
         return P.fmt == Fmt::E4M3 ? (const void*)Q8.p : (const void*)Q.p;
     }
@@ -578,7 +578,7 @@ static int pack_side(const float* Y32, const float* Yerr, const uint8_t* bad, ui
     else EJ_TRY(S.Q.alloc(n_pad * P.width, s, "packed operands"));
     EJ_TRY(S.Aug.alloc(n_pad * 32, s, "aug operands"));
     EJ_TRY(S.beta.alloc(n_pad, s, "out margins"));
-    EJ_TRY(S.tmax.alloc(n_pad / 128, s, "tile margins"));
+    EJ_TRY(S.cmax.alloc(n_pad / 32, s, "chunk margins"));
     EJ_TRY(S.Xf.alloc(n_pad * P.d, s, "FP32 coordinates"));
     EJ_TRY(S.rad.alloc(n_pad, s, "FP32 radii"));
     if (fp8) {
@@ -590,7 +590,7 @@ static int pack_side(const float* Y32, const float* Yerr, const uint8_t* bad, ui
         EJ_TRY(launch_pack16(Y32, Yerr, n, n_pad, perm, bad, P, S.Q.p, S.Aug.p, S.beta.p, S.Xf.p,
                              S.rad.p, s));
     }
-    return launch_tile_max(S.beta.p, nullptr, n_pad, S.tmax.p, s);
+    return launch_chunk_max(S.beta.p, n_pad, S.cmax.p, s);
 }
 
 // L owns the permutation that J.perm points to; it must outlive the final
@@ -705,7 +705,7 @@ static int run_screen16(Join& J, Fmt fmt, bool split, Learned& L) {
     const void* Qp = side.operands(P);
     auto screen = [&](BandPair* band, uint64_t cap, DevStatus* st) {
         const GramSide gs{Qp, side.Aug.p, n_pad};
-        return launch_gram16(gs, gs, P, work.p, nwork, side.tmax.p, side.beta.p, side.tsig.p,
+        return launch_gram16(gs, gs, P, work.p, nwork, side.cmax.p, side.beta.p, side.tsig.p,
                              side.sig.p, false,
                              J.counts, reinterpret_cast<BandRec*>(band), cap, st, J.em, J.sms,
                              J.s);
@@ -747,7 +747,7 @@ static int run_screen16(Join& J, Fmt fmt, bool split, Learned& L) {
         EJ_TRY(est.alloc(1, J.s, "band estimate"));
         EJ_TRY(est.zero(J.s));
         const GramSide gs{Qp, side.Aug.p, n_pad};
-        EJ_TRY(launch_gram16(gs, gs, P, sw.p, ns, side.tmax.p, side.beta.p, side.tsig.p,
+        EJ_TRY(launch_gram16(gs, gs, P, sw.p, ns, side.cmax.p, side.beta.p, side.tsig.p,
                              side.sig.p, false, J.counts, nullptr, 0, est.p, nullptr, J.sms, J.s));
         DevStatus h;
         EJ_CUDA(cudaMemcpyAsync(&h, est.p, sizeof h, cudaMemcpyDeviceToHost, J.s));
@@ -1091,7 +1091,7 @@ static int cross_join(Join& J, const double* Xq, uint64_t nq, int prec, int32_t*
             Jq.counts = qcounts;
             const GramSide A{sq.operands(P), sq.Aug.p, npq}, B{sx.operands(P), sx.Aug.p, npx};
             auto screen = [&](BandPair* band, uint64_t cap, DevStatus* st) {
-                return launch_gram16(A, B, P, work.p, nwork, sx.tmax.p, sq.beta.p, sx.tsig.p,
+                return launch_gram16(A, B, P, work.p, nwork, sx.cmax.p, sq.beta.p, sx.tsig.p,
                                      sq.sig.p, true, qcounts, reinterpret_cast<BandRec*>(band), cap,
                                      st, nullptr, J.sms, J.s);
             };

@@ -340,20 +340,21 @@ struct GramSide {
     const void* aug;
     uint64_t n_pad;
 };
-// Rows of A against columns of B over the blocks of the work list.  tmax_b:
-// per 128-row tile of B, max beta; beta_a: per row of A; FP8: tsig_b / sig_a
+// Rows of A against columns of B over the blocks of the work list.  cmax_b:
+// per 32-row chunk of B, max beta; beta_a: per row of A; FP8: tsig_b / sig_a
 // per-tile minimum / per-row scales.  cross: A and B are different point
 // sets (only A's rows are counted, every block as a diagonal one); else A is
 // B and the upper-triangle blocks credit both sides.
 int launch_gram16(const GramSide& A, const GramSide& B, const ScreenParams& P, const uint2* work,
-                  uint64_t nwork, const float* tmax_b, const float* beta_a, const float* tsig_b,
+                  uint64_t nwork, const float* cmax_b, const float* beta_a, const float* tsig_b,
                   const float* sig_a, bool cross, int32_t* counts, BandRec* band, uint64_t band_cap,
                   DevStatus* st, const Emit* em, int num_sms, cudaStream_t s);
 
 // k_misc.cu
-// Ordered list of 128 x 256 blocks (row tile I, column tiles 2p, 2p+1)
+// Ordered list of 128 x 256 blocks (row tile I, column tiles Ja, Jb)
 // covering the upper-triangle tile pairs (I <= J < nTa), grouped by
-// super-block pairs; entry = (I, p | active-half mask << 30).  With `boxes`,
+// super-block pairs; entry = (I | active-half mask << 30, Ja | (Jb - Ja) << 24);
+// a row's active tiles within a super-block are paired.  With `boxes`,
 // tile pairs whose squared box gap exceeds thr are inactive (super-block
 // pairs are dropped first).  ntiles_out: active 128 x 128 tile pairs.
 int build_worklist(uint64_t nT, uint64_t nTa, const LearnedBoxes* boxes, float thr,
@@ -456,8 +457,7 @@ int launch_pack8(const float* Y32, const float* Yerr, uint64_t n, uint64_t n_pad
                  const uint32_t* perm, const uint8_t* bad, const ScreenParams& P, uint8_t* Q,
                  void* Aug, float* beta, float* sig, float* Xf, float* rad, float* tsig,
                  cudaStream_t s);
-// per 128-row tile: max of beta (16-bit) or of meta.z (FP8), as float
-int launch_tile_max(const float* beta, const float4* meta, uint64_t n_pad, float* tmax,
-                    cudaStream_t s);
+// per group of 32 rows: max of beta (the band width of a 32-column chunk)
+int launch_chunk_max(const float* beta, uint64_t n_pad, float* cmax, cudaStream_t s);
 
 }  // namespace ejoin

@@ -1,12 +1,16 @@
 // k_misc.cu -- tile-pair work lists, totals and count scatter.
 //
-// Work list: blocks of one 128-row tile I x two 128-column tiles (2p, 2p+1)
+// Work list: blocks of one 128-row tile I x two 128-column tiles (Ja, Jb)
 // covering the upper-triangle tile pairs (I <= J), in a blocked order --
 // super-blocks of SB x SB tiles, super-blocks in row-major triangular order
 // -- so that the CTAs running concurrently touch a few MB of operand rows
 // that stay resident in L2.  Each entry carries a 2-bit mask of its active
-// halves (J = 2p + h in the upper triangle, below the last data tile, and not
+// halves (tile pairs in the upper triangle, below the last data tile, and not
 // proven empty by the learned projection; see k_learn.cu for the bound).
+// The two column tiles of a block need not be adjacent: a row's active tiles
+// within a super-block are paired, so that a block's second half is inactive
+// only for the row's last, odd tile (a 128 x 128 MMA costs as much as a
+// 128 x 256 one, so two lone tiles in one block halve their cost).
 #include <cub/cub.cuh>
 
 #include "ejoin_internal.cuh"
@@ -60,8 +64,14 @@ __global__ void superpairs_kernel(uint64_t nS, BoxArgs b, uint32_t* out, unsigne
     if (keep) out[base + __popc(m & ((1u << lane) - 1u))] = (uint32_t)sp;
 }
 
-// One block of SB * SB / 2 threads per surviving super-block pair: its
-// (I, column pair) blocks with at least one active half, in row-major order.
+// One block of SB * SB / 2 threads per surviving super-block pair.  Thread
+// (r, pp) tests the tile pairs (I, 2 pp') and (I, 2 pp' + 1) of row tile
+// I = SI SB + r (pp' = SJ SB / 2 + pp); the up to 16 active column tiles of
+// row I in this super-block (gathered from its 8 threads with two ballots)
+// are paired in ascending order, and thread pp of the row emits the pp-th
+// pair as one 128 x 256 block, a lone last tile with an inactive second
+// half.  Entry: x = I | active mask << 30, y = Ja | (Jb - Ja) << 24 (half 0
+// is column tile Ja, half 1 is Jb; Jb = Ja when half 1 is inactive).
 // count[0] += blocks, count[1] += active halves (128x128 tile pairs).
 constexpr uint32_t EXPAND_THREADS = SB * SB / 2;
 __global__ void __launch_bounds__(EXPAND_THREADS) expand_kernel(const uint32_t* __restrict__ sps,
@@ -80,18 +90,38 @@ __global__ void __launch_bounds__(EXPAND_THREADS) expand_kernel(const uint32_t* 
         hsum = 0;
     }
     __syncthreads();
+    const uint32_t pp = threadIdx.x % (SB / 2);
     const uint64_t I = sSI * SB + threadIdx.x / (SB / 2);
-    const uint64_t p = sSJ * (SB / 2) + threadIdx.x % (SB / 2);
+    const uint64_t J0 = sSJ * SB;  // first column tile of the super-block
     uint32_t mask = 0;
     for (uint32_t h = 0; h < 2; ++h) {
-        const uint64_t J = 2 * p + h;
+        const uint64_t J = J0 + 2 * pp + h;
         bool act = I < nTa && J < nTa && I <= J;
         if (act && b.lo) act = !boxes_far(b.lo, b.hi, I, J, b.k, b.thr);
         mask |= act ? (1u << h) : 0u;
     }
-    const bool keep = mask != 0;
-    const unsigned m = __ballot_sync(0xffffffffu, keep);
+    // the row's active tiles: 8 lanes of the warp hold 2 bits each
     const unsigned lane = threadIdx.x & 31, wid = threadIdx.x / 32;
+    const unsigned g0 = __ballot_sync(0xffffffffu, mask & 1u), g1 = __ballot_sync(0xffffffffu, mask & 2u);
+    const unsigned sh = lane & ~7u;  // first lane of this row's 8
+    uint32_t act16 = 0;
+#pragma unroll
+    for (uint32_t t = 0; t < 8; ++t)
+        act16 |= (((g0 >> (sh + t)) & 1u) << (2 * t)) | (((g1 >> (sh + t)) & 1u) << (2 * t + 1));
+    const uint32_t nact = __popc(act16);
+    const bool keep = pp < (nact + 1) / 2;
+    uint2 entry = make_uint2(0u, 0u);
+    if (keep) {
+        uint32_t m = act16;
+        for (uint32_t k = 0; k < 2 * pp; ++k) m &= m - 1;  // drop the first 2 pp tiles
+        const uint32_t ta = __ffs(m) - 1;
+        m &= m - 1;
+        const bool two = m != 0;
+        const uint32_t tb = two ? __ffs(m) - 1 : ta;
+        const uint32_t bmask = two ? 3u : 1u;
+        entry = make_uint2((uint32_t)I | (bmask << 30), (uint32_t)(J0 + ta) | ((tb - ta) << 24));
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, keep);
     if (lane == 0) wsum[wid] = __popc(m);
     const unsigned halves = __reduce_add_sync(0xffffffffu, __popc(mask));
     if (lane == 0 && halves) atomicAdd(&hsum, halves);
@@ -107,9 +137,7 @@ __global__ void __launch_bounds__(EXPAND_THREADS) expand_kernel(const uint32_t* 
         if (hsum) atomicAdd(&count[1], (unsigned long long)hsum);
     }
     __syncthreads();
-    if (keep)
-        out[sbase + wsum[wid] + __popc(m & ((1u << lane) - 1u))] =
-            make_uint2((uint32_t)I, (uint32_t)p | (mask << 30));
+    if (keep) out[sbase + wsum[wid] + __popc(m & ((1u << lane) - 1u))] = entry;
 }
 
 // Work list of a join of two point sets (rows: nTa tiles of A, columns: the
@@ -128,7 +156,7 @@ __global__ void cross_work_kernel(uint64_t nTa, uint64_t nTb, uint64_t total, ui
     const uint64_t pw = min((uint64_t)8, npb - SP * 8);
     const uint64_t I = SI * 16 + rem2 / pw, p = SP * 8 + rem2 % pw;
     const uint32_t mask = 1u | (2 * p + 1 < nTb ? 2u : 0u);
-    out[e] = make_uint2((uint32_t)I, (uint32_t)p | (mask << 30));
+    out[e] = make_uint2((uint32_t)I | (mask << 30), (uint32_t)(2 * p) | (1u << 24));
 }
 
 // Band records -> pairs: a thread per record; block-level exclusive scan of

@@ -705,24 +705,13 @@ __global__ void tile_min_sigma_kernel(const float* __restrict__ sig, uint64_t nt
     }
 }
 
-__global__ void tile_max_kernel(const float* __restrict__ beta, const float4* __restrict__ meta,
-                                uint64_t ntiles, float* tmax) {
-    const uint64_t t = blockIdx.x;
-    if (t >= ntiles) return;
-    float m = 0.0f;  // pad / bad rows carry 0
-    for (int r = threadIdx.x; r < 128; r += blockDim.x) {
-        float v = beta ? beta[t * 128 + r] : meta[t * 128 + r].z;
-        m = fmaxf(m, v);
-    }
+// Maximum of beta over every group of 32 consecutive rows (the column chunks
+// of the Gram epilogue): a thread per row, one warp per group.
+__global__ void chunk_max_kernel(const float* __restrict__ beta, uint64_t n_pad, float* cmax) {
+    const uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    float m = r < n_pad ? beta[r] : 0.0f;  // pad / bad rows carry 0
     for (int o = 16; o; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-    __shared__ float sm[4];
-    if ((threadIdx.x & 31) == 0) sm[threadIdx.x / 32] = m;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        float r = sm[0];
-        for (int w = 1; w < (int)(blockDim.x / 32); ++w) r = fmaxf(r, sm[w]);
-        tmax[t] = r;
-    }
+    if ((threadIdx.x & 31) == 0 && r < n_pad) cmax[r / 32] = m;
 }
 
 }  // namespace
@@ -911,11 +900,10 @@ int launch_pack8(const float* Y32, const float* Yerr, uint64_t n, uint64_t n_pad
     return EJOIN_OK;
 }
 
-int launch_tile_max(const float* beta, const float4* meta, uint64_t n_pad, float* tmax,
-                    cudaStream_t s) {
-    const uint64_t nt = n_pad / 128;
-    if (nt == 0) return EJOIN_OK;
-    tile_max_kernel<<<(unsigned)nt, 128, 0, s>>>(beta, meta, nt, tmax);
+int launch_chunk_max(const float* beta, uint64_t n_pad, float* cmax, cudaStream_t s) {
+    if (n_pad % 32) return set_error(EJOIN_EINTERNAL, "chunk max: rows not padded");
+    if (n_pad == 0) return EJOIN_OK;
+    chunk_max_kernel<<<(unsigned)((n_pad + 255) / 256), 256, 0, s>>>(beta, n_pad, cmax);
     EJ_CUDA(cudaGetLastError());
     note_launch();
     return EJOIN_OK;

@@ -8,13 +8,15 @@
 // sqrt(|d2|) <= eps.  Here:
 //
 //  * A persistent CTA per SM walks a list of blocks of 128 rows (row tile I)
-//    x 256 columns (column tiles 2p, 2p+1), taking runs of consecutive list
+//    x 256 columns (two column tiles Ja, Jb, not necessarily adjacent: the
+//    B slab is loaded as two 128-row boxes), taking runs of consecutive list
 //    entries.  Each 128x128 half carries an "active" bit: it lies in the
-//    upper triangle (2p + h >= I) and was not pruned; inactive halves are
-//    computed but ignored.  N = 256 per MMA instruction: on GB300 a
-//    tcgen05.mma of 128x256x16 takes about as long to issue and retire as
-//    one of 128x128x16 (measured: 1.8 vs 0.92 PFLOP/s through the same TMA /
-//    MMA pipeline), so the wide tile doubles the tensor-pipe throughput.
+//    upper triangle (J >= I) and was not pruned; an inactive half (a row's
+//    odd last tile) is computed but ignored.  N = 256 per MMA instruction: on
+//    GB300 a tcgen05.mma of 128x256x16 takes about as long to issue and
+//    retire as one of 128x128x16 (measured: 1.8 vs 0.92 PFLOP/s through the
+//    same TMA / MMA pipeline), so the wide tile doubles the tensor-pipe
+//    throughput, and pairing lone tiles halves their cost.
 //  * Warp 0 streams the K-slabs of both blocks into a 4-stage ring with TMA
 //    (128-byte swizzle; a 128-row A slab and a 256-row B slab per stage; the
 //    aug boxes of a block go to a separate 2-slot ring).  Four stages in
@@ -29,10 +31,11 @@
 //    + lo*hi.  The aug MMA adds -alpha_i - alpha_j, so the accumulator holds
 //    C_ij = q_i.q_j - alpha_i - alpha_j and the rigorous screen is a sign test:
 //        C >= 0          pair certainly within eps        (counted)
-//        C < -W_iJ       pair certainly outside eps
+//        C < -W_iK       pair certainly outside eps
 //        otherwise       band: queued for the FP64 recheck
-//    W_iJ = beta_i + max beta over tile J >= beta_i + beta_j (one value per
-//    row and column tile, so the test costs the same as a tile-wide width).
+//    W_iK = beta_i + max beta over the 32-column chunk K >= beta_i + beta_j
+//    (one value per row and column chunk, so the test costs one add per
+//    element, like a tile-wide width, with a narrower band).
 //  * Each epilogue warp reads its two 32x32 chunks one after the other with
 //    tcgen05.ld.red (the load also returns each lane's maximum, which decides
 //    the all-out fast path), packs sign bits with one funnel shift per
@@ -67,14 +70,21 @@ constexpr uint32_t ACC_COLS = 256;         // one 128x256 FP32 accumulator
 constexpr uint32_t TMEM_COLS = 2 * ACC_COLS;
 constexpr uint32_t FULL = 0xffffffffu;
 
-// Work-list entry: x = row tile I; y = column pair p | active mask << 30
-// (bit h: the 128x128 half with column tile 2p + h is computed).
-constexpr uint32_t kPairMask = (1u << 30) - 1u;
+// Work-list entry: x = row tile I | active mask << 30, y = Ja | (Jb - Ja) << 24:
+// half 0 of the block is column tile Ja, half 1 is Jb (bit h of the mask:
+// half h is computed).
+constexpr uint32_t kRowMask = (1u << 30) - 1u;
+__device__ __forceinline__ uint32_t e_row(uint2 e) { return e.x & kRowMask; }
+__device__ __forceinline__ uint32_t e_mask(uint2 e) { return e.x >> 30; }
+__device__ __forceinline__ uint32_t e_col(uint2 e, uint32_t h) {
+    const uint32_t ja = e.y & 0xffffffu;
+    return h ? ja + ((e.y >> 24) & 63u) : ja;
+}
 
 struct GramArgs {
     const uint2* work;
     uint64_t nwork;
-    const float* tmax;  // per 128-row tile: max beta
+    const float* cmax;  // per 32-row chunk of B: max beta
     const float* beta;  // per row: beta (out margin, Gram units)
     const float* tsig;  // FP8: per-tile minimum row scale (null for 16-bit operands)
     const float* sig;   // FP8: per-row scale
@@ -317,8 +327,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 if (u >= a.nwork) break;
                 const uint2 w = wnext;
                 wnext = entry_or_end(a, item_at(idx + 1, a.lrun));
-                const int32_t ya = (int32_t)(w.x * 128u);
-                const int32_t yb = (int32_t)((w.y & kPairMask) * 256u);
+                const int32_t ya = (int32_t)(e_row(w) * 128u);
+                const int32_t yb0 = (int32_t)(e_col(w, 0) * 128u), yb1 = (int32_t)(e_col(w, 1) * 128u);
                 {
                     // this block's aug boxes
                     const uint32_t g = (uint32_t)(idx % NAUG), guse = (uint32_t)(idx / NAUG);
@@ -326,7 +336,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                     uint8_t* sg = augs + (size_t)g * AUG_SLOT;
                     ptx::mbar_arrive_expect_tx(&S.gfull[g], AUG_SLOT);
                     ptx::tma_load_2d(sg, &taa, 0, ya, &S.gfull[g]);
-                    ptx::tma_load_2d(sg + AUG_A, &tab, 16, yb, &S.gfull[g]);
+                    ptx::tma_load_2d(sg + AUG_A, &tab, 16, yb0, &S.gfull[g]);
+                    ptx::tma_load_2d(sg + AUG_A + AUG_B / 2, &tab, 16, yb1, &S.gfull[g]);
                     aug_ph[g] = guse & 1u;
                     ++aug_issued;
                 }
@@ -342,7 +353,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                     } else {
                         ptx::mbar_arrive_expect_tx(&S.full[st], DATA_TX);
                         ptx::tma_load_2d(sa, &tqa, x, ya, &S.full[st]);
-                        ptx::tma_load_2d(sa + SLAB_A, &tqb, x, yb, &S.full[st]);
+                        ptx::tma_load_2d(sa + SLAB_A, &tqb, x, yb0, &S.full[st]);
+                        ptx::tma_load_2d(sa + SLAB_A + SLAB_B / 2, &tqb, x, yb1, &S.full[st]);
                         issued_ph[st] = ph;
                         ++issued;
                     }
@@ -436,7 +448,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     } else if (warp < FLUSH_WARP) {
         // ------------------------------------------------ epilogue warps
         // warp e reads lane quarter (warp % 4) and the 64 columns 64 * (e / 4),
-        // which lie in half h = e / 8 (column tile 2p + h)
+        // which lie in half h = e / 8 (column tile Ja or Jb)
         const uint32_t ew = warp - 2;          // 0..15
         const uint32_t q = warp & 3u;          // tensor-memory lane quarter
         const uint32_t cg = ew >> 2;           // 64-column group
@@ -451,16 +463,18 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         // block ahead, both consumed a block later, so no global-load latency
         // lands on a block's own path.
         struct Margins {
-            float b, t, sr, st;
+            float b, t0, t1, sr, st;
             bool on;
         };
         auto load_margins = [&](uint2 e) -> Margins {
-            Margins m{0.0f, 0.0f, 1.0f, 1.0f, false};
-            if (e.x != 0xffffffffu && ((e.y >> (30 + h)) & 1u)) {
-                const uint32_t Je = 2u * (e.y & kPairMask) + h;
-                const uint32_t r = e.x * 128u + q * 32u + lane;
+            Margins m{0.0f, 0.0f, 0.0f, 1.0f, 1.0f, false};
+            if (e.x != 0xffffffffu && ((e_mask(e) >> h) & 1u)) {
+                const uint32_t Je = e_col(e, h);
+                const uint32_t r = e_row(e) * 128u + q * 32u + lane;
+                const uint32_t c = (Je * 128u + (cg & 1u) * 64u) / 32u;  // first chunk
                 m.b = __ldg(&a.beta[r]);
-                m.t = __ldg(&a.tmax[Je]);
+                m.t0 = __ldg(&a.cmax[c]);
+                m.t1 = __ldg(&a.cmax[c + 1]);
                 if (OPK) {
                     m.sr = __ldg(&a.sig[r]);
                     m.st = __ldg(&a.tsig[Je]);
@@ -469,17 +483,20 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             }
             return m;
         };
-        auto width = [&](const Margins& m) -> float {
+        // chunk k (0, 1) of the warp's 64 columns: W >= beta_i + max beta over
+        // the chunk's 32 columns
+        auto width = [&](const Margins& m, int k) -> float {
             if (!m.on) return 0.0f;
-            const float sm = m.b + m.t;
+            const float sm = m.b + (k ? m.t1 : m.t0);
             float Wv = fmaf(fabsf(sm), 9.5367431640625e-07f, sm);
             if (OPK) Wv = Wv / (m.sr * m.st);
             return Wv;
         };
         uint2 w = entry_or_end(a, item_at(0, a.lrun));
         uint2 wn = entry_or_end(a, item_at(1, a.lrun));
-        float W = width(load_margins(w));
-        auto is_active = [&](uint2 e) { return e.x != 0xffffffffu && ((e.y >> (30 + h)) & 1u); };
+        Margins mc = load_margins(w);
+        float W0 = width(mc, 0), W1 = width(mc, 1);
+        auto is_active = [&](uint2 e) { return e.x != 0xffffffffu && ((e_mask(e) >> h) & 1u); };
         // Software pipeline: the first 32-column chunk of block idx + 1 is
         // loaded from tensor memory before the counting work of block idx, so
         // the load's latency hides behind that work.  v holds the chunk in
@@ -499,7 +516,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             const uint32_t b = it & 1u, use = it >> 1;
             const uint2 wnn = entry_or_end(a, item_at(idx + 2, a.lrun));
             const Margins mn = load_margins(wn);
-            const uint32_t I = w.x, p = w.y & kPairMask, J = 2u * p + h;
+            const uint32_t I = e_row(w), J = e_col(w, h);
             const bool active = is_active(w);
             const bool diag = a.cross || (I == J);  // credit rows only
             // the two 32-column chunks one after the other (32 live values);
@@ -509,14 +526,14 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             bool busy0 = false, busy1 = false;
             if (active) {
                 ptx::tmem_ld_wait_regs(v, mx);
-                busy0 = classify(v, mx, W, in0, bd0);
+                busy0 = classify(v, mx, W0, in0, bd0);
                 ptx::tmem_ld_max_32x32b_x32(taddr + 32u, v, mx);
                 ptx::tmem_ld_wait_regs(v, mx);
             }
             ptx::tc_fence_before();
             __syncwarp();
             if (lane == 0) ptx::mbar_arrive(&S.tempty[b]);
-            if (active) busy1 = classify(v, mx, W, in1, bd1);
+            if (active) busy1 = classify(v, mx, W1, in1, bd1);
             // next block: wait for its accumulator, start its first load
             const bool more = item_at(idx + 1, a.lrun) < a.nwork;
             if (more) {
@@ -531,7 +548,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 int* racc = S.rowacc[b];
                 int* cacc = S.colacc[b];
                 const uint32_t row = I * 128u + q * 32u + lane;
-                const uint32_t col0 = p * 256u + cg * 64u;
+                const uint32_t col0 = J * 128u + (cg & 1u) * 64u;
                 if (__any_sync(FULL, (bd0 | bd1) != 0)) stage_band(a, S, b, bd0, bd1, row, col0, diag, lane);
                 if (!diag) {
                     col_counts(in0, cacc + cg * 64u, lane);
@@ -543,7 +560,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             }
             __syncwarp();
             if (lane == 0) ptx::mbar_arrive(&S.ebar[b]);
-            W = width(mn);
+            W0 = width(mn, 0);
+            W1 = width(mn, 1);
             w = wn;
             wn = wnn;
             run = more;
@@ -574,19 +592,19 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             if (!ptx::mbar_wait(&S.ebar[b], use & 1u, a.st, 40)) break;
             int* racc = S.rowacc[b];
             int* cacc = S.colacc[b];
-            const uint32_t col_base = (w.y & kPairMask) * 256u;
+            const uint32_t col_a = e_col(w, 0) * 128u, col_b = e_col(w, 1) * 128u;
 #pragma unroll
             for (int e = 0; e < 4; ++e) {
                 const uint32_t r = lane + 32 * e;
                 const int rv = racc[r];
-                if (rv) atomicAdd(&a.counts[w.x * 128u + r], rv);
+                if (rv) atomicAdd(&a.counts[e_row(w) * 128u + r], rv);
                 racc[r] = 0;
             }
 #pragma unroll
             for (int e = 0; e < 8; ++e) {
                 const uint32_t c = lane + 32 * e;
                 const int cv = cacc[c];
-                if (cv) atomicAdd(&a.counts[col_base + c], cv);
+                if (cv) atomicAdd(&a.counts[(c < 128u ? col_a : col_b - 128u) + c], cv);
                 cacc[c] = 0;
             }
             // staged band records of this block: one global reservation, coalesced
@@ -642,7 +660,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 }  // namespace
 
 int launch_gram16(const GramSide& A, const GramSide& B, const ScreenParams& P, const uint2* work,
-                  uint64_t nwork, const float* tmax, const float* beta, const float* tsig,
+                  uint64_t nwork, const float* cmax, const float* beta, const float* tsig,
                   const float* sig, bool cross, int32_t* counts, BandRec* band, uint64_t band_cap,
                   DevStatus* st, const Emit* em, int num_sms, cudaStream_t s) {
     if (nwork == 0) return EJOIN_OK;
@@ -656,23 +674,23 @@ int launch_gram16(const GramSide& A, const GramSide& B, const ScreenParams& P, c
         P.fmt == Fmt::FP16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
     if (fp8) {
         EJ_TRY(make_tmap_2d(&ma, A.Q, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, P.width, A.n_pad, 128, 128));
-        EJ_TRY(make_tmap_2d(&mb, B.Q, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, P.width, B.n_pad, 128, 256));
+        EJ_TRY(make_tmap_2d(&mb, B.Q, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, P.width, B.n_pad, 128, 128));
     } else {
         EJ_TRY(make_tmap_2d(&ma, A.Q, adt, 2, P.width, A.n_pad, 64, 128));
-        EJ_TRY(make_tmap_2d(&mb, B.Q, adt, 2, P.width, B.n_pad, 64, 256));
+        EJ_TRY(make_tmap_2d(&mb, B.Q, adt, 2, P.width, B.n_pad, 64, 128));
     }
     EJ_TRY(make_tmap_2d(&maa, A.aug, adt, 2, 32, A.n_pad, 16, 128));
-    EJ_TRY(make_tmap_2d(&mab, B.aug, adt, 2, 32, B.n_pad, 16, 256));
+    EJ_TRY(make_tmap_2d(&mab, B.aug, adt, 2, 32, B.n_pad, 16, 128));
     GramArgs a;
     a.work = work;
     a.nwork = nwork;
-    a.tmax = tmax;
+    a.cmax = cmax;
     a.beta = beta;
     a.tsig = fp8 ? tsig : nullptr;
     a.sig = fp8 ? sig : nullptr;
     a.em = em ? *em : Emit{nullptr, 0, nullptr, 0, nullptr};
     a.cross = cross ? 1u : 0u;
-    if (!tmax || !beta || (fp8 && (!tsig || !sig))) return set_error(EJOIN_EINTERNAL, "gram: margins missing");
+    if (!cmax || !beta || (fp8 && (!tsig || !sig))) return set_error(EJOIN_EINTERNAL, "gram: margins missing");
     a.counts = counts;
     a.band = band;
     a.band_cap = band_cap;
