@@ -550,8 +550,31 @@ static ScreenParams screen_params(Fmt fmt, bool split, uint32_t d, double maxabs
     P.sTlo = sqrt(P.Tlo) * (1 - 4 * kU);
     P.sThi = sqrt(P.Thi) * (1 + 4 * kU);
     const double kprod = (split ? 3.0 : 1.0) * P.dp + 16.0;  // + the aug K = 16 step
+    // Accumulation bound.  Model of one tcgen05.mma of K_t products (K_t = 16
+    // for the 16-bit kinds, 32 for E4M3) into an FP32 accumulator:
+    //   S_t = S_{t-1} + sum_t p + e_t,  |e_t| <= K_t 2^-22 (|S_{t-1}| + sum_t |p|),
+    // twice the error of K_t truncating FP32 additions, each charged with the
+    // magnitude of all that was accumulated up to the end of the instruction;
+    // 16 2^-22 of the total magnitude more covers the final value.  MMAs into
+    // one accumulator act in issue order (D = A B + D), and the issuer
+    // (k_umma.cu) orders them by magnitude: with the split, the hi*lo and
+    // lo*hi products of the first K-slab (128 products, everything so far
+    // <= L_ij = sum |hi_i lo_j| + |lo_i hi_j|), then every other data product
+    // (<= L_ij + H_ij <= a_i a_j, a = |(|hi| + |lo|)|), then the aug step
+    // (<= a_i a_j + |alpha_i| + |alpha_j|).  So
+    //   |err| <= 2^-22 [128 L_ij + c_h a_i a_j + 32 (|alpha_i| + |alpha_j|)],
+    //   c_h = 64 + 192 (slabs - 1) + 16 + 16 with the split, dp + 16 + 16 without,
+    // and a_i a_j <= (a_i^2 + a_j^2) / 2, L_ij <= a_i l_j + l_i a_j
+    // <= 2^-9 (a_i^2 + a_j^2) / 2 + 2^9 (l_i^2 + l_j^2) / 2 split it into the
+    // per-row terms of acc_margin2.  (Charging every product with the total
+    // instead gives the coarser (kprod + 16) 2^-22 (a_i a_j + |alpha_i| +
+    // |alpha_j|), which this bound never exceeds.)
     const double scale_opt = acc_bound_scale > 0 ? acc_bound_scale : 1.0;
-    P.cacc = scale_opt * (kprod + 16.0) * ldexp(1.0, -22);
+    const double slabs = P.dp / 64.0;
+    const double c_h = split ? 96.0 + 192.0 * (slabs - 1.0) : P.dp + 32.0;
+    P.cacc_a = scale_opt * c_h * ldexp(1.0, -22);
+    P.cacc_l = split ? scale_opt * 128.0 * ldexp(1.0, -22) : 0.0;
+    P.cacc_al = scale_opt * 32.0 * ldexp(1.0, -22);
     P.absacc = (kprod + 16.0) * ldexp(1.0, -125);
     P.clamp_lo = (fmt == Fmt::FP16) ? -16384.0 : -kTwo100;
     *kprod_out = kprod;

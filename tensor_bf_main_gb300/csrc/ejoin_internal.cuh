@@ -285,7 +285,9 @@ struct ScreenParams {
     double scale;      // s, a power of two
     double Tlo, Thi;   // s^2 * T_lo, s^2 * T_hi (oracle rounding folded in)
     double sTlo, sThi; // sqrt(Tlo) rounded down, sqrt(Thi) rounded up
-    double cacc;       // relative bound of the tensor-core accumulation error
+    // tensor-core accumulation error of C_ij: |err| <= e_i + e_j with
+    // 2 e_i = acc_margin2(a_i^2, l_i^2) + 2 cacc_al |alpha_i| (api.cu: screen_params)
+    double cacc_a, cacc_l, cacc_al;
     double absacc;     // absolute bound (FP32 underflow) of the same
     double clamp_lo;   // smallest alpha the operand format can carry
     uint32_t d, dp;    // coordinates, padded coordinates (per slab multiple)
@@ -293,6 +295,13 @@ struct ScreenParams {
     int split;         // 1 = hi + lo products
     Fmt fmt;
 };
+
+// The row's share of the accumulation bound that does not depend on alpha,
+// doubled: cacc_a a^2 + cacc_l (2^-9 a^2 + 2^9 l^2), where a^2 bounds
+// |(|hi| + |lo|)|^2 and l^2 bounds |lo|^2 (0 without the split).
+__host__ __device__ __forceinline__ double acc_margin2(const ScreenParams& P, double a2, double l2) {
+    return P.cacc_a * a2 + P.cacc_l * (a2 * (1.0 / 512.0) + l2 * 512.0);
+}
 
 // Per-join constants of the FP64 DMMA screen (unscaled centred space y).
 struct DmmaParams {

@@ -497,9 +497,10 @@ __global__ void __launch_bounds__(256) pack16_kernel(const float* __restrict__ Y
                              1.1754943508222875e-38 * sqrt((double)P.d)) * (1 + 4 * kU);
         const double rho = (sqrt((double)m_e2) * (1 + 1e-7) + zerr) * (1 + 8 * kU);
         radius = __double2float_ru(zerr);
-        double R = nup + P.cacc * a2u + lu + P.absacc - 0.5 * P.Tlo + 2.0 * P.sTlo * rho;
-        R += 8 * kU * (nup + P.cacc * a2u + lu + P.absacc + 0.5 * P.Tlo + 2.0 * P.sTlo * rho);
-        double at = R >= 0 ? R / (2.0 * (1.0 - P.cacc)) : R / (2.0 * (1.0 + P.cacc));
+        const double m2 = acc_margin2(P, a2u, lu);
+        double R = nup + m2 + lu + P.absacc - 0.5 * P.Tlo + 2.0 * P.sTlo * rho;
+        R += 12 * kU * (nup + m2 + lu + P.absacc + 0.5 * P.Tlo + 2.0 * P.sTlo * rho);
+        double at = R >= 0 ? R / (2.0 * (1.0 - P.cacc_al)) : R / (2.0 * (1.0 + P.cacc_al));
         at += fabs(at) * 4 * kU;
         at = fmax(at, P.clamp_lo);
         ah[0] = round_fmt(at, fi);
@@ -509,9 +510,9 @@ __global__ void __launch_bounds__(256) pack16_kernel(const float* __restrict__ Y
         ah[2] = round_fmt_up(r2, fi);
         const double alpha = ah[0] + ah[1] + ah[2];  // >= at (ah[2] >= r2)
         b = 0.5 * P.Thi + 2.0 * P.sThi * rho + 2.0 * rho * rho - ndn + 2.0 * alpha +
-            P.cacc * (a2u + 2.0 * fabs(alpha)) + lu + P.absacc;
-        b += 8 * kU * (0.5 * P.Thi + 2.0 * P.sThi * rho + 2.0 * rho * rho + ndn + 2.0 * fabs(alpha) +
-                       P.cacc * (a2u + 2.0 * fabs(alpha)) + lu + P.absacc);
+            m2 + 2.0 * P.cacc_al * fabs(alpha) + lu + P.absacc;
+        b += 12 * kU * (0.5 * P.Thi + 2.0 * P.sThi * rho + 2.0 * rho * rho + ndn + 2.0 * fabs(alpha) +
+                        m2 + 2.0 * P.cacc_al * fabs(alpha) + lu + P.absacc);
         b *= 0.5;
     } else {
         // never in, never band: C = q_i.q_j - alpha_i - alpha_j << -W
@@ -639,9 +640,10 @@ __global__ void __launch_bounds__(256) pack8_kernel(const float* __restrict__ Y3
                              1.1754943508222875e-38 * sqrt((double)P.d)) * (1 + 4 * kU);
         const double rho = (sqrt((double)m_e2) * (1 + 1e-7) + zerr) * (1 + 8 * kU);
         radius = __double2float_ru(zerr);
-        double R = nup + P.cacc * a2u + P.absacc - 0.5 * P.Tlo + 2.0 * P.sTlo * rho;
-        R += 8 * kU * (nup + P.cacc * a2u + P.absacc + 0.5 * P.Tlo + 2.0 * P.sTlo * rho);
-        double at = R >= 0 ? R / (2.0 * (1.0 - P.cacc)) : R / (2.0 * (1.0 + P.cacc));
+        const double m2 = acc_margin2(P, a2u, 0.0);
+        double R = nup + m2 + P.absacc - 0.5 * P.Tlo + 2.0 * P.sTlo * rho;
+        R += 12 * kU * (nup + m2 + P.absacc + 0.5 * P.Tlo + 2.0 * P.sTlo * rho);
+        double at = R >= 0 ? R / (2.0 * (1.0 - P.cacc_al)) : R / (2.0 * (1.0 + P.cacc_al));
         at += fabs(at) * 4 * kU;
         rsig = 1.0 / (double)m_sig;  // exact
         double as = fmax(at * rsig, -kTwo100);  // alpha / sigma, clamped upwards (safe)
@@ -652,9 +654,9 @@ __global__ void __launch_bounds__(256) pack8_kernel(const float* __restrict__ Y3
         ah[2] = round_fmt_up(r2, bf);
         const double alpha = (ah[0] + ah[1] + ah[2]) * (double)m_sig;  // >= at
         b = 0.5 * P.Thi + 2.0 * P.sThi * rho + 2.0 * rho * rho - ndn + 2.0 * alpha +
-            P.cacc * (a2u + 2.0 * fabs(alpha)) + P.absacc;
-        b += 8 * kU * (0.5 * P.Thi + 2.0 * P.sThi * rho + 2.0 * rho * rho + ndn + 2.0 * fabs(alpha) +
-                       P.cacc * (a2u + 2.0 * fabs(alpha)) + P.absacc);
+            m2 + 2.0 * P.cacc_al * fabs(alpha) + P.absacc;
+        b += 12 * kU * (0.5 * P.Thi + 2.0 * P.sThi * rho + 2.0 * rho * rho + ndn + 2.0 * fabs(alpha) +
+                        m2 + 2.0 * P.cacc_al * fabs(alpha) + P.absacc);
         b *= 0.5;
     } else {
         ah[0] = kTwo100;  // never in, never band

@@ -400,6 +400,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 if (!ptx::mbar_wait(&S.tempty[b], (use & 1u) ^ 1u, a.st, 21)) break;
                 ptx::tc_fence_after();
                 const uint32_t d_tmem = tmem + b * ACC_COLS;
+                // Order by magnitude (the accumulation bound of screen_params
+                // in api.cu relies on it): the first slab's hi*lo and lo*hi
+                // products, then the hi*hi ones, then the later slabs, and
+                // the aug step (-alpha_i - alpha_j) last.
                 uint32_t acc = 0;
                 for (uint32_t c = 0; c < a.nhi && ok; ++c) {
                     uint32_t s_hi, s_lo = 0;
@@ -409,36 +413,40 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                     uint8_t* st_hi = stages + (size_t)s_hi * STAGE_BYTES;
                     const uint64_t ah = ptx::sdesc_sw128(ptx::smem_u32(st_hi));
                     const uint64_t bh = ptx::sdesc_sw128(ptx::smem_u32(st_hi + SLAB_A));
-                    if (c == 0) {
-                        // aug: A side (alpha_i, -1) x B side (-1, alpha_j), one K = 16 step
-                        const uint32_t g = (uint32_t)(idx % NAUG), guse = (uint32_t)(idx / NAUG);
-                        if (!ptx::mbar_wait(&S.gfull[g], guse & 1u, a.st, 22)) { ok = false; break; }
-                        ptx::tc_fence_after();
-                        uint8_t* sg = augs + (size_t)g * AUG_SLOT;
-                        ptx::mma_f16(d_tmem, ptx::sdesc_sw32(ptx::smem_u32(sg)),
-                                     ptx::sdesc_sw32(ptx::smem_u32(sg + AUG_A)), idesc_aug, 0);
-                        ptx::mma_commit(&S.gempty[g]);
-                        acc = 1;
-                    }
                     if (a.split) {
                         uint8_t* st_lo = stages + (size_t)s_lo * STAGE_BYTES;
                         const uint64_t al = ptx::sdesc_sw128(ptx::smem_u32(st_lo));
                         const uint64_t bl = ptx::sdesc_sw128(ptx::smem_u32(st_lo + SLAB_A));
 #pragma unroll
                         for (uint32_t kk = 0; kk < 4; ++kk) {
-                            mma(d_tmem, ah + 2 * kk, bh + 2 * kk, acc);
-                            mma(d_tmem, ah + 2 * kk, bl + 2 * kk, 1);
+                            mma(d_tmem, ah + 2 * kk, bl + 2 * kk, acc);
                             mma(d_tmem, al + 2 * kk, bh + 2 * kk, 1);
+                            acc = 1;
                         }
+#pragma unroll
+                        for (uint32_t kk = 0; kk < 4; ++kk) mma(d_tmem, ah + 2 * kk, bh + 2 * kk, 1);
                         ptx::mma_commit(&S.empty[s_hi]);
                         ptx::mma_commit(&S.empty[s_lo]);
                     } else {
 #pragma unroll
-                        for (uint32_t kk = 0; kk < 4; ++kk) mma(d_tmem, ah + 2 * kk, bh + 2 * kk, acc);
+                        for (uint32_t kk = 0; kk < 4; ++kk) {
+                            mma(d_tmem, ah + 2 * kk, bh + 2 * kk, acc);
+                            acc = 1;
+                        }
                         ptx::mma_commit(&S.empty[s_hi]);
                     }
                 }
                 if (!ok) break;
+                {
+                    // aug: A side (alpha_i, -1) x B side (-1, alpha_j), one K = 16 step
+                    const uint32_t g = (uint32_t)(idx % NAUG), guse = (uint32_t)(idx / NAUG);
+                    if (!ptx::mbar_wait(&S.gfull[g], guse & 1u, a.st, 22)) break;
+                    ptx::tc_fence_after();
+                    uint8_t* sg = augs + (size_t)g * AUG_SLOT;
+                    ptx::mma_f16(d_tmem, ptx::sdesc_sw32(ptx::smem_u32(sg)),
+                                 ptx::sdesc_sw32(ptx::smem_u32(sg + AUG_A)), idesc_aug, acc);
+                    ptx::mma_commit(&S.gempty[g]);
+                }
                 ptx::mma_commit(&S.tfull[b]);
             }
             // drain: all MMAs complete before tensor memory is freed

@@ -95,6 +95,84 @@ def test_probe_accumulation_error_within_bound(probe):
     assert rel * 4 <= bound
 
 
+def prefix_model_bound(af, bf, kstep):
+    """The screen's per-instruction accumulation model: instruction t (kstep
+    products, issued in K order) errs by at most kstep 2^-22 times the sum of
+    |products| accumulated up to its end, plus 16 2^-22 of the total."""
+    K = af.shape[1]
+    prefix = np.zeros((af.shape[0], bf.shape[0]))
+    total = np.zeros_like(prefix)
+    for t in range(K // kstep):
+        sl = slice(t * kstep, (t + 1) * kstep)
+        prefix += np.abs(af[:, sl]) @ np.abs(bf[:, sl]).T
+        total += kstep * prefix
+    return (total + 16 * prefix) * 2.0 ** -22
+
+
+def magnitude_pattern(rng, pattern, K):
+    """Per-coordinate exponent offsets for the prefix-model probes."""
+    s = np.zeros(K)
+    if pattern == "small_then_large":    # the split screen's order: lo products first
+        s[: K // 2] = -9
+    elif pattern == "large_last":        # one big instruction at the end (the aug step)
+        s[: K - 16] = -10
+    elif pattern == "ramp":              # magnitudes growing along K
+        s = np.floor(np.linspace(-14, 0, K))
+    elif pattern == "large_first":
+        s[16:] = -8
+    return 2.0 ** s
+
+
+@pytest.mark.parametrize("pattern", ["small_then_large", "large_last", "ramp", "large_first"])
+@pytest.mark.parametrize("fmt", [0, 1])
+def test_probe_accumulation_prefix_model(probe, fmt, pattern):
+    """The bound the screen's margins use (api.cu screen_params): every
+    observed error, with small products issued before large ones and with
+    signs that cancel, stays a factor >= 4 inside the per-instruction model."""
+    rng = np.random.default_rng(100 + fmt * 10 + len(pattern))
+    K = 256
+    m = magnitude_pattern(rng, pattern, K)
+    a = (rng.standard_normal((128, K)) * m).astype(np.float32)
+    b = (rng.standard_normal((128, K)) * m).astype(np.float32)
+    # rows 64..: b_j = -a_j on the last 16 coordinates, so the last
+    # instruction of pair (j, j) only subtracts
+    b[64:, K - 16:] = -a[64:, K - 16:]
+    if fmt == 1:
+        A, B = f32_to_bf16_bits(a), f32_to_bf16_bits(b)
+        af, bf = bf16_bits_to_f64(A), bf16_bits_to_f64(B)
+    else:
+        # the screen stores no subnormal operand (the packer flushes them)
+        a16, b16 = a.astype(np.float16), b.astype(np.float16)
+        a16[np.abs(a16) < 2.0 ** -14] = 0
+        b16[np.abs(b16) < 2.0 ** -14] = 0
+        A, B = a16.view(np.uint16), b16.view(np.uint16)
+        af, bf = a16.astype(np.float64), b16.astype(np.float64)
+    D = probe(np.ascontiguousarray(A), np.ascontiguousarray(B), K // 64, fmt, 0)
+    err = np.abs(D - af @ bf.T)
+    bound = prefix_model_bound(af, bf, 16)
+    worst = float((err / bound).max())
+    print(f"{pattern} fmt {fmt}: max error / model bound = {worst:.3e}")
+    assert worst * 4 <= 1.0
+
+
+@pytest.mark.parametrize("pattern", ["small_then_large", "large_last", "ramp"])
+def test_probe_fp8_accumulation_prefix_model(probe, pattern):
+    rng = np.random.default_rng(200 + len(pattern))
+    K = 256
+    lo_hi = {"small_then_large": [(-6, -4)] * 4 + [(2, 5)] * 4,
+             "large_last": [(-6, -5)] * 7 + [(5, 7)],
+             "ramp": [(-6 + i, -5 + i) for i in range(8)]}[pattern]
+    A = np.concatenate([random_e4m3(rng, (128, 32), l, h) for l, h in lo_hi], axis=1)
+    B = np.concatenate([random_e4m3(rng, (128, 32), l, h) for l, h in lo_hi], axis=1)
+    af, bf = e4m3_decode(A), e4m3_decode(B)
+    D = probe(np.ascontiguousarray(A), np.ascontiguousarray(B), K // 128, 2, 0)
+    err = np.abs(D - af @ bf.T)
+    bound = prefix_model_bound(af, bf, 32)
+    worst = float((err / bound).max())
+    print(f"FP8 {pattern}: max error / model bound = {worst:.3e}")
+    assert worst * 4 <= 1.0
+
+
 @pytest.mark.parametrize("fmt", [0, 1])
 def test_probe_sw32_aug_tiles(probe, fmt):
     """The aug operands: [rows][32] 16-bit arrays, A = columns 0..15 and
