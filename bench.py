@@ -375,6 +375,8 @@ def run_ours(args):
         "tile_pairs_run": stats[-1]["tile_pairs_run"],
         "gram_blocks": stats[-1].get("gram_blocks", 0),
         "exact_rechecks": stats[-1].get("exact_rechecks", 0),
+        "band_records": stats[-1].get("band_records", 0),
+        "scratch_peak_bytes": stats[-1].get("scratch_peak_bytes", 0),
         "tile_pairs_total": stats[-1]["tile_pairs_total"],
         "phase_ms": {k: stats[-1][k] for k in ("ms_prep", "ms_train", "ms_order", "ms_gram",
                                                 "ms_recheck", "ms_total")},

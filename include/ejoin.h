@@ -115,6 +115,8 @@ typedef struct ejoin_stats {
        reserved[1]: 128 x 256 blocks the tensor-core Gram kernel computed
        (each covers up to two of the tile_pairs_run 128 x 128 tile pairs);
        reserved[2]: peak device scratch the call reserved (bytes);
+       reserved[3]: band records the tensor-core Gram kernel wrote (one per row
+       and 32-column chunk with band pairs, 16 bytes each);
        ejoin_train_projection: reserved[0] / [1] = first / last hinge loss. */
     double reserved[5];
 } ejoin_stats;

@@ -97,6 +97,7 @@ class Stats(ctypes.Structure):
         d["exact_rechecks"] = int(self.reserved[0])
         d["gram_blocks"] = int(self.reserved[1])
         d["scratch_peak_bytes"] = int(self.reserved[2])
+        d["band_records"] = int(self.reserved[3])
         return d
 
 

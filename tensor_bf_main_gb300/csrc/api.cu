@@ -377,6 +377,7 @@ static int screen_and_recheck(Join& J, uint64_t cap0, Screen&& screen, Recheck&&
             J.st->band_pairs = pairs;
             J.st->band_hits = h.band_hits;
             J.st->reserved[0] = (double)h.exact_rechecks;
+            J.st->reserved[3] = unit == 2 ? (double)h.band_records : 0.0;
             J.st->ms_gram = tg.ms();
             J.st->ms_recheck = tr.ms();
             return EJOIN_OK;
