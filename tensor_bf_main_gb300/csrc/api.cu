@@ -587,7 +587,8 @@ struct PackedSide {
     uint64_t n_pad = 0;
     DBuf<uint16_t> Q, Aug;
     DBuf<uint8_t> Q8;
-    DBuf<float> beta, cmax, Xf, rad, sig, tsig;
+    DBuf<float> beta, cmax, Xf, rad, sig, tsig, radh;
+    DBuf<uint16_t> Xh;  // FP16 copy of Xf (FP8 screen, rows longer than 64)
     const void* operands(const ScreenParams& P) const {
         return P.fmt == Fmt::E4M3 ? (const void*)Q8.p : (const void*)Q.p;
     }
@@ -608,8 +609,14 @@ static int pack_side(const float* Y32, const float* Yerr, const uint8_t* bad, ui
     if (fp8) {
         EJ_TRY(S.sig.alloc(n_pad, s, "row scales"));
         EJ_TRY(S.tsig.alloc(n_pad / 128, s, "tile scales"));
+        // the wide E4M3 band is first rechecked on FP16 copies (half the
+        // bytes of the FP32 rows); the warp recheck kernel (d > 64) uses them
+        if (P.d > 64) {
+            EJ_TRY(S.Xh.alloc(n_pad * P.d, s, "FP16 coordinates"));
+            EJ_TRY(S.radh.alloc(n_pad, s, "FP16 radii"));
+        }
         EJ_TRY(launch_pack8(Y32, Yerr, n, n_pad, perm, bad, P, S.Q8.p, S.Aug.p, S.beta.p, S.sig.p,
-                            S.Xf.p, S.rad.p, S.tsig.p, s));
+                            S.Xf.p, S.rad.p, S.tsig.p, S.Xh.p, S.radh.p, s));
     } else {
         EJ_TRY(launch_pack16(Y32, Yerr, n, n_pad, perm, bad, P, S.Q.p, S.Aug.p, S.beta.p, S.Xf.p,
                              S.rad.p, s));
@@ -737,6 +744,8 @@ static int run_screen16(Join& J, Fmt fmt, bool split, Learned& L) {
     Recheck32 R;
     R.Xf = R.Xfb = side.Xf.p;
     R.rad = R.radb = side.rad.p;
+    R.Xh = R.Xhb = side.Xh.p;
+    R.radh = R.radhb = side.radh.p;
     R.Xb = J.X;
     R.nb = J.n;
     R.permb = J.perm;
@@ -1124,6 +1133,12 @@ static int cross_join(Join& J, const double* Xq, uint64_t nq, int prec, int32_t*
             R.rad = sq.rad.p;
             R.Xfb = sx.Xf.p;
             R.radb = sx.rad.p;
+            if (sq.Xh.p && sx.Xh.p) {
+                R.Xh = sq.Xh.p;
+                R.radh = sq.radh.p;
+                R.Xhb = sx.Xh.p;
+                R.radhb = sx.radh.p;
+            }
             R.Xb = J.X;
             R.nb = J.n;
             R.permb = nullptr;

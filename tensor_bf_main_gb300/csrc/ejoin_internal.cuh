@@ -204,6 +204,12 @@ struct Recheck32 {
     const float* rad;  // A: per-row radius (|zf - s (x - mu)| bound; inf = undecidable row)
     const float* Xfb;  // B: the same for the second point set
     const float* radb;
+    // optional first pass (wide bands of the FP8 screen): FP16 copies of the
+    // coordinates with their own radius (rad + |zh - zf|); null = none
+    const uint16_t* Xh = nullptr;
+    const float* radh = nullptr;
+    const uint16_t* Xhb = nullptr;
+    const float* radhb = nullptr;
     const double* Xb;  // B: original FP64 rows (the exact chain)
     uint64_t nb;       // B: rows
     const uint32_t* permb;  // B: packed -> original row (null = identity)
@@ -465,7 +471,7 @@ int launch_pack16(const float* Y32, const float* Yerr, uint64_t n, uint64_t n_pa
 int launch_pack8(const float* Y32, const float* Yerr, uint64_t n, uint64_t n_pad,
                  const uint32_t* perm, const uint8_t* bad, const ScreenParams& P, uint8_t* Q,
                  void* Aug, float* beta, float* sig, float* Xf, float* rad, float* tsig,
-                 cudaStream_t s);
+                 uint16_t* Xh, float* radh, cudaStream_t s);
 // per group of 32 rows: max of beta (the band width of a 32-column chunk)
 int launch_chunk_max(const float* beta, uint64_t n_pad, float* cmax, cudaStream_t s);
 

@@ -15,6 +15,8 @@
 // Every chain follows the reference's compiled arithmetic (exact_d2:
 // fma(t0, t0, fl(t1*t1)), then fma(t, t, acc) in index order).  Zero padding
 // of the k loop is exact: fma(0, 0, acc) == acc for acc >= +0.
+#include <cuda_fp16.h>
+
 #include <algorithm>
 
 #include "ejoin_internal.cuh"
@@ -334,10 +336,47 @@ __global__ void __launch_bounds__(256) band_recheck_thread_kernel(const double* 
     recheck_totals(st, hits, exact_runs);
 }
 
+// First decision of a band pair from the FP16 copies (S = their squared
+// distance, computed in FP32 like the FP32 one: the conversions are exact):
+// 1 = in, 0 = out, -1 = undecided.  The copies' radii (rad + |zh - zf|)
+// replace the FP32 radii; otherwise the same directed-rounding tests as
+// recheck_decide.
+__device__ __forceinline__ int decide16(const Recheck32& R, uint32_t i, uint32_t j, float S) {
+    const float rr = __fadd_ru(R.radh[i], R.radhb[j]);
+    const float lo = __fsub_rd(R.f_sTlo, rr);
+    if (lo >= 0.0f && __fadd_ru(S, R.f_abs) <= __fmul_rd(__fmul_rd(lo, lo), R.f_kin)) return 1;
+    const float hi = __fadd_ru(R.f_sThi, rr);
+    if (__fsub_rd(S, R.f_abs) > __fmul_ru(__fmul_ru(hi, hi), R.f_kout)) return 0;
+    return -1;
+}
+
+// 8 FP16 values (16 bytes, p 16-byte aligned): the cached form for the row a
+// warp reuses, the no-allocate form for the gathered one.
+__device__ __forceinline__ uint4 ldg8hc(const uint16_t* p) {
+    uint4 r;
+    asm("ld.global.nc.v4.u32 {%0,%1,%2,%3}, [%4];" : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w) : "l"(p));
+    return r;
+}
+__device__ __forceinline__ uint4 ldg8h(const uint16_t* p) {
+    uint4 r;
+    asm("ld.global.nc.L1::no_allocate.v4.u32 {%0,%1,%2,%3}, [%4];"
+        : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w)
+        : "l"(p));
+    return r;
+}
+__device__ __forceinline__ float sqdiff_h2(uint32_t a, uint32_t b, float S) {
+    const float2 fa = __half22float2(*reinterpret_cast<const __half2*>(&a));
+    const float2 fb = __half22float2(*reinterpret_cast<const __half2*>(&b));
+    const float t0 = fa.x - fb.x, t1 = fa.y - fb.y;
+    return fmaf(t1, t1, fmaf(t0, t0, S));
+}
+
 // Longer rows: a warp takes 32 band pairs; for each pair the lanes stream the
-// two rows (coalesced; with VEC = 8, eight floats per lane and load when d is
+// two rows (coalesced; with VEC = 8, eight values per lane and load when d is
 // a multiple of 256 and the rows are 32-byte aligned) and reduce S across the
-// warp, and lane p then decides pair p.
+// warp, and lane p then decides pair p.  With FP16 copies (R.Xh) a first pass
+// over them decides almost every pair of a wide band at half the bytes; only
+// the pairs it leaves open stream the FP32 rows.
 template <int VEC>
 __global__ void __launch_bounds__(256) band_recheck_warp_kernel(const double* __restrict__ X,
                                                                 uint32_t d,
@@ -357,12 +396,48 @@ __global__ void __launch_bounds__(256) band_recheck_warp_kernel(const double* __
         if (e < nband) bp = band[e];
         const uint32_t mi = bp.i, mj = bp.j & ~kBandBoth;
         const bool valid = e < nband && mi < n && mj < R.nb;
+        bool open = valid, hit = false;
+        if (R.Xh) {
+            float mh = 0.0f;
+            for (uint32_t q = 0; q < 32; ++q) {
+                const uint32_t i = __shfl_sync(0xffffffffu, mi, q);
+                const uint32_t j = __shfl_sync(0xffffffffu, mj, q);
+                const bool v = __shfl_sync(0xffffffffu, valid, q);
+                if (!v) continue;  // warp-uniform
+                const uint16_t* a = R.Xh + (uint64_t)i * d;
+                const uint16_t* b = R.Xhb + (uint64_t)j * d;
+                float S = 0.0f;
+                if (VEC == 8) {
+                    for (uint32_t c = 8 * lane; c < d; c += 256) {
+                        const uint4 u = ldg8hc(a + c), w = ldg8h(b + c);
+                        S = sqdiff_h2(u.x, w.x, S);
+                        S = sqdiff_h2(u.y, w.y, S);
+                        S = sqdiff_h2(u.z, w.z, S);
+                        S = sqdiff_h2(u.w, w.w, S);
+                    }
+                } else {
+                    for (uint32_t c = lane; c < d; c += 32) {
+                        const float t = __half2float(__ushort_as_half(a[c])) -
+                                        __half2float(__ushort_as_half(b[c]));
+                        S = fmaf(t, t, S);
+                    }
+                }
+                for (int o = 16; o; o >>= 1) S += __shfl_xor_sync(0xffffffffu, S, o);
+                if (lane == q) mh = S;
+            }
+            if (valid) {
+                const int dec = decide16(R, mi, mj, mh);
+                if (dec >= 0) {
+                    open = false;
+                    hit = dec == 1;
+                }
+            }
+        }
         float mine = 0.0f;
-        for (uint32_t q = 0; q < 32; ++q) {
+        for (uint32_t left = __ballot_sync(0xffffffffu, open); left; left &= left - 1) {
+            const uint32_t q = __ffs(left) - 1;
             const uint32_t i = __shfl_sync(0xffffffffu, mi, q);
             const uint32_t j = __shfl_sync(0xffffffffu, mj, q);
-            const bool v = __shfl_sync(0xffffffffu, valid, q);
-            if (!v) continue;  // warp-uniform
             const float* a = R.Xf + (uint64_t)i * d;
             const float* b = R.Xfb + (uint64_t)j * d;
             float S = 0.0f;
@@ -386,7 +461,8 @@ __global__ void __launch_bounds__(256) band_recheck_warp_kernel(const double* __
             for (int o = 16; o; o >>= 1) S += __shfl_xor_sync(0xffffffffu, S, o);
             if (lane == q) mine = S;
         }
-        if (valid && recheck_decide(X, d, perm, T, R, mi, mj, mine, exact_runs)) {
+        if (open) hit = recheck_decide(X, d, perm, T, R, mi, mj, mine, exact_runs);
+        if (hit) {
             atomicAdd(&counts[mi], 1);
             if (bp.j & kBandBoth) atomicAdd(&counts[mj], 1);
             emit_pair(em, bp);

@@ -564,12 +564,13 @@ __global__ void __launch_bounds__(256) pack8_kernel(const float* __restrict__ Y3
                                                     const uint8_t* __restrict__ bad,
                                                     const float* __restrict__ Yerr, ScreenParams P,
                                                     uint8_t* Q, uint16_t* Aug, float* beta,
-                                                    float* sig, float* Xf, float* rad) {
+                                                    float* sig, float* Xf, float* rad,
+                                                    uint16_t* Xh, float* radh) {
     const uint64_t p0 = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / 32 * 32;
     const uint32_t lane = threadIdx.x & 31;
     if (p0 >= n_pad) return;
     const float mnf = 0.015625f;  // E4M3 smallest normal 2^-6
-    float m_nq = 0, m_e2 = 0, m_sig = 1.0f;
+    float m_nq = 0, m_e2 = 0, m_eh = 0, m_sig = 1.0f;
     uint64_t m_src = 0;
     bool m_good = false;
     for (uint32_t r = 0; r < 32; ++r) {
@@ -598,7 +599,7 @@ __global__ void __launch_bounds__(256) pack8_kernel(const float* __restrict__ Y3
             sgm = ldexpf(1.0f, e);
         }
         const float inv = 1.0f / sgm;  // exact (power of two)
-        float nq = 0, e2 = 0;
+        float nq = 0, e2 = 0, eh = 0;
         uint8_t* row = Q + p * (uint64_t)P.width;
 #pragma unroll
         for (int t = 0; t < PACK8_MAXV; ++t) {
@@ -611,15 +612,26 @@ __global__ void __launch_bounds__(256) pack8_kernel(const float* __restrict__ Y3
             nq = __fmaf_rn(q, q, nq);
             e2 = __fmaf_ru(ef, ef, e2);
             row[k] = (uint8_t)__nv_cvt_float_to_fp8(f, __NV_SATFINITE, __NV_E4M3);
-            if (k < P.d) Xf[p * P.d + k] = zf;
+            if (k < P.d) {
+                Xf[p * P.d + k] = zf;
+                if (Xh) {
+                    // |zf| <= 1 (the scale): no overflow; zf - zh is exact
+                    const __half hv = __float2half_rn(zf);
+                    const float dh = zf - __half2float(hv);
+                    eh = __fmaf_ru(dh, dh, eh);
+                    Xh[p * P.d + k] = __half_as_ushort(hv);
+                }
+            }
         }
         for (int o = 16; o; o >>= 1) {
             nq = __fadd_rn(nq, __shfl_xor_sync(0xffffffffu, nq, o));
             e2 = __fadd_ru(e2, __shfl_xor_sync(0xffffffffu, e2, o));
+            eh = __fadd_ru(eh, __shfl_xor_sync(0xffffffffu, eh, o));
         }
         if (lane == r) {
             m_nq = nq;
             m_e2 = e2;
+            m_eh = eh;
             m_src = src;
             m_sig = sgm;
             m_good = good;
@@ -688,6 +700,8 @@ __global__ void __launch_bounds__(256) pack8_kernel(const float* __restrict__ Y3
     beta[p] = m_good ? __double2float_ru(b) : 0.0f;
     sig[p] = m_good ? m_sig : INFINITY;  // padding / bad rows do not lower a tile's minimum
     rad[p] = radius;
+    // radius of the FP16 copy: |zh - z| <= |zh - zf| + |zf - z| (rounded up)
+    if (radh) radh[p] = __fadd_ru(radius, __fsqrt_ru(m_eh));
 }
 
 // per 128-row tile: min sigma of its rows (1 for a tile without finite rows)
@@ -889,11 +903,12 @@ int launch_pack16(const float* Y32, const float* Yerr, uint64_t n, uint64_t n_pa
 int launch_pack8(const float* Y32, const float* Yerr, uint64_t n, uint64_t n_pad,
                  const uint32_t* perm, const uint8_t* bad, const ScreenParams& P, uint8_t* Q,
                  void* Aug, float* beta, float* sig, float* Xf, float* rad, float* tsig,
-                 cudaStream_t s) {
+                 uint16_t* Xh, float* radh, cudaStream_t s) {
     if (n_pad % 128) return set_error(EJOIN_EINTERNAL, "pack8: rows not padded");
     if (P.d > 32u * PACK8_MAXV) return set_error(EJOIN_EUNSUPPORTED, "FP8 screen supports d <= %d", 32 * PACK8_MAXV);
     pack8_kernel<<<(unsigned)((n_pad + 255) / 256), 256, 0, s>>>(Y32, n, n_pad, perm, bad, Yerr, P,
-                                                                 Q, (uint16_t*)Aug, beta, sig, Xf, rad);
+                                                                 Q, (uint16_t*)Aug, beta, sig, Xf, rad,
+                                                                 Xh, radh);
     EJ_CUDA(cudaGetLastError());
     note_launch();
     tile_min_sigma_kernel<<<(unsigned)(n_pad / 128), 128, 0, s>>>(sig, n_pad / 128, tsig);
