@@ -41,8 +41,9 @@
 //    the all-out fast path), packs sign bits with one funnel shift per
 //    element, counts rows with popc, transposes 32x32 bit blocks across the
 //    warp to count columns (off-diagonal tiles credit both points), and a
-//    flusher warp adds the per-block counts to global memory.  No distance
-//    reaches global memory.
+//    flusher warp adds the per-block counts to global memory.  A block's
+//    counting comes before the wait for the next block's accumulator.  No
+//    distance reaches global memory.
 //
 // Every wait is bounded (umma_ptx.cuh); on expiry all roles stop, in-flight
 // copies and MMAs are drained (bounded) and tensor memory is freed.
@@ -505,34 +506,31 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         Margins mc = load_margins(w);
         float W0 = width(mc, 0), W1 = width(mc, 1);
         auto is_active = [&](uint2 e) { return e.x != 0xffffffffu && ((e_mask(e) >> h) & 1u); };
-        // Software pipeline: the first 32-column chunk of block idx + 1 is
-        // loaded from tensor memory before the counting work of block idx, so
-        // the load's latency hides behind that work.  v holds the chunk in
-        // flight; nothing reads it before tmem_ld_wait_regs.
+        // Per block: wait for the accumulator, load and classify the two
+        // 32-column chunks (one at a time, 32 live values), release the
+        // accumulator, then count and stage band records before waiting for
+        // the next block.  A tensor-memory load takes a few tens of cycles,
+        // so nothing is gained by loading ahead; counting first keeps the
+        // counting of one block from waiting on the next block's MMAs
+        // (measured: that wait, placed before the counting, held the
+        // epilogue a block behind the MMAs).
         uint32_t v[32];
         float mx = 0.0f;
         const uint32_t tq = tmem + ((q * 32u) << 16) + cg * 64u;
-        bool run = item_at(0, a.lrun) < a.nwork;
-        if (run) {
-            run = ptx::mbar_wait(&S.tfull[0], 0u, a.st, 30);
-            if (run) {
-                ptx::tc_fence_after();
-                if (is_active(w)) ptx::tmem_ld_max_32x32b_x32(tq, v, mx);
-            }
-        }
-        for (uint64_t idx = 0; run; ++idx, ++it) {
+        for (uint64_t idx = 0; item_at(idx, a.lrun) < a.nwork; ++idx, ++it) {
             const uint32_t b = it & 1u, use = it >> 1;
             const uint2 wnn = entry_or_end(a, item_at(idx + 2, a.lrun));
             const Margins mn = load_margins(wn);
             const uint32_t I = e_row(w), J = e_col(w, h);
             const bool active = is_active(w);
             const bool diag = a.cross || (I == J);  // credit rows only
-            // the two 32-column chunks one after the other (32 live values);
-            // the accumulator is released after the second load
             const uint32_t taddr = tq + b * ACC_COLS;
             uint32_t in0 = 0, bd0 = 0, in1 = 0, bd1 = 0;
             bool busy0 = false, busy1 = false;
+            if (!ptx::mbar_wait(&S.tfull[b], use & 1u, a.st, 30)) break;
+            ptx::tc_fence_after();
             if (active) {
+                ptx::tmem_ld_max_32x32b_x32(taddr, v, mx);
                 ptx::tmem_ld_wait_regs(v, mx);
                 busy0 = classify(v, mx, W0, in0, bd0);
                 ptx::tmem_ld_max_32x32b_x32(taddr + 32u, v, mx);
@@ -542,14 +540,6 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             __syncwarp();
             if (lane == 0) ptx::mbar_arrive(&S.tempty[b]);
             if (active) busy1 = classify(v, mx, W1, in1, bd1);
-            // next block: wait for its accumulator, start its first load
-            const bool more = item_at(idx + 1, a.lrun) < a.nwork;
-            if (more) {
-                const uint32_t bn = (it + 1) & 1u, usen = (it + 1) >> 1;
-                if (!ptx::mbar_wait(&S.tfull[bn], usen & 1u, a.st, 31)) break;
-                ptx::tc_fence_after();
-                if (is_active(wn)) ptx::tmem_ld_max_32x32b_x32(tq + bn * ACC_COLS, v, mx);
-            }
             // the counts of buffer b were flushed and cleared for block it - 2
             if (!ptx::mbar_wait(&S.fdone[b], (use & 1u) ^ 1u, a.st, 32)) break;
             if (busy0 || busy1) {
@@ -572,11 +562,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             W1 = width(mn, 1);
             w = wn;
             wn = wnn;
-            run = more;
         }
-        // a load still in flight (a wait that gave up) completes before the
-        // tensor memory is freed
-        ptx::tmem_ld_wait_regs(v, mx);
     } else {
         // ------------------------------------------------ count flusher
         // adds the per-block row / column counts to global memory and clears
