@@ -127,6 +127,7 @@ struct Ctl {
     int rowacc[2][128];
     int colacc[2][256];
     uint32_t band_n[2];                  // band entries staged for buffer b
+    uint32_t has_counts[2];              // some epilogue warp added counts to buffer b
     BandRec band_buf[2][BAND_SMEM];      // staged band records (flushed by the flusher warp)
 };
 
@@ -300,7 +301,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         if (i < 256) (&S.rowacc[0][0])[i] = 0;
         else (&S.colacc[0][0])[i - 256] = 0;
     }
-    if (threadIdx.x < 2) S.band_n[threadIdx.x] = 0;
+    if (threadIdx.x < 2) {
+        S.band_n[threadIdx.x] = 0;
+        S.has_counts[threadIdx.x] = 0;
+    }
     ptx::tc_fence_before();
     __syncthreads();
     ptx::tc_fence_after();
@@ -554,6 +558,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 }
                 const int rowcnt = __popc(in0) + __popc(in1);
                 if (rowcnt) atomicAdd(&racc[q * 32u + lane], rowcnt);
+                // the flusher skips the count arrays of blocks without in-pairs
+                // (every lane takes part in the vote)
+                const bool any_in = __any_sync(FULL, rowcnt != 0);
+                if (lane == 0 && any_in) S.has_counts[b] = 1u;
                 if (a.em.cnt) emit_in(a, in0, in1, row, col0, diag, lane);
             }
             __syncwarp();
@@ -576,6 +584,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         static_assert(kResChunk >= BAND_SMEM, "a block's records fit one new chunk");
         unsigned long long rbase = 0;
         uint32_t rleft = 0;
+        // pairs (per lane) and records of the staged band records, added to
+        // the status once at the end (two contended global atomics per block
+        // otherwise)
+        unsigned long long np_acc = 0, nrec_acc = 0;
         uint32_t it = 0;
         uint2 wnext = entry_or_end(a, item_at(0, a.lrun));
         for (uint64_t idx = 0;; ++idx, ++it) {
@@ -587,19 +599,32 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             int* racc = S.rowacc[b];
             int* cacc = S.colacc[b];
             const uint32_t col_a = e_col(w, 0) * 128u, col_b = e_col(w, 1) * 128u;
+            // counts: only blocks with in-pairs wrote any (a column count
+            // implies a row count), and only nonzero entries are cleared
+            if (S.has_counts[b]) {
+                int rv[4], cv[8];
 #pragma unroll
-            for (int e = 0; e < 4; ++e) {
-                const uint32_t r = lane + 32 * e;
-                const int rv = racc[r];
-                if (rv) atomicAdd(&a.counts[e_row(w) * 128u + r], rv);
-                racc[r] = 0;
-            }
+                for (int e = 0; e < 4; ++e) rv[e] = racc[lane + 32 * e];
 #pragma unroll
-            for (int e = 0; e < 8; ++e) {
-                const uint32_t c = lane + 32 * e;
-                const int cv = cacc[c];
-                if (cv) atomicAdd(&a.counts[(c < 128u ? col_a : col_b - 128u) + c], cv);
-                cacc[c] = 0;
+                for (int e = 0; e < 8; ++e) cv[e] = cacc[lane + 32 * e];
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    const uint32_t r = lane + 32 * e;
+                    if (rv[e]) {
+                        atomicAdd(&a.counts[e_row(w) * 128u + r], rv[e]);
+                        racc[r] = 0;
+                    }
+                }
+#pragma unroll
+                for (int e = 0; e < 8; ++e) {
+                    const uint32_t c = lane + 32 * e;
+                    if (cv[e]) {
+                        atomicAdd(&a.counts[(c < 128u ? col_a : col_b - 128u) + c], cv[e]);
+                        cacc[c] = 0;
+                    }
+                }
+                __syncwarp();
+                if (lane == 0) S.has_counts[b] = 0u;
             }
             // staged band records of this block: one global reservation, coalesced
             // copy, and their pair count
@@ -613,18 +638,13 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                     if (lane == 0) nbase = atomicAdd(&a.st->band_count, (unsigned long long)kResChunk);
                     nbase = __shfl_sync(FULL, nbase, 0);
                 }
-                uint32_t np = 0;
                 for (uint32_t e = lane; e < nst; e += 32) {
                     const BandRec r = S.band_buf[b][e];
-                    np += __popc(r.mask);
+                    np_acc += __popc(r.mask);
                     const unsigned long long g = e < rleft ? rbase + e : nbase + (e - rleft);
                     if (g < a.band_cap) a.band[g] = r;
                 }
-                np = __reduce_add_sync(FULL, np);
-                if (lane == 0) {
-                    atomicAdd(&a.st->band_pairs, (unsigned long long)np);
-                    atomicAdd(&a.st->band_records, (unsigned long long)nst);
-                }
+                nrec_acc += nst;
                 if (grow) {
                     rbase = nbase + (nst - rleft);
                     rleft = kResChunk - (nst - rleft);
@@ -641,6 +661,12 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         // empty records in the unused tail of the last reserved chunk
         for (uint32_t e = lane; e < rleft; e += 32)
             if (rbase + e < a.band_cap) a.band[rbase + e] = BandRec{0u, 0u, 0u, 0u};
+#pragma unroll
+        for (int o = 16; o; o >>= 1) np_acc += __shfl_xor_sync(FULL, np_acc, o);
+        if (lane == 0 && nrec_acc) {
+            atomicAdd(&a.st->band_pairs, np_acc);
+            atomicAdd(&a.st->band_records, nrec_acc);
+        }
     }
 
     ptx::tc_fence_before();
