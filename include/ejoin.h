@@ -71,7 +71,7 @@ typedef struct ejoin_options {
     uint64_t ld;              /* row stride of `points` in elements (0 = d) */
     const float* projection;  /* optional host k x d projection to reuse (skips
                                  training); its spectral norm is re-certified */
-    uint64_t train_pairs;     /* pairs sampled for training (default 1<<20) */
+    uint64_t train_pairs;     /* pairs sampled for training (default 1<<19) */
     uint32_t train_steps;     /* optimiser steps (default 50: longer training lowers the
                                  hinge loss but not the number of pruned tile pairs) */
     uint32_t order;           /* ejoin_order (default MORTON) */

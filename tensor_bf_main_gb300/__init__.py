@@ -179,7 +179,7 @@ def _check(rc: int):
 
 
 def _options(device=0, precision=Precision.AUTO, proj_k=0, ld=0, projection=None,
-             train_pairs=1 << 20, train_steps=50, order=Order.MORTON, seed=0x5EED5EED,
+             train_pairs=1 << 19, train_steps=50, order=Order.MORTON, seed=0x5EED5EED,
              stream=None, band_capacity=0, acc_bound_scale=1.0, keep_scratch=False):
     o = Options()
     _check(load_library().ejoin_default_options(ctypes.byref(o)))

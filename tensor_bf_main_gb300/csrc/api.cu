@@ -764,10 +764,11 @@ static int run_screen16(Join& J, Fmt fmt, bool split, Learned& L) {
         return launch_band_recheck2(J.X, J.n, J.d, J.perm, J.T, R, pairs.p, npairs, J.counts, st,
                                     J.em, J.s);
     };
-    // First queue: sized from a systematic sample of the blocks (every 64th,
-    // counting records only) when the list could produce more records than
-    // the minimum queue; an overflow re-runs the whole screen with the exact
-    // size.  (A block produces at most 128 rows x 8 chunks = 1024 records.)
+    // First queue: sized from a systematic sample of the blocks (every
+    // stride-th, about 8,192 of them, stride 64 to 256; counting records
+    // only) when the list could produce more records than the minimum queue;
+    // an overflow re-runs the whole screen with the exact size.  (A block
+    // produces at most 128 rows x 8 chunks = 1024 records.)
     uint64_t cap_rec = 1u << 22;
     if (!J.opt.band_capacity && nwork * 1024 > cap_rec) {
         EventTimer te;
@@ -775,7 +776,7 @@ static int run_screen16(Join& J, Fmt fmt, bool split, Learned& L) {
         DBuf<uint2> sw;
         DBuf<DevStatus> est;
         uint64_t ns = 0;
-        const uint64_t stride = 64;
+        const uint64_t stride = std::min<uint64_t>(256, std::max<uint64_t>(64, nwork / 8192));
         EJ_TRY(sample_worklist(work.p, nwork, stride, sw, &ns, J.s));
         EJ_TRY(est.alloc(1, J.s, "band estimate"));
         EJ_TRY(est.zero(J.s));
@@ -1001,7 +1002,7 @@ int ejoin_default_options(ejoin_options* opt) {
     opt->device = 0;
     opt->precision = EJOIN_AUTO;
     opt->proj_k = 0;
-    opt->train_pairs = 1u << 20;
+    opt->train_pairs = 1u << 19;
     opt->train_steps = 50;
     opt->order = EJOIN_ORDER_MORTON;
     opt->seed = 0x5eed5eedull;

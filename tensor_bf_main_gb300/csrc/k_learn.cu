@@ -935,7 +935,7 @@ int train_projection_dev(const float* Y32, const uint8_t* bad, uint64_t n, uint3
     DBuf<unsigned int> done;  // blocks finished per step (the fused Adam step)
     EJ_TRY(done.alloc(1, s, "step counter"));
     EJ_TRY(done.zero(s));
-    const uint64_t M = std::max<uint64_t>(pairs ? pairs : (1u << 20), 256);
+    const uint64_t M = std::max<uint64_t>(pairs ? pairs : (1u << 19), 256);
     const uint64_t B = std::min<uint64_t>(M, 65536);  // minibatch
     DBuf<float> V, tgt;
     EJ_TRY(V.alloc(M * d, s, "training pair differences"));
