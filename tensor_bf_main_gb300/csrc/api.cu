@@ -577,6 +577,9 @@ static ScreenParams screen_params(Fmt fmt, bool split, uint32_t d, double maxabs
     P.cacc_l = split ? scale_opt * 128.0 * ldexp(1.0, -22) : 0.0;
     P.cacc_al = scale_opt * 32.0 * ldexp(1.0, -22);
     P.absacc = (kprod + 16.0) * ldexp(1.0, -125);
+    P.inv_in_pos = nextafter(1.0 / (2.0 * (1.0 - P.cacc_al)), INFINITY);
+    P.inv_in_neg = nextafter(1.0 / (2.0 * (1.0 + P.cacc_al)), 0.0);
+    P.flush_err = nextafter(ldexp(1.0, -126) * sqrt((double)d), INFINITY);
     P.clamp_lo = (fmt == Fmt::FP16) ? -16384.0 : -kTwo100;
     *kprod_out = kprod;
     return P;

@@ -295,6 +295,9 @@ struct ScreenParams {
     // 2 e_i = acc_margin2(a_i^2, l_i^2) + 2 cacc_al |alpha_i| (api.cu: screen_params)
     double cacc_a, cacc_l, cacc_al;
     double absacc;     // absolute bound (FP32 underflow) of the same
+    double inv_in_pos; // 1 / (2 (1 - cacc_al)) rounded up
+    double inv_in_neg; // 1 / (2 (1 + cacc_al)) rounded down
+    double flush_err;  // 2^-126 sqrt(d) rounded up: coordinates flushed below FP32 range
     double clamp_lo;   // smallest alpha the operand format can carry
     uint32_t d, dp;    // coordinates, padded coordinates (per slab multiple)
     uint32_t width;    // packed row width in elements (dp, or 2 dp with the split)

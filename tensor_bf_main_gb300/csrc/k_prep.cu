@@ -494,13 +494,18 @@ __global__ void __launch_bounds__(256) pack16_kernel(const float* __restrict__ Y
         // distance of the FP32 coordinates from the exact scaled centred point:
         // the centring bound (exact scaling) plus values flushed below 2^-126
         const double zerr = ((double)__ldg(&Yerr[m_src]) * P.scale +
-                             1.1754943508222875e-38 * sqrt((double)P.d)) * (1 + 4 * kU);
-        const double rho = (sqrt((double)m_e2) * (1 + 1e-7) + zerr) * (1 + 8 * kU);
+                             P.flush_err) * (1 + 4 * kU);
+        // FP32 square root rounded up: an upper bound, without an FP64 square
+        // root (FP64 runs at a small fraction of FP32 on GB300)
+        const double rho = ((double)__fsqrt_ru(m_e2) * (1 + 1e-7) + zerr) * (1 + 8 * kU);
         radius = __double2float_ru(zerr);
         const double m2 = acc_margin2(P, a2u, lu);
         double R = nup + m2 + lu + P.absacc - 0.5 * P.Tlo + 2.0 * P.sTlo * rho;
         R += 12 * kU * (nup + m2 + lu + P.absacc + 0.5 * P.Tlo + 2.0 * P.sTlo * rho);
-        double at = R >= 0 ? R / (2.0 * (1.0 - P.cacc_al)) : R / (2.0 * (1.0 + P.cacc_al));
+        // R / (2 (1 -/+ cacc_al)) as a product with reciprocals rounded towards
+        // a larger alpha on the host; the margin below covers the product's
+        // rounding
+        double at = R * (R >= 0 ? P.inv_in_pos : P.inv_in_neg);
         at += fabs(at) * 4 * kU;
         at = fmax(at, P.clamp_lo);
         ah[0] = round_fmt(at, fi);
@@ -649,13 +654,18 @@ __global__ void __launch_bounds__(256) pack8_kernel(const float* __restrict__ Y3
         const double ndn = (double)m_nq * (1 - nb.rel) - nb.abs;
         const double a2u = nup;  // |(|q|)|^2 = |q|^2
         const double zerr = ((double)__ldg(&Yerr[m_src]) * P.scale +
-                             1.1754943508222875e-38 * sqrt((double)P.d)) * (1 + 4 * kU);
-        const double rho = (sqrt((double)m_e2) * (1 + 1e-7) + zerr) * (1 + 8 * kU);
+                             P.flush_err) * (1 + 4 * kU);
+        // FP32 square root rounded up: an upper bound, without an FP64 square
+        // root (FP64 runs at a small fraction of FP32 on GB300)
+        const double rho = ((double)__fsqrt_ru(m_e2) * (1 + 1e-7) + zerr) * (1 + 8 * kU);
         radius = __double2float_ru(zerr);
         const double m2 = acc_margin2(P, a2u, 0.0);
         double R = nup + m2 + P.absacc - 0.5 * P.Tlo + 2.0 * P.sTlo * rho;
         R += 12 * kU * (nup + m2 + P.absacc + 0.5 * P.Tlo + 2.0 * P.sTlo * rho);
-        double at = R >= 0 ? R / (2.0 * (1.0 - P.cacc_al)) : R / (2.0 * (1.0 + P.cacc_al));
+        // R / (2 (1 -/+ cacc_al)) as a product with reciprocals rounded towards
+        // a larger alpha on the host; the margin below covers the product's
+        // rounding
+        double at = R * (R >= 0 ? P.inv_in_pos : P.inv_in_neg);
         at += fabs(at) * 4 * kU;
         rsig = 1.0 / (double)m_sig;  // exact
         double as = fmax(at * rsig, -kTwo100);  // alpha / sigma, clamped upwards (safe)
