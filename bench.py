@@ -22,7 +22,7 @@ are timed on the same GPU by the default arm and reported in its line under
 "reference_gpu".
 
 With --gpus N under torchrun every rank runs an independent replica
-(replicas only: the spec path is single-GPU) and rank 0 reports the
+(replicas only: the join runs on one GPU) and rank 0 reports the
 whole-job rate.
 """
 from __future__ import annotations

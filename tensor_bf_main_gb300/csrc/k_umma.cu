@@ -467,7 +467,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         const uint32_t cg = ew >> 2;           // 64-column group
         const uint32_t h = cg >> 1;            // half
         uint32_t it = 0;
-        // band width of row i against column tile J: W >= beta_i + beta_j
+        // band width of row i against a 32-column chunk K of column tile J:
+        // W >= beta_i + max beta over K >= beta_i + beta_j for every j in K
         // (Gram units; FP8 operands: divided by sigma_i sigma_J,min, the
         // accumulator's unit for pair (i, j) being 1 / (sigma_i sigma_j)); the
         // sum is rounded up by the 2^-20 relative margin, division by the
