@@ -2,7 +2,7 @@
 
 Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU legs of ``bench.py``
 (``cpu_baseline`` and ``--impl reference``) may import this package.  It is
-the checker the CUDA path is compared with, never part of the product.
+the oracle the CUDA path is compared with, never part of the product.
 
 ``oracle.c`` restates the reference's FP64 CUDA-core join
 (kernel_join.cu:168-200) and its loader (dataset.cu:10-39); see the header of

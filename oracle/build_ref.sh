@@ -1,5 +1,5 @@
 #!/bin/sh
-# Builds checkers from the reference's own sources, where they lie, into
+# Builds test oracles from the reference's own sources, where they lie, into
 # oracle/_ref/ (git-ignored).  Test and measurement infrastructure only; run in
 # the container that has the reference checkout.
 #

@@ -1,5 +1,5 @@
 """CPU restatement of the learned projection's training arithmetic --
-TEST INFRASTRUCTURE ONLY (the checker of the GPU training kernels).
+TEST INFRASTRUCTURE ONLY (the oracle of the GPU training kernels).
 
 The learned pruning has no reference counterpart; this file restates, in
 FP64 numpy, the loss and gradient the training kernel (k_learn.cu,

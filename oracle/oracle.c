@@ -1,7 +1,7 @@
 /*
  * oracle.c -- CPU restatement of the reference's brute-force epsilon self-join.
  *
- * TEST INFRASTRUCTURE ONLY.  This file is the checker: the parity tests,
+ * TEST INFRASTRUCTURE ONLY.  This file is the oracle: the parity tests,
  * __graft_entry__.smoke() and the cpu_baseline / reference legs of bench.py
  * load it.  The product (libejoin.so) never links, loads or calls it.
  *
