@@ -406,10 +406,16 @@ __global__ void __launch_bounds__(256) pack16_kernel(const float* __restrict__ Y
     float m_nq = 0, m_e2 = 0, m_a2 = 0, m_l2 = 0;
     uint64_t m_src = 0;
     bool m_good = false;
+    // the warp's 32 source rows and their flags, loaded once (lane r: row
+    // p0 + r) and handed out by shuffles, so that no index load sits in
+    // front of each row's gather
+    const uint64_t pl = p0 + lane;
+    const uint64_t src_l = pl < n ? (perm ? perm[pl] : pl) : 0;
+    const uint32_t good_l = (pl < n && !bad[src_l]) ? 1u : 0u;
     for (uint32_t it = 0; it < 16; ++it) {
         const uint64_t p = p0 + 2 * it + hw;
-        const uint64_t src = p < n ? (perm ? perm[p] : p) : 0;
-        const bool good = p < n && !bad[src];
+        const uint64_t src = __shfl_sync(0xffffffffu, src_l, 2 * it + hw);
+        const bool good = __shfl_sync(0xffffffffu, good_l, 2 * it + hw) != 0u;
         uint16_t* row = Q + p * (uint64_t)P.width;
         float nq = 0, e2 = 0, a2 = 0, l2 = 0;
         for (uint32_t k0 = 4 * l; k0 < P.dp; k0 += 64) {
@@ -578,10 +584,14 @@ __global__ void __launch_bounds__(256) pack8_kernel(const float* __restrict__ Y3
     float m_nq = 0, m_e2 = 0, m_eh = 0, m_sig = 1.0f;
     uint64_t m_src = 0;
     bool m_good = false;
+    // the warp's 32 source rows and their flags, loaded once and shuffled
+    const uint64_t pl = p0 + lane;
+    const uint64_t src_l = pl < n ? (perm ? perm[pl] : pl) : 0;
+    const uint32_t good_l = (pl < n && !bad[src_l]) ? 1u : 0u;
     for (uint32_t r = 0; r < 32; ++r) {
         const uint64_t p = p0 + r;
-        const uint64_t src = p < n ? (perm ? perm[p] : p) : 0;
-        const bool good = p < n && !bad[src];
+        const uint64_t src = __shfl_sync(0xffffffffu, src_l, r);
+        const bool good = __shfl_sync(0xffffffffu, good_l, r) != 0u;
         float zv[PACK8_MAXV];
         float mx = 0.0f;
 #pragma unroll
