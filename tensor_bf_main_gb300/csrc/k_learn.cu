@@ -628,15 +628,20 @@ __global__ void __launch_bounds__(TRAIN_THREADS) train_step_kernel(float* P, uin
     const uint32_t TP = train_tile_pairs(d);
     const uint32_t pitch = d + 1;
     const uint32_t Q = train_slices(d, K);
-    float* sPT = sm;               // d * K, P transposed, zero beyond k
+    // P transposed as K/4 planes of float4 (plane a4, column c: rows 4 a4 ..
+    // 4 a4 + 3 of column c), zero beyond k: lanes that read different columns
+    // (warp per pair) hit consecutive 16-byte words, conflict-free, and
+    // threads that read one column (thread per pair) get a broadcast
+    float* sPT = sm;
     float* sG = sPT + K * d;       // K * d: this block's gradient partial
     float* sV = sG + K * d;        // TP * pitch (also the backward partials)
     float* sC = sV + train_tile_floats(d);  // TP * K coefficients (16-byte aligned)
     for (uint32_t e = threadIdx.x; e < K * d; e += blockDim.x) {
-        const uint32_t c = e / K, a = e % K;
+        const uint32_t t = e / 4, c = t % d, a = 4 * (t / d) + e % 4;
         sPT[e] = a < k ? P[a * d + c] : 0.0f;
         sG[e] = 0.0f;
     }
+    const float4* sPT4 = reinterpret_cast<const float4*>(sPT);
     const float invM = 1.0f / (float)M;
     float lsum = 0.0f;
     for (uint64_t base = blockIdx.x * (uint64_t)TP; base < M; base += (uint64_t)gridDim.x * TP) {
@@ -679,10 +684,9 @@ __global__ void __launch_bounds__(TRAIN_THREADS) train_step_kernel(float* P, uin
                     const float* v = sV + p * pitch;
                     for (uint32_t c = 0; c < d; ++c) {
                         const float vc = v[c];
-                        const float4* pt = reinterpret_cast<const float4*>(sPT + c * K);
 #pragma unroll
                         for (int a4 = 0; a4 < K / 4; ++a4) {
-                            const float4 w = pt[a4];
+                            const float4 w = sPT4[a4 * d + c];
                             y[4 * a4 + 0] = fmaf(w.x, vc, y[4 * a4 + 0]);
                             y[4 * a4 + 1] = fmaf(w.y, vc, y[4 * a4 + 1]);
                             y[4 * a4 + 2] = fmaf(w.z, vc, y[4 * a4 + 2]);
@@ -713,10 +717,9 @@ __global__ void __launch_bounds__(TRAIN_THREADS) train_step_kernel(float* P, uin
                     const float* v = sV + p * pitch;
                     for (uint32_t c = lane; c < d; c += 32) {
                         const float vc = v[c];
-                        const float4* pt = reinterpret_cast<const float4*>(sPT + c * K);
 #pragma unroll
                         for (int a4 = 0; a4 < K / 4; ++a4) {
-                            const float4 w = pt[a4];
+                            const float4 w = sPT4[a4 * d + c];
                             y[4 * a4 + 0] = fmaf(w.x, vc, y[4 * a4 + 0]);
                             y[4 * a4 + 1] = fmaf(w.y, vc, y[4 * a4 + 1]);
                             y[4 * a4 + 2] = fmaf(w.z, vc, y[4 * a4 + 2]);
