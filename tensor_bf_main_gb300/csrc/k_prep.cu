@@ -297,10 +297,6 @@ __device__ __forceinline__ uint16_t to_bits16(double r, Fmt f) {
     return __half_as_ushort(__float2half_rn(x));
 }
 
-__device__ __forceinline__ uint8_t to_bits8(double r) {
-    return (uint8_t)__nv_cvt_float_to_fp8((float)r, __NV_SATFINITE, __NV_E4M3);
-}
-
 // ------------------------------------------------------------ DMMA pack --
 
 __global__ void pack_dmma_kernel(const double* __restrict__ X, uint64_t n, uint64_t n_pad,
